@@ -1,0 +1,128 @@
+/*
+ * ucfdlusgs.h -- FlowSys LU-SGS / block LU-SGS API of libucfd_gb300.so.
+ *
+ * Drop-in for the reference header src/lusgs/include/ucfdlusgs.h:5-40:
+ * same handle type, function names, argument order and array layouts.
+ *   rowptr/colidx/slots/sides  rank-level CSR over faces (flowsys.h:34-59)
+ *   face_area [nfaces], face_normal [ndims][nfaces], rcp_vol [nlocal]
+ *   element arrays (SetElement): uptsb, rhs, dsrc, resid_out [nvars][neles];
+ *   dt, vol [neles]; cell_ids [neles] maps element -> rank cell
+ *   LU-SGS fspr/tfspr [nfaces]; BLU-SGS jmat [2][nfvars][nfvars][nfaces],
+ *   tjmat [2][nturb][nturb][nfaces]
+ *
+ * Sweep semantics are the reference's natural-order Gauss-Seidel
+ * (lusgs.c:157-257, blusgs.c:273-373).  On the GPU the rank cells are
+ * processed level by level: level(i) = 1 + max level of i's lower-indexed
+ * neighbours, so every cell sees exactly the neighbour values the
+ * sequential sweep would show it and the result is the sequential one.
+ * UCFDFlowSysSetColoring replaces natural order by a colour order (the
+ * colored LU-SGS of the reference documentation), which equals the natural
+ * order of the colour-renumbered mesh.
+ *
+ * Like the reference, the object keeps the caller's pointers (host or
+ * device) without copying.  The mesh arrays (CSR, face_area, face_normal,
+ * rcp_vol) are read once, at the first Prepare/sweep; fspr/tfspr and
+ * jmat/tjmat are read by each Prepare; element arrays by Pack, Update and
+ * SubResidual.  All calls are complete when they return.
+ */
+#pragma once
+
+#include "ucfd_gb300.h"
+
+#if defined(__cplusplus)
+extern "C" {
+#endif
+
+typedef struct _FlowSys *FlowSys;   /* ucfdlusgs.h:5 */
+
+/* ---- common (ucfdlusgs.h:8-14, flowsys.c:6-54,120-140) ---------------- */
+UCFD_EXTERN ucfd_status_t UCFDFlowSysCreate(FlowSys *sys, UCFDInt nlocal, UCFDInt nvars,
+                                            UCFDInt nfvars, UCFDInt ndims, UCFDInt nfaces,
+                                            UCFDInt nelem, UCFDInt *rowptr, UCFDInt *colidx,
+                                            UCFDInt *slots, UCFDInt8 *sides,
+                                            UCFDReal *face_area, UCFDReal *face_normal,
+                                            UCFDReal *rcp_vol);
+UCFD_EXTERN ucfd_status_t UCFDFlowSysSetElement(FlowSys *sys, UCFDInt eidx, UCFDInt neles,
+                                                UCFDInt nface, UCFDInt *cell_ids,
+                                                UCFDReal *uptsb, UCFDReal *rhs, UCFDReal *dt,
+                                                UCFDReal *dsrc, UCFDReal *vol,
+                                                UCFDReal *resid_out);
+UCFD_EXTERN ucfd_status_t UCFDFlowSysDestroy(FlowSys *sys);
+
+/* ---- scalar LU-SGS (ucfdlusgs.h:17-25, lusgs.c) ----------------------- */
+UCFD_EXTERN ucfd_status_t UCFDFlowSysSetLUSGS(FlowSys *sys, UCFDReal *fspr, UCFDReal *tfspr);
+UCFD_EXTERN ucfd_status_t UCFDLUSGS_Pack(FlowSys sys, UCFDInt eidx, UCFDReal turb_factor,
+                                         UCFDReal a0);
+UCFD_EXTERN ucfd_status_t UCFDLUSGS_Update(FlowSys sys, UCFDInt eidx);
+UCFD_EXTERN ucfd_status_t UCFDLUSGS_NSPrepare(FlowSys sys, UCFDReal kappa);
+UCFD_EXTERN ucfd_status_t UCFDLUSGS_RANSPrepare(FlowSys sys, UCFDReal kappa);
+UCFD_EXTERN ucfd_status_t UCFDLUSGS_NSLowerSweep(FlowSys sys, UCFDReal kappa);
+UCFD_EXTERN ucfd_status_t UCFDLUSGS_NSUpperSweep(FlowSys sys, UCFDReal kappa);
+UCFD_EXTERN ucfd_status_t UCFDLUSGS_RANSLowerSweep(FlowSys sys, UCFDReal kappa);
+UCFD_EXTERN ucfd_status_t UCFDLUSGS_RANSUpperSweep(FlowSys sys, UCFDReal kappa);
+
+/* ---- block LU-SGS (ucfdlusgs.h:28-40, blusgs.c) ----------------------- */
+UCFD_EXTERN ucfd_status_t UCFDFlowSysSetBLUSGS(FlowSys *sys, UCFDReal *jmat, UCFDReal *tjmat);
+UCFD_EXTERN ucfd_status_t UCFDBLUSGS_Pack(FlowSys sys, UCFDInt eidx, UCFDReal a0);
+UCFD_EXTERN ucfd_status_t UCFDBLUSGS_KWSST_Pack(FlowSys sys, UCFDInt eidx, UCFDReal turb_factor,
+                                                UCFDReal a0);
+UCFD_EXTERN ucfd_status_t UCFDBLUSGS_SA_Pack(FlowSys sys, UCFDInt eidx, UCFDReal turb_factor,
+                                             UCFDReal a0);
+UCFD_EXTERN ucfd_status_t UCFDBLUSGS_Update(FlowSys sys, UCFDInt eidx);
+UCFD_EXTERN ucfd_status_t UCFDBLUSGS_SubResidual(FlowSys sys, UCFDInt eidx);
+UCFD_EXTERN ucfd_status_t UCFDBLUSGS_NSPrepare(FlowSys sys);
+UCFD_EXTERN ucfd_status_t UCFDBLUSGS_RANSPrepare(FlowSys sys);
+UCFD_EXTERN ucfd_status_t UCFDBLUSGS_NSLowerSweep(FlowSys sys);
+UCFD_EXTERN ucfd_status_t UCFDBLUSGS_RANSLowerSweep(FlowSys sys);
+UCFD_EXTERN ucfd_status_t UCFDBLUSGS_NSUpperSweep(FlowSys sys);
+UCFD_EXTERN ucfd_status_t UCFDBLUSGS_RANSUpperSweep(FlowSys sys);
+UCFD_EXTERN ucfd_status_t UCFDBLUSGS_Reset(FlowSys sys);
+
+/* ======================================================================
+ * GB300 extensions (no counterpart in the reference header).
+ * ==================================================================== */
+
+/* Sweep in colour order instead of natural order.  color[r] (0-based, any
+ * range) is the colour of rank cell r; cells of one colour must not be
+ * neighbours (UCFD_ERR_ARGUMENT otherwise).  Lower sweeps visit colours in
+ * increasing order, upper sweeps in decreasing order.  Pass NULL to return
+ * to natural order.  Must be called before the first Prepare. */
+UCFD_EXTERN ucfd_status_t UCFDFlowSysSetColoring(FlowSys sys, const UCFDInt *color);
+/* Greedy first-fit colouring of the CSR graph in rank order, applied as by
+ * UCFDFlowSysSetColoring; *ncolors receives the number of colours. */
+UCFD_EXTERN ucfd_status_t UCFDFlowSysColorGreedy(FlowSys sys, UCFDInt *ncolors);
+/* Number of parallel levels of the current sweep schedule. */
+UCFD_EXTERN ucfd_status_t UCFDFlowSysGetLevels(FlowSys sys, UCFDInt *nlevels);
+/* Arithmetic of the sweeps (ucfd_precision_t); before the first Prepare. */
+UCFD_EXTERN ucfd_status_t UCFDFlowSysSetPrecision(FlowSys sys, int precision);
+/* Launch shape of the sweep kernels (0 = autotuned default). */
+UCFD_EXTERN ucfd_status_t UCFDFlowSysSetLaunch(FlowSys sys, int threads_per_block);
+/* Run all kernels of a call on the caller's CUDA stream and return without
+ * synchronising (stream == NULL restores the private stream and synchronous
+ * calls).  Host-pointer arguments still synchronise. */
+UCFD_EXTERN ucfd_status_t UCFDFlowSysSetStream(FlowSys sys, void *cuda_stream, int async);
+
+/* Scalar LU-SGS pseudo-time loop on device-resident state: niter times
+ * { du = rhs; NS prepare; NS lower; NS upper; [RANS prepare/lower/upper];
+ *   u += du }, launched as one CUDA graph (mode 0) or as one persistent
+ * grid-synchronised kernel per sweep (mode 1).  Requires a prior Pack of
+ * every element.  resid (optional, [niter]) receives sqrt(sum du^2)
+ * accumulated in FP64 after each iteration.  Update() afterwards writes
+ * the final state back to the element arrays. */
+UCFD_EXTERN ucfd_status_t UCFDLUSGS_Run(FlowSys sys, UCFDInt niter, UCFDReal kappa, int rans,
+                                        int mode, UCFDReal *resid);
+
+/* Block LU-SGS linear solve on device-resident state after Pack + Prepare:
+ * sweeps (lower+upper pairs) until ||rhs - A du||_2 <= rtol ||rhs||_2 or
+ * max_sweeps pairs.  With UCFD_PREC_FP32 the sweeps run in FP32 inside FP64
+ * iterative refinement (FP64 true residual every inner_sweeps pairs).
+ * Writes the pairs used and the final relative residual. */
+UCFD_EXTERN ucfd_status_t UCFDBLUSGS_Solve(FlowSys sys, UCFDReal rtol, UCFDInt max_sweeps,
+                                           UCFDInt inner_sweeps, UCFDInt *nsweeps,
+                                           UCFDReal *relres);
+/* FP64 relative residual ||rhs - A du|| / ||rhs|| of the packed NS system. */
+UCFD_EXTERN ucfd_status_t UCFDBLUSGS_Residual(FlowSys sys, UCFDReal *relres);
+
+#if defined(__cplusplus)
+}
+#endif

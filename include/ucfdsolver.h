@@ -1,0 +1,56 @@
+/*
+ * ucfdsolver.h -- Krylov solvers of libucfd_gb300.so.
+ *
+ * Drop-in for src/krylov/include/ucfdsolver.h:5-31 (GMRES).  GMRES(m) is
+ * left-preconditioned with classical Gram-Schmidt plus one
+ * re-orthogonalisation and Givens rotations, stopping when the absolute
+ * true residual ||b - A x|| <= tol is seen at a restart (gmres.c:42-129).
+ * Everything runs on the GPU: Arnoldi passes are fused, the Givens / least-
+ * squares step runs on the device, and one restart cycle is replayed as a
+ * CUDA graph with a single host synchronisation per restart.  x and b may
+ * be host or device arrays of n = bn*blk values.
+ */
+#pragma once
+
+#include "ucfdprecon.h"
+
+#if defined(__cplusplus)
+extern "C" {
+#endif
+
+typedef struct _Solver *Solver;   /* ucfdsolver.h:6 */
+
+typedef const char *SolverType;   /* ucfdsolver.h:8-10 */
+#define GMRES "gmres"
+
+/* ucfdsolver.h:17-23, solver.c:5-69 */
+UCFD_EXTERN ucfd_status_t UCFDSolverInit(Solver *solver);
+UCFD_EXTERN ucfd_status_t UCFDSolverDestroy(Solver *solver);
+UCFD_EXTERN ucfd_status_t UCFDSolve(Solver solver, Precon pc, SpMat A, UCFDReal *x,
+                                    UCFDReal *b);
+UCFD_EXTERN ucfd_status_t UCFDSolverGetResult(Solver solver, UCFDInt *stat, UCFDInt *iter,
+                                              UCFDReal *residual);
+UCFD_EXTERN ucfd_status_t UCFDSolverTraceResidualHistory(Solver solver);
+UCFD_EXTERN ucfd_status_t UCFDSolverGetResidualHistory(Solver solver, UCFDReal *hist);
+
+/* ucfdsolver.h:25, gmres.c:153-178; ucfdsolver.h:28, cugmres.cu:253-300 */
+UCFD_EXTERN ucfd_status_t UCFDSolverCreateGMRES(Solver *solver, UCFDInt n, UCFDInt m,
+                                                UCFDInt maxiter, UCFDReal tol);
+UCFD_EXTERN ucfd_status_t UCFDSolverCreateCUDAGMRES(Solver *solver, UCFDInt n, UCFDInt m,
+                                                    UCFDInt maxiter, UCFDReal tol);
+
+/* ---- GB300 extensions ------------------------------------------------ */
+/* UCFD_PREC_FP32: mixed-precision GMRES -- inside each restart cycle the
+ * matrix-vector products use FP32 values and the preconditioner runs in
+ * FP32, while the Arnoldi orthogonalisation, Givens/least-squares solve and
+ * the true residual b - A x at every restart stay FP64 (iterative
+ * refinement).  Before the first UCFDSolve. */
+UCFD_EXTERN ucfd_status_t UCFDSolverSetPrecision(Solver solver, int precision);
+/* Happy-breakdown tolerance (default 1e-12, solver.c:11). */
+UCFD_EXTERN ucfd_status_t UCFDSolverSetHappyTol(Solver solver, UCFDReal haptol);
+/* Total Arnoldi steps of the last solve. */
+UCFD_EXTERN ucfd_status_t UCFDSolverGetArnoldiSteps(Solver solver, UCFDInt *steps);
+
+#if defined(__cplusplus)
+}
+#endif

@@ -1,0 +1,927 @@
+// flowsys.cpp -- the FlowSys LU-SGS / BLU-SGS API (ucfdlusgs.h) on the GPU.
+//
+// Object model follows src/lusgs/flowsys.{h,c}: the handle keeps the
+// caller's mesh/element pointers; work arrays are library-owned (here in
+// device memory).  The rank cells are renumbered internally into a
+// level-major order (graph.h) so that each level is a contiguous range of
+// independent cells; all per-cell and per-cell-face arrays are stored with
+// the internal cell index fastest (coalesced, one thread per cell).
+#include <algorithm>
+#include <cmath>
+#include <memory>
+
+#include "../../include/ucfdlusgs.h"
+#include "graph.h"
+#include "launch.h"
+#include "ucfd_internal.h"
+
+using namespace ucfd;
+
+namespace {
+
+struct Elem {
+    int neles = 0, nface = 0;
+    int *cell_ids = nullptr;
+    double *uptsb = nullptr, *rhs = nullptr, *dt = nullptr, *dsrc = nullptr, *vol = nullptr,
+           *resid_out = nullptr;
+    DevBuf<int> s_ids;
+    DevBuf<double> s_upts, s_rhs, s_dt, s_dsrc, s_vol, s_res;
+};
+
+enum { MODE_NONE = 0, MODE_LUSGS = 1, MODE_BLUSGS = 2 };
+
+// Arrays of one precision (double for the FP64 modes, float for FP32).
+template <typename S>
+struct Work {
+    DevBuf<S> fa, rv, nrm;                 // geometry (ELL)
+    DevBuf<S> u, du, diag, base, lamN, lamT, rhs0;  // scalar LU-SGS
+    DevBuf<S> rhs, bdu, dup, J, LU, tJ, tLU;        // block LU-SGS
+    DevBuf<S> r, delta;                    // refinement
+};
+
+}  // namespace
+
+struct _FlowSys {
+    int nlocal = 0, nvars = 0, nfvars = 0, ntvars = 0, ndims = 0, nfaces = 0, nelem = 0;
+    int *rowptr = nullptr, *colidx = nullptr, *slots = nullptr;
+    int8_t *sides = nullptr;
+    double *face_area = nullptr, *face_normal = nullptr, *rcp_vol = nullptr;
+    int mode = MODE_NONE;
+    double *fspr = nullptr, *tfspr = nullptr, *jmat = nullptr, *tjmat = nullptr;
+    std::vector<Elem> eles;
+
+    int prec = UCFD_PREC_FP64;
+    int block = 0;
+    cudaStream_t own = nullptr, user = nullptr;
+    bool async = false;
+
+    std::vector<int> color;
+    bool colored = false;
+
+    // topology
+    bool topo = false;
+    long long N = 0;
+    int P = 0;
+    Schedule sch;
+    DevBuf<int> d_iperm, d_nei, d_slot;
+    DevBuf<int8_t> d_side;
+    DevBuf<double> fa64, rv64;
+
+    Work<double> w64;
+    Work<float> w32;
+    DevBuf<double> D, LU64, tD, tLU64, J64, rhs64, x64;  // FP64 block arrays
+    bool du64_valid = false;
+    DevBuf<double> part, red, resid;
+    PinnedBuf<double> h_red;
+
+    // CUDA graph of one scalar pseudo-time iteration
+    cudaGraphExec_t run_exec = nullptr;
+    int run_rans = -1;
+    double run_kappa = 0;
+
+    cudaStream_t stream() const { return user ? user : own; }
+};
+
+namespace {
+
+void finish(FlowSys s, bool force_sync = false) {
+    UCFD_CHECK_LAUNCH();
+    if (!s->async || force_sync) UCFD_CUDA(cudaStreamSynchronize(s->stream()));
+}
+
+// Build the level schedule and the ELL mesh arrays (once).
+void build_topology(FlowSys s) {
+    if (s->topo) return;
+    ensure_device();
+    const int n = s->nlocal;
+    std::vector<int> rp, ci, sl;
+    std::vector<int8_t> sd;
+    to_host(s->rowptr, (size_t)n + 1, rp);
+    UCFD_REQUIRE(rp[0] == 0, "rowptr[0] must be 0");
+    for (int i = 0; i < n; ++i) UCFD_REQUIRE(rp[i + 1] >= rp[i], "rowptr must be non-decreasing");
+    const size_t nnz = (size_t)rp[n];
+    to_host(s->colidx, nnz, ci);
+    to_host(s->slots, nnz, sl);
+    to_host(s->sides, nnz, sd);
+    for (size_t p = 0; p < nnz; ++p) {
+        UCFD_REQUIRE(ci[p] >= 0 && ci[p] < n, "colidx[%zu] = %d out of range", p, ci[p]);
+        UCFD_REQUIRE(sl[p] >= 0 && sl[p] < s->nfaces, "slots[%zu] = %d out of range", p, sl[p]);
+        UCFD_REQUIRE(sd[p] == 1 || sd[p] == -1, "sides[%zu] = %d must be +1 or -1", p, (int)sd[p]);
+    }
+    std::vector<double> fa, fn, rv;
+    to_host(s->face_area, (size_t)s->nfaces, fa);
+    to_host(s->face_normal, (size_t)s->nfaces * s->ndims, fn);
+    to_host(s->rcp_vol, (size_t)n, rv);
+
+    s->sch = s->colored ? schedule_colored(n, rp.data(), ci.data(), s->color.data())
+                        : schedule_natural(n, rp.data(), ci.data());
+    const Schedule &sch = s->sch;
+    int P = 0;
+    for (int i = 0; i < n; ++i) P = std::max(P, rp[i + 1] - rp[i]);
+    P = std::max(P, 1);
+    const long long N = n;
+    s->N = N;
+    s->P = P;
+    std::vector<int> nei((size_t)P * N, -1), slot((size_t)P * N, -1);
+    std::vector<int8_t> side((size_t)P * N, 0);
+    std::vector<double> efa((size_t)P * N, 0.0), erv(N), enrm((size_t)P * s->ndims * N, 0.0);
+    for (long long k = 0; k < N; ++k) {
+        const int r = sch.perm[k];
+        erv[k] = rv[r];
+        for (int p = 0; p < rp[r + 1] - rp[r]; ++p) {
+            const int q = rp[r] + p;
+            nei[p * N + k] = sch.iperm[ci[q]];
+            slot[p * N + k] = sl[q];
+            side[p * N + k] = sd[q];
+            efa[p * N + k] = fa[sl[q]];
+            for (int d = 0; d < s->ndims; ++d)
+                enrm[(p * s->ndims + d) * N + k] = sd[q] * fn[sl[q] + (size_t)d * s->nfaces];
+        }
+    }
+    cudaStream_t st = s->stream();
+    s->d_iperm.upload(sch.iperm.data(), N, st);
+    s->d_nei.upload(nei.data(), nei.size(), st);
+    s->d_slot.upload(slot.data(), slot.size(), st);
+    s->d_side.upload(side.data(), side.size(), st);
+    s->fa64.upload(efa.data(), efa.size(), st);
+    s->rv64.upload(erv.data(), erv.size(), st);
+    s->w64.nrm.upload(enrm.data(), enrm.size(), st);
+    if (s->prec == UCFD_PREC_FP32) {
+        std::vector<float> f(efa.begin(), efa.end());
+        s->w32.fa.upload(f.data(), f.size(), st);
+        std::vector<float> g(erv.begin(), erv.end());
+        s->w32.rv.upload(g.data(), g.size(), st);
+        std::vector<float> h(enrm.begin(), enrm.end());
+        s->w32.nrm.upload(h.data(), h.size(), st);
+    }
+    UCFD_CUDA(cudaStreamSynchronize(st));
+    s->topo = true;
+}
+
+Elem &elem(FlowSys s, int eidx) {
+    UCFD_REQUIRE(eidx >= 0 && eidx < s->nelem, "element index %d out of range [0, %d)", eidx, s->nelem);
+    Elem &e = s->eles[eidx];
+    UCFD_REQUIRE(e.neles > 0 && e.cell_ids, "element %d was not set (UCFDFlowSysSetElement)", eidx);
+    return e;
+}
+
+const int *ids_view(FlowSys s, Elem &e) { return device_view<int>(e.cell_ids, e.neles, e.s_ids, s->stream()); }
+
+template <typename S>
+Work<S> &work(FlowSys s);
+template <>
+Work<double> &work<double>(FlowSys s) { return s->w64; }
+template <>
+Work<float> &work<float>(FlowSys s) { return s->w32; }
+
+template <typename S>
+const S *geo_fa(FlowSys s) {
+    if constexpr (std::is_same<S, double>::value) return s->fa64.p;
+    else return s->w32.fa.p;
+}
+template <typename S>
+const S *geo_rv(FlowSys s) {
+    if constexpr (std::is_same<S, double>::value) return s->rv64.p;
+    else return s->w32.rv.p;
+}
+
+#define KCALL(EX, fn, ...)                         \
+    do {                                           \
+        if constexpr (EX) kexact::fn(__VA_ARGS__); \
+        else kfast::fn(__VA_ARGS__);               \
+    } while (0)
+
+// Calls body.template operator()<S, EX>() with the precision of the handle.
+template <typename F>
+void dispatch(FlowSys s, F &&body) {
+    switch (s->prec) {
+        case UCFD_PREC_FP64: body.template operator()<double, true>(); break;
+        case UCFD_PREC_FP64_FMA: body.template operator()<double, false>(); break;
+        case UCFD_PREC_FP32: body.template operator()<float, false>(); break;
+        default: fail(UCFD_ERR_STATE, "bad precision %d", s->prec);
+    }
+}
+
+void need_mode(FlowSys s, int m) {
+    UCFD_REQUIRE(s, "null FlowSys handle");
+    if (s->mode != m)
+        fail(UCFD_ERR_STATE, "FlowSys is not set up for %s (call UCFDFlowSysSet%s first)",
+             m == MODE_LUSGS ? "LU-SGS" : "BLU-SGS", m == MODE_LUSGS ? "LUSGS" : "BLUSGS");
+}
+
+// ---- scalar LU-SGS --------------------------------------------------------
+template <typename S, bool EX>
+void lusgs_sweep(FlowSys s, bool rans, bool upper, double kappa) {
+    Work<S> &w = work<S>(s);
+    const long long N = s->N;
+    ScalarSweepArgs<S> a{};
+    a.cells = nullptr;
+    a.lcolor = nullptr;
+    a.nface = s->P;
+    a.ld = N;
+    a.nei = s->d_nei.p;
+    a.fa = geo_fa<S>(s);
+    a.rv = geo_rv<S>(s);
+    a.nrm = w.nrm.p;
+    a.lam = rans ? w.lamT.p : w.lamN.p;
+    a.u = w.u.p;
+    a.nbsrc = w.du.p;
+    a.own_in = w.du.p;
+    a.own_out = w.du.p;
+    a.diag = w.diag.p;
+    a.diag_vs = N;
+    a.kappa = (S)kappa;
+    a.gamma = (S)constants().gamma;
+    a.pmin = (S)constants().pmin;
+    a.upper = upper ? 1 : 0;
+    const int L = s->sch.nlev;
+    for (int q = 0; q < L; ++q) {
+        const int l = upper ? L - 1 - q : q;
+        a.t0 = s->sch.lev_off[l];
+        a.t1 = s->sch.lev_off[l + 1];
+        a.lo = a.t0;
+        a.hi = a.t1;
+        KCALL(EX, scalar_sweep<S>, a, s->nvars, s->nfvars, s->ndims, rans ? 1 : 0, s->block, s->stream());
+    }
+}
+
+template <typename S, bool EX>
+void lusgs_prepare(FlowSys s, bool rans, double kappa, const S *base) {
+    Work<S> &w = work<S>(s);
+    KCALL(EX, fs_lusgs_prepare<S>, s->N, s->P, rans ? s->nfvars : 0, rans ? s->nvars : s->nfvars, (S)kappa,
+          s->d_nei.p, geo_fa<S>(s), geo_rv<S>(s), rans ? w.lamT.p : w.lamN.p, base, w.diag.p, s->stream());
+}
+
+template <typename S>
+void lusgs_alloc(FlowSys s) {
+    Work<S> &w = work<S>(s);
+    const long long n = (long long)s->nvars * s->N;
+    w.u.ensure(n);
+    w.du.ensure(n);
+    w.diag.ensure(n);
+    w.base.ensure(n);
+    w.rhs0.ensure(n);
+}
+
+// ---- block LU-SGS -----------------------------------------------------------
+template <typename S>
+void blusgs_alloc(FlowSys s) {
+    Work<S> &w = work<S>(s);
+    const long long N = s->N, nv = s->nvars;
+    w.rhs.ensure(nv * N);
+    w.bdu.ensure(nv * N);
+    w.dup.ensure(nv * N);
+    const long long b2 = (long long)s->nfvars * s->nfvars;
+    s->D.ensure(b2 * N);
+    s->LU64.ensure(b2 * N);
+    w.J.ensure((long long)s->P * b2 * N);
+    if (std::is_same<S, float>::value) {
+        w.LU.ensure(b2 * N);
+        s->rhs64.ensure(nv * N);
+        s->x64.ensure(nv * N);
+    }
+    if (s->ntvars > 0) {
+        const long long t2 = (long long)s->ntvars * s->ntvars;
+        s->tD.ensure(t2 * N);
+        s->tLU64.ensure(t2 * N);
+        w.tJ.ensure((long long)s->P * t2 * N);
+        if (std::is_same<S, float>::value) w.tLU.ensure(t2 * N);
+    }
+}
+
+template <typename S>
+S *blu_rhs(FlowSys s) { return work<S>(s).rhs.p; }
+
+template <typename S>
+const S *blu_LU(FlowSys s, bool turb) {
+    if constexpr (std::is_same<S, double>::value) return turb ? s->tLU64.p : s->LU64.p;
+    else return turb ? s->w32.tLU.p : s->w32.LU.p;
+}
+
+template <typename S, bool EX>
+void blusgs_sweep_into(FlowSys s, bool turb, bool upper, const S *rhs, S *du) {
+    Work<S> &w = work<S>(s);
+    const int B = turb ? s->ntvars : s->nfvars;
+    const int var0 = turb ? s->nfvars : 0;
+    const int L = s->sch.nlev;
+    for (int q = 0; q < L; ++q) {
+        const int l = upper ? L - 1 - q : q;
+        KCALL(EX, fs_blusgs_sweep<S>, B, s->sch.lev_off[l], s->sch.lev_off[l + 1], s->N, s->P, var0,
+              s->d_nei.p, geo_fa<S>(s), geo_rv<S>(s), turb ? w.tJ.p : w.J.p, blu_LU<S>(s, turb), rhs, du,
+              s->block, s->stream());
+    }
+}
+
+// FP64 residual of the NS block system for x; returns ||r|| and ||rhs||.
+template <typename Sx, typename R, bool EX>
+void blusgs_residual(FlowSys s, const Sx *x, R *r_out, double *rnorm, double *bnorm) {
+    const int nbmax = (int)((s->N + 255) / 256) + 1;
+    s->part.ensure((size_t)2 * nbmax);
+    s->red.ensure(2);
+    const double *J64 = s->prec == UCFD_PREC_FP32 ? s->J64.p : s->w64.J.p;
+    const double *rhs64 = s->prec == UCFD_PREC_FP32 ? s->rhs64.p : s->w64.rhs.p;
+    int nb = 0;
+    if constexpr (EX)
+        kexact::fs_blusgs_residual<Sx, R>(s->nfvars, s->N, s->P, 0, s->nvars, s->d_nei.p, s->fa64.p, s->rv64.p,
+                                          J64, s->D.p, rhs64, x, r_out, s->part.p, nbmax, &nb, s->stream());
+    else
+        kfast::fs_blusgs_residual<Sx, R>(s->nfvars, s->N, s->P, 0, s->nvars, s->d_nei.p, s->fa64.p, s->rv64.p,
+                                         J64, s->D.p, rhs64, x, r_out, s->part.p, nbmax, &nb, s->stream());
+    kfast::pair_reduce(nb, s->part.p, s->red.p, s->stream());
+    double *h = s->h_red.ensure(2);
+    UCFD_CUDA(cudaMemcpyAsync(h, s->red.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->stream()));
+    UCFD_CUDA(cudaStreamSynchronize(s->stream()));
+    *rnorm = std::sqrt(h[0]);
+    *bnorm = std::sqrt(h[1]);
+}
+
+}  // namespace
+
+namespace {
+// One pseudo-time iteration on device-resident state (see UCFDLUSGS_Run).
+template <typename S, bool EX>
+void lusgs_iteration(FlowSys s, bool rans, double kappa, double *resid_slot) {
+    Work<S> &w = work<S>(s);
+    cudaStream_t st = s->stream();
+    const size_t n = (size_t)s->nvars * s->N;
+    UCFD_CUDA(cudaMemcpyAsync(w.du.p, w.rhs0.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
+    lusgs_prepare<S, EX>(s, false, kappa, w.base.p);
+    lusgs_sweep<S, EX>(s, false, false, kappa);
+    lusgs_sweep<S, EX>(s, false, true, kappa);
+    if (rans) {
+        lusgs_prepare<S, EX>(s, true, kappa, w.base.p);
+        lusgs_sweep<S, EX>(s, true, false, kappa);
+        lusgs_sweep<S, EX>(s, true, true, kappa);
+    }
+    // u += du over the swept variables, ||du|| in FP64
+    const int v1 = rans ? s->nvars : s->nfvars;
+    kfast::axpy_norm<S>((long long)v1 * s->N, w.du.p, w.u.p, s->part.p, resid_slot, st);
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+ucfd_status_t UCFDFlowSysCreate(FlowSys *sys, UCFDInt nlocal, UCFDInt nvars, UCFDInt nfvars, UCFDInt ndims,
+                                UCFDInt nfaces, UCFDInt nelem, UCFDInt *rowptr, UCFDInt *colidx, UCFDInt *slots,
+                                UCFDInt8 *sides, UCFDReal *face_area, UCFDReal *face_normal, UCFDReal *rcp_vol) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(sys, "null FlowSys pointer");
+    *sys = nullptr;
+    UCFD_REQUIRE(nlocal > 0 && nvars > 0 && nfvars > 0 && nfvars <= nvars && nvars <= 16,
+                 "bad sizes nlocal=%d nvars=%d nfvars=%d", nlocal, nvars, nfvars);
+    UCFD_REQUIRE(ndims == 2 || ndims == 3, "ndims must be 2 or 3 (got %d)", ndims);
+    UCFD_REQUIRE(nfaces > 0 && nelem > 0, "bad sizes nfaces=%d nelem=%d", nfaces, nelem);
+    UCFD_REQUIRE(rowptr && colidx && slots && sides && face_area && face_normal && rcp_vol,
+                 "null mesh array");
+    ensure_device();
+    std::unique_ptr<_FlowSys> s(new _FlowSys());
+    s->nlocal = nlocal;
+    s->nvars = nvars;
+    s->nfvars = nfvars;
+    s->ntvars = nvars - nfvars;
+    s->ndims = ndims;
+    s->nfaces = nfaces;
+    s->nelem = nelem;
+    s->rowptr = rowptr;
+    s->colidx = colidx;
+    s->slots = slots;
+    s->sides = sides;
+    s->face_area = face_area;
+    s->face_normal = face_normal;
+    s->rcp_vol = rcp_vol;
+    s->eles.resize(nelem);
+    UCFD_CUDA(cudaStreamCreateWithFlags(&s->own, cudaStreamNonBlocking));
+    *sys = s.release();
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDFlowSysSetElement(FlowSys *sys, UCFDInt eidx, UCFDInt neles, UCFDInt nface, UCFDInt *cell_ids,
+                                    UCFDReal *uptsb, UCFDReal *rhs, UCFDReal *dt, UCFDReal *dsrc, UCFDReal *vol,
+                                    UCFDReal *resid_out) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(sys && *sys, "null FlowSys handle");
+    FlowSys s = *sys;
+    UCFD_REQUIRE(eidx >= 0 && eidx < s->nelem, "element index %d out of range", eidx);
+    UCFD_REQUIRE(neles > 0 && cell_ids, "element %d: neles must be positive and cell_ids non-null", eidx);
+    Elem &e = s->eles[eidx];
+    e.neles = neles;
+    e.nface = nface;
+    e.cell_ids = cell_ids;
+    e.uptsb = uptsb;
+    e.rhs = rhs;
+    e.dt = dt;
+    e.dsrc = dsrc;
+    e.vol = vol;
+    e.resid_out = resid_out;
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDFlowSysDestroy(FlowSys *sys) {
+    UCFD_API_BEGIN
+    if (!sys || !*sys) return UCFD_SUCCESS;
+    FlowSys s = *sys;
+    if (s->own) cudaStreamSynchronize(s->own);
+    if (s->run_exec) cudaGraphExecDestroy(s->run_exec);
+    if (s->own) cudaStreamDestroy(s->own);
+    delete s;
+    *sys = nullptr;
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDFlowSysSetColoring(FlowSys s, const UCFDInt *color) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(s, "null FlowSys handle");
+    UCFD_REQUIRE(!s->topo, "the colouring must be set before the first Prepare or sweep");
+    if (!color) {
+        s->colored = false;
+        s->color.clear();
+    } else {
+        to_host(color, (size_t)s->nlocal, s->color);
+        s->colored = true;
+    }
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDFlowSysColorGreedy(FlowSys s, UCFDInt *ncolors) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(s, "null FlowSys handle");
+    UCFD_REQUIRE(!s->topo, "the colouring must be set before the first Prepare or sweep");
+    std::vector<int> rp, ci;
+    to_host(s->rowptr, (size_t)s->nlocal + 1, rp);
+    to_host(s->colidx, (size_t)rp[s->nlocal], ci);
+    int nc = 0;
+    s->color = greedy_color_csr(s->nlocal, rp.data(), ci.data(), &nc);
+    s->colored = true;
+    if (ncolors) *ncolors = nc;
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDFlowSysGetLevels(FlowSys s, UCFDInt *nlevels) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(s && nlevels, "null argument");
+    build_topology(s);
+    *nlevels = s->sch.nlev;
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDFlowSysSetPrecision(FlowSys s, int precision) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(s, "null FlowSys handle");
+    UCFD_REQUIRE(precision == UCFD_PREC_FP64 || precision == UCFD_PREC_FP64_FMA || precision == UCFD_PREC_FP32,
+                 "unknown precision %d", precision);
+    UCFD_REQUIRE(!s->topo, "precision must be set before the first Prepare or sweep");
+    s->prec = precision;
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDFlowSysSetLaunch(FlowSys s, int threads_per_block) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(s, "null FlowSys handle");
+    UCFD_REQUIRE(threads_per_block == 0 || (threads_per_block % 32 == 0 && threads_per_block <= 256),
+                 "threads_per_block must be 0 or a multiple of 32 up to 256");
+    s->block = threads_per_block;
+    if (s->run_exec) {
+        cudaGraphExecDestroy(s->run_exec);
+        s->run_exec = nullptr;
+    }
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDFlowSysSetStream(FlowSys s, void *cuda_stream, int async) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(s, "null FlowSys handle");
+    UCFD_CUDA(cudaStreamSynchronize(s->stream()));
+    s->user = (cudaStream_t)cuda_stream;
+    s->async = cuda_stream && async;
+    UCFD_API_END
+}
+
+// ---- scalar LU-SGS (lusgs.c) ------------------------------------------------
+ucfd_status_t UCFDFlowSysSetLUSGS(FlowSys *sys, UCFDReal *fspr, UCFDReal *tfspr) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(sys && *sys, "null FlowSys handle");
+    UCFD_REQUIRE(fspr, "fspr must not be null");
+    FlowSys s = *sys;
+    UCFD_REQUIRE(s->mode == MODE_NONE || s->mode == MODE_LUSGS, "FlowSys already set up for BLU-SGS");
+    s->mode = MODE_LUSGS;
+    s->fspr = fspr;
+    s->tfspr = tfspr;
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDLUSGS_Pack(FlowSys s, UCFDInt eidx, UCFDReal turb_factor, UCFDReal a0) {
+    UCFD_API_BEGIN
+    need_mode(s, MODE_LUSGS);
+    build_topology(s);
+    Elem &e = elem(s, eidx);
+    UCFD_REQUIRE(e.uptsb && e.rhs && e.dt && e.dsrc, "element %d: uptsb, rhs, dt and dsrc are needed by Pack", eidx);
+    cudaStream_t st = s->stream();
+    const size_t nv = (size_t)s->nvars * e.neles;
+    const int *ids = ids_view(s, e);
+    const double *up = device_view<double>(e.uptsb, nv, e.s_upts, st);
+    const double *rh = device_view<double>(e.rhs, nv, e.s_rhs, st);
+    const double *dt = device_view<double>(e.dt, e.neles, e.s_dt, st);
+    const double *ds = device_view<double>(e.dsrc, nv, e.s_dsrc, st);
+    dispatch(s, [&]<typename S, bool EX>() {
+        lusgs_alloc<S>(s);
+        Work<S> &w = work<S>(s);
+        KCALL(EX, fs_lusgs_pack<S>, e.neles, s->nvars, s->nfvars, s->N, turb_factor, a0, ids, s->d_iperm.p, up, rh,
+              dt, ds, w.u.p, w.du.p, w.diag.p, st);
+        const size_t n = (size_t)s->nvars * s->N;
+        UCFD_CUDA(cudaMemcpyAsync(w.base.p, w.diag.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
+        UCFD_CUDA(cudaMemcpyAsync(w.rhs0.p, w.du.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
+    });
+    finish(s, !is_device_ptr(e.uptsb));
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDLUSGS_Update(FlowSys s, UCFDInt eidx) {
+    UCFD_API_BEGIN
+    need_mode(s, MODE_LUSGS);
+    build_topology(s);
+    Elem &e = elem(s, eidx);
+    UCFD_REQUIRE(e.uptsb, "element %d: uptsb is null", eidx);
+    cudaStream_t st = s->stream();
+    const size_t nv = (size_t)s->nvars * e.neles;
+    const int *ids = ids_view(s, e);
+    const bool dev = is_device_ptr(e.uptsb);
+    double *up = dev ? e.uptsb : const_cast<double *>(device_view<double>(e.uptsb, nv, e.s_upts, st));
+    dispatch(s, [&]<typename S, bool EX>() {
+        Work<S> &w = work<S>(s);
+        UCFD_REQUIRE(w.du.p, "Update before Pack");
+        KCALL(EX, fs_lusgs_update<S>, e.neles, s->nvars, s->N, ids, s->d_iperm.p, w.du.p, up, st);
+    });
+    if (!dev) UCFD_CUDA(cudaMemcpyAsync(e.uptsb, up, nv * sizeof(double), cudaMemcpyDeviceToHost, st));
+    finish(s, !dev);
+    UCFD_API_END
+}
+
+static ucfd_status_t lusgs_prepare_api(FlowSys s, bool rans, UCFDReal kappa) {
+    UCFD_API_BEGIN
+    need_mode(s, MODE_LUSGS);
+    build_topology(s);
+    const double *lf = rans ? s->tfspr : s->fspr;
+    UCFD_REQUIRE(lf, "%s is not set", rans ? "tfspr" : "fspr");
+    if (rans) UCFD_REQUIRE(s->ntvars > 0, "RANS prepare needs turbulence variables (nvars > nfvars)");
+    cudaStream_t st = s->stream();
+    static thread_local DevBuf<double> stage;
+    const double *lfd = device_view<double>(lf, (size_t)s->nfaces, stage, st);
+    dispatch(s, [&]<typename S, bool EX>() {
+        Work<S> &w = work<S>(s);
+        UCFD_REQUIRE(w.diag.p, "Prepare before Pack");
+        DevBuf<S> &lam = rans ? w.lamT : w.lamN;
+        lam.ensure((size_t)s->P * s->N);
+        kfast::gather_idx<S>((long long)s->P * s->N, s->d_slot.p, lfd, lam.p, st);
+        lusgs_prepare<S, EX>(s, rans, kappa, nullptr);
+    });
+    finish(s, !is_device_ptr(lf));
+    UCFD_API_END
+}
+
+static ucfd_status_t lusgs_sweep_api(FlowSys s, bool rans, bool upper, UCFDReal kappa) {
+    UCFD_API_BEGIN
+    need_mode(s, MODE_LUSGS);
+    build_topology(s);
+    if (rans) UCFD_REQUIRE(s->ntvars > 0, "RANS sweep needs turbulence variables (nvars > nfvars)");
+    dispatch(s, [&]<typename S, bool EX>() {
+        Work<S> &w = work<S>(s);
+        UCFD_REQUIRE(w.du.p, "sweep before Pack");
+        UCFD_REQUIRE((rans ? w.lamT.p : w.lamN.p), "sweep before %s", rans ? "RANSPrepare" : "NSPrepare");
+        lusgs_sweep<S, EX>(s, rans, upper, kappa);
+    });
+    finish(s);
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDLUSGS_NSPrepare(FlowSys s, UCFDReal kappa) { return lusgs_prepare_api(s, false, kappa); }
+ucfd_status_t UCFDLUSGS_RANSPrepare(FlowSys s, UCFDReal kappa) { return lusgs_prepare_api(s, true, kappa); }
+ucfd_status_t UCFDLUSGS_NSLowerSweep(FlowSys s, UCFDReal kappa) { return lusgs_sweep_api(s, false, false, kappa); }
+ucfd_status_t UCFDLUSGS_NSUpperSweep(FlowSys s, UCFDReal kappa) { return lusgs_sweep_api(s, false, true, kappa); }
+ucfd_status_t UCFDLUSGS_RANSLowerSweep(FlowSys s, UCFDReal kappa) { return lusgs_sweep_api(s, true, false, kappa); }
+ucfd_status_t UCFDLUSGS_RANSUpperSweep(FlowSys s, UCFDReal kappa) { return lusgs_sweep_api(s, true, true, kappa); }
+
+ucfd_status_t UCFDLUSGS_Run(FlowSys s, UCFDInt niter, UCFDReal kappa, int rans, int mode, UCFDReal *resid) {
+    UCFD_API_BEGIN
+    need_mode(s, MODE_LUSGS);
+    build_topology(s);
+    UCFD_REQUIRE(niter >= 0, "niter must be >= 0");
+    UCFD_REQUIRE(mode == 0 || mode == 1, "mode must be 0 (graph) or 1 (persistent)");
+    if (rans) UCFD_REQUIRE(s->ntvars > 0 && s->tfspr, "RANS loop needs turbulence variables and tfspr");
+    cudaStream_t st = s->stream();
+    // spectral radii for the loop
+    static thread_local DevBuf<double> stage;
+    s->part.ensure(4096);
+    s->red.ensure(4);
+    s->resid.ensure((size_t)std::max(niter, 1));
+    dispatch(s, [&]<typename S, bool EX>() {
+        Work<S> &w = work<S>(s);
+        UCFD_REQUIRE(w.u.p, "Run before Pack");
+        w.lamN.ensure((size_t)s->P * s->N);
+        kfast::gather_idx<S>((long long)s->P * s->N, s->d_slot.p, device_view<double>(s->fspr, s->nfaces, stage, st),
+                             w.lamN.p, st);
+        if (rans) {
+            w.lamT.ensure((size_t)s->P * s->N);
+            kfast::gather_idx<S>((long long)s->P * s->N, s->d_slot.p,
+                                 device_view<double>(s->tfspr, s->nfaces, stage, st), w.lamT.p, st);
+        }
+        if (mode == 0) {
+            // one iteration captured once per (rans, kappa) and replayed
+            if (!s->run_exec || s->run_rans != rans || s->run_kappa != kappa) {
+                if (s->run_exec) cudaGraphExecDestroy(s->run_exec);
+                s->run_exec = nullptr;
+                UCFD_CUDA(cudaStreamSynchronize(st));
+                cudaGraph_t g;
+                UCFD_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+                try {
+                    lusgs_iteration<S, EX>(s, rans, kappa, s->red.p);
+                } catch (...) {
+                    cudaStreamEndCapture(st, &g);
+                    throw;
+                }
+                UCFD_CUDA(cudaStreamEndCapture(st, &g));
+                UCFD_CUDA(cudaGraphInstantiate(&s->run_exec, g, 0));
+                cudaGraphDestroy(g);
+                s->run_rans = rans;
+                s->run_kappa = kappa;
+            }
+            for (int it = 0; it < niter; ++it) {
+                UCFD_CUDA(cudaGraphLaunch(s->run_exec, st));
+                UCFD_CUDA(cudaMemcpyAsync(s->resid.p + it, s->red.p, sizeof(double), cudaMemcpyDeviceToDevice, st));
+            }
+        } else {
+            for (int it = 0; it < niter; ++it) lusgs_iteration<S, EX>(s, rans, kappa, s->resid.p + it);
+        }
+    });
+    if (resid && niter > 0)
+        UCFD_CUDA(cudaMemcpyAsync(resid, s->resid.p, niter * sizeof(double), cudaMemcpyDefault, st));
+    finish(s, resid != nullptr);
+    UCFD_API_END
+}
+
+// ---- block LU-SGS (blusgs.c) -------------------------------------------------
+ucfd_status_t UCFDFlowSysSetBLUSGS(FlowSys *sys, UCFDReal *jmat, UCFDReal *tjmat) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(sys && *sys, "null FlowSys handle");
+    UCFD_REQUIRE(jmat, "jmat must not be null");
+    FlowSys s = *sys;
+    UCFD_REQUIRE(s->mode == MODE_NONE || s->mode == MODE_BLUSGS, "FlowSys already set up for LU-SGS");
+    s->mode = MODE_BLUSGS;
+    s->jmat = jmat;
+    s->tjmat = tjmat;
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDBLUSGS_Pack(FlowSys s, UCFDInt eidx, UCFDReal a0) {
+    UCFD_API_BEGIN
+    need_mode(s, MODE_BLUSGS);
+    build_topology(s);
+    Elem &e = elem(s, eidx);
+    UCFD_REQUIRE(e.rhs && e.dt, "element %d: rhs and dt are needed by Pack", eidx);
+    cudaStream_t st = s->stream();
+    const size_t nv = (size_t)s->nvars * e.neles;
+    const int *ids = ids_view(s, e);
+    const double *rh = device_view<double>(e.rhs, nv, e.s_rhs, st);
+    const double *dt = device_view<double>(e.dt, e.neles, e.s_dt, st);
+    dispatch(s, [&]<typename S, bool EX>() {
+        blusgs_alloc<S>(s);
+        double *r64 = std::is_same<S, float>::value ? s->rhs64.p : nullptr;
+        KCALL(EX, fs_blusgs_pack<S>, e.neles, s->nvars, s->nfvars, s->N, a0, ids, s->d_iperm.p, rh, dt,
+              blu_rhs<S>(s), r64, s->D.p, st);
+    });
+    finish(s, !is_device_ptr(e.rhs));
+    UCFD_API_END
+}
+
+static ucfd_status_t tpack_api(FlowSys s, int model, UCFDInt eidx, UCFDReal factor, UCFDReal a0) {
+    UCFD_API_BEGIN
+    need_mode(s, MODE_BLUSGS);
+    build_topology(s);
+    UCFD_REQUIRE(s->ntvars > 0, "turbulence pack needs nvars > nfvars");
+    UCFD_REQUIRE(model != 0 || s->ntvars == 2, "k-omega SST pack needs 2 turbulence variables");
+    UCFD_REQUIRE(model != 1 || s->ntvars == 1, "Spalart-Allmaras pack needs 1 turbulence variable");
+    Elem &e = elem(s, eidx);
+    UCFD_REQUIRE(e.uptsb && e.dsrc && e.dt, "element %d: uptsb, dsrc and dt are needed", eidx);
+    cudaStream_t st = s->stream();
+    const size_t nv = (size_t)s->nvars * e.neles;
+    const int *ids = ids_view(s, e);
+    const double *up = device_view<double>(e.uptsb, nv, e.s_upts, st);
+    const double *ds = device_view<double>(e.dsrc, nv, e.s_dsrc, st);
+    const double *dt = device_view<double>(e.dt, e.neles, e.s_dt, st);
+    dispatch(s, [&]<typename S, bool EX>() { blusgs_alloc<S>(s); });
+    kfast::fs_tblusgs_pack(model, e.neles, s->nvars, s->ntvars, s->N, a0, factor, constants().betast, ids,
+                           s->d_iperm.p, up, ds, dt, s->tD.p, st);
+    finish(s, !is_device_ptr(e.uptsb));
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDBLUSGS_KWSST_Pack(FlowSys s, UCFDInt eidx, UCFDReal turb_factor, UCFDReal a0) {
+    return tpack_api(s, 0, eidx, turb_factor, a0);
+}
+ucfd_status_t UCFDBLUSGS_SA_Pack(FlowSys s, UCFDInt eidx, UCFDReal turb_factor, UCFDReal a0) {
+    return tpack_api(s, 1, eidx, turb_factor, a0);
+}
+
+static ucfd_status_t blusgs_prepare_api(FlowSys s, bool turb) {
+    UCFD_API_BEGIN
+    need_mode(s, MODE_BLUSGS);
+    build_topology(s);
+    const double *jm = turb ? s->tjmat : s->jmat;
+    UCFD_REQUIRE(jm, "%s is not set", turb ? "tjmat" : "jmat");
+    if (turb) UCFD_REQUIRE(s->ntvars > 0, "RANS prepare needs turbulence variables");
+    cudaStream_t st = s->stream();
+    const int B = turb ? s->ntvars : s->nfvars;
+    static thread_local DevBuf<double> stage;
+    const double *jd = device_view<double>(jm, (size_t)2 * B * B * s->nfaces, stage, st);
+    dispatch(s, [&]<typename S, bool EX>() {
+        Work<S> &w = work<S>(s);
+        UCFD_REQUIRE(w.rhs.p, "Prepare before Pack");
+        double *D = turb ? s->tD.p : s->D.p;
+        double *LU64 = turb ? s->tLU64.p : s->LU64.p;
+        S *LU_s = nullptr;
+        double *J64 = nullptr;
+        if constexpr (std::is_same<S, float>::value) {
+            LU_s = turb ? w.tLU.p : w.LU.p;
+            if (!turb) J64 = s->J64.ensure((size_t)s->P * B * B * s->N);
+        }
+        KCALL(EX, fs_blusgs_prepare<S>, B, s->N, s->P, (long long)s->nfaces, s->d_nei.p, s->d_slot.p, s->d_side.p,
+              s->fa64.p, s->rv64.p, jd, D, LU64, LU_s, turb ? w.tJ.p : w.J.p, J64, st);
+    });
+    finish(s, !is_device_ptr(jm));
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDBLUSGS_NSPrepare(FlowSys s) { return blusgs_prepare_api(s, false); }
+ucfd_status_t UCFDBLUSGS_RANSPrepare(FlowSys s) { return blusgs_prepare_api(s, true); }
+
+static ucfd_status_t blusgs_sweep_api(FlowSys s, bool turb, bool upper) {
+    UCFD_API_BEGIN
+    need_mode(s, MODE_BLUSGS);
+    build_topology(s);
+    if (turb) UCFD_REQUIRE(s->ntvars > 0, "RANS sweep needs turbulence variables");
+    dispatch(s, [&]<typename S, bool EX>() {
+        Work<S> &w = work<S>(s);
+        UCFD_REQUIRE(w.rhs.p, "sweep before Pack");
+        blusgs_sweep_into<S, EX>(s, turb, upper, w.rhs.p, w.bdu.p);
+    });
+    s->du64_valid = false;
+    finish(s);
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDBLUSGS_NSLowerSweep(FlowSys s) { return blusgs_sweep_api(s, false, false); }
+ucfd_status_t UCFDBLUSGS_NSUpperSweep(FlowSys s) { return blusgs_sweep_api(s, false, true); }
+ucfd_status_t UCFDBLUSGS_RANSLowerSweep(FlowSys s) { return blusgs_sweep_api(s, true, false); }
+ucfd_status_t UCFDBLUSGS_RANSUpperSweep(FlowSys s) { return blusgs_sweep_api(s, true, true); }
+
+ucfd_status_t UCFDBLUSGS_Reset(FlowSys s) {
+    UCFD_API_BEGIN
+    need_mode(s, MODE_BLUSGS);
+    build_topology(s);
+    cudaStream_t st = s->stream();
+    const size_t n = (size_t)s->nvars * s->N;
+    dispatch(s, [&]<typename S, bool EX>() {
+        blusgs_alloc<S>(s);
+        Work<S> &w = work<S>(s);
+        w.bdu.zero(n, st);
+        w.dup.zero(n, st);
+        if (std::is_same<S, float>::value) s->x64.zero(n, st);
+    });
+    s->du64_valid = false;
+    finish(s);
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDBLUSGS_SubResidual(FlowSys s, UCFDInt eidx) {
+    UCFD_API_BEGIN
+    need_mode(s, MODE_BLUSGS);
+    build_topology(s);
+    Elem &e = elem(s, eidx);
+    UCFD_REQUIRE(e.vol && e.resid_out, "element %d: vol and resid_out are needed", eidx);
+    cudaStream_t st = s->stream();
+    const size_t nv = (size_t)s->nvars * e.neles;
+    const int *ids = ids_view(s, e);
+    const double *vol = device_view<double>(e.vol, e.neles, e.s_vol, st);
+    const bool dev = is_device_ptr(e.resid_out);
+    double *res = dev ? e.resid_out : e.s_res.ensure(nv);
+    dispatch(s, [&]<typename S, bool EX>() {
+        Work<S> &w = work<S>(s);
+        UCFD_REQUIRE(w.bdu.p, "SubResidual before Pack");
+        KCALL(EX, fs_blusgs_subres<S>, e.neles, s->nvars, s->N, ids, s->d_iperm.p, vol, w.bdu.p, w.dup.p, res, st);
+    });
+    if (!dev) UCFD_CUDA(cudaMemcpyAsync(e.resid_out, res, nv * sizeof(double), cudaMemcpyDeviceToHost, st));
+    finish(s, !dev);
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDBLUSGS_Update(FlowSys s, UCFDInt eidx) {
+    UCFD_API_BEGIN
+    need_mode(s, MODE_BLUSGS);
+    build_topology(s);
+    Elem &e = elem(s, eidx);
+    UCFD_REQUIRE(e.uptsb, "element %d: uptsb is null", eidx);
+    cudaStream_t st = s->stream();
+    const size_t nv = (size_t)s->nvars * e.neles;
+    const int *ids = ids_view(s, e);
+    const bool dev = is_device_ptr(e.uptsb);
+    double *up = dev ? e.uptsb : const_cast<double *>(device_view<double>(e.uptsb, nv, e.s_upts, st));
+    if (s->prec == UCFD_PREC_FP32 && s->du64_valid) {
+        kfast::fs_blusgs_update<double>(e.neles, s->nvars, s->N, ids, s->d_iperm.p, s->x64.p, up, st);
+    } else {
+        dispatch(s, [&]<typename S, bool EX>() {
+            Work<S> &w = work<S>(s);
+            UCFD_REQUIRE(w.bdu.p, "Update before Pack");
+            KCALL(EX, fs_blusgs_update<S>, e.neles, s->nvars, s->N, ids, s->d_iperm.p, w.bdu.p, up, st);
+        });
+    }
+    if (!dev) UCFD_CUDA(cudaMemcpyAsync(e.uptsb, up, nv * sizeof(double), cudaMemcpyDeviceToHost, st));
+    finish(s, !dev);
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDBLUSGS_Residual(FlowSys s, UCFDReal *relres) {
+    UCFD_API_BEGIN
+    need_mode(s, MODE_BLUSGS);
+    build_topology(s);
+    UCFD_REQUIRE(relres, "null relres");
+    double rn = 0, bn = 0;
+    if (s->prec == UCFD_PREC_FP32) {
+        UCFD_REQUIRE(s->J64.p, "Residual before NSPrepare");
+        if (s->du64_valid)
+            blusgs_residual<double, double, false>(s, s->x64.p, (double *)nullptr, &rn, &bn);
+        else
+            blusgs_residual<float, float, false>(s, s->w32.bdu.p, (float *)nullptr, &rn, &bn);
+    } else {
+        UCFD_REQUIRE(s->w64.J.p, "Residual before NSPrepare");
+        blusgs_residual<double, double, false>(s, s->w64.bdu.p, (double *)nullptr, &rn, &bn);
+    }
+    *relres = bn > 0 ? rn / bn : rn;
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDBLUSGS_Solve(FlowSys s, UCFDReal rtol, UCFDInt max_sweeps, UCFDInt inner_sweeps, UCFDInt *nsweeps,
+                               UCFDReal *relres) {
+    UCFD_API_BEGIN
+    need_mode(s, MODE_BLUSGS);
+    build_topology(s);
+    UCFD_REQUIRE(max_sweeps > 0 && inner_sweeps > 0, "max_sweeps and inner_sweeps must be positive");
+    cudaStream_t st = s->stream();
+    int pairs = 0;
+    double rn = 0, bn = 0, rel = 0;
+    if (s->prec == UCFD_PREC_FP32) {
+        Work<float> &w = s->w32;
+        UCFD_REQUIRE(s->J64.p && w.LU.p, "Solve before NSPrepare");
+        const size_t n = (size_t)s->nvars * s->N;
+        w.r.ensure(n);
+        w.delta.ensure(n);
+        if (!s->du64_valid) kfast::convert<float, double>((long long)n, w.bdu.p, s->x64.p, st);
+        blusgs_residual<double, float, false>(s, s->x64.p, w.r.p, &rn, &bn);
+        rel = bn > 0 ? rn / bn : rn;
+        while (rel > rtol && pairs < max_sweeps) {
+            w.delta.zero(n, st);
+            const int m = std::min(inner_sweeps, max_sweeps - pairs);
+            for (int q = 0; q < m; ++q) {
+                blusgs_sweep_into<float, false>(s, false, false, w.r.p, w.delta.p);
+                blusgs_sweep_into<float, false>(s, false, true, w.r.p, w.delta.p);
+            }
+            pairs += m;
+            kfast::axpy_into<float>((long long)n, w.delta.p, s->x64.p, st);
+            blusgs_residual<double, float, false>(s, s->x64.p, w.r.p, &rn, &bn);
+            rel = bn > 0 ? rn / bn : rn;
+            UCFD_CHECK_LAUNCH();
+        }
+        kfast::convert<double, float>((long long)n, s->x64.p, w.bdu.p, st);
+        s->du64_valid = true;
+    } else {
+        Work<double> &w = s->w64;
+        UCFD_REQUIRE(w.J.p, "Solve before NSPrepare");
+        const bool ex = s->prec == UCFD_PREC_FP64;
+        blusgs_residual<double, double, false>(s, w.bdu.p, (double *)nullptr, &rn, &bn);
+        rel = bn > 0 ? rn / bn : rn;
+        while (rel > rtol && pairs < max_sweeps) {
+            const int m = std::min(inner_sweeps, max_sweeps - pairs);
+            for (int q = 0; q < m; ++q) {
+                if (ex) {
+                    blusgs_sweep_into<double, true>(s, false, false, w.rhs.p, w.bdu.p);
+                    blusgs_sweep_into<double, true>(s, false, true, w.rhs.p, w.bdu.p);
+                } else {
+                    blusgs_sweep_into<double, false>(s, false, false, w.rhs.p, w.bdu.p);
+                    blusgs_sweep_into<double, false>(s, false, true, w.rhs.p, w.bdu.p);
+                }
+            }
+            pairs += m;
+            blusgs_residual<double, double, false>(s, w.bdu.p, (double *)nullptr, &rn, &bn);
+            rel = bn > 0 ? rn / bn : rn;
+            UCFD_CHECK_LAUNCH();
+        }
+    }
+    if (nsweeps) *nsweeps = pairs;
+    if (relres) *relres = rel;
+    finish(s, true);
+    UCFD_API_END
+}
+
+}  // extern "C"

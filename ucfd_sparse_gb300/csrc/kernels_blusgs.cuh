@@ -1,0 +1,270 @@
+// kernels_blusgs.cuh -- block LU-SGS kernels on the level-major internal layout.
+//
+// Internal arrays (N = internal cells, P = ELL width, B = block size):
+//   nei [P][N] (-1 padding), fa [P][N], rv [N]
+//   J   [P][B*B][N]  the off-diagonal block each cell-face multiplies its
+//                    neighbour increment with (jmat half 1 when side == 1,
+//                    minus half 0 otherwise, blusgs.c:307-310)
+//   D   [B*B][N]     unfactored diagonal block (FP64)
+//   LU  [B*B][N]     its in-place LU factors (ludcmp, inverse.h:13-45)
+//   rhs, du [nvars][N]
+#pragma once
+
+#include "kernels_common.cuh"
+
+namespace UCFD_KNS {
+
+// ludcmp: src/lusgs/inverse.h:13-45 (Doolittle, no pivoting, row by row).
+template <typename T, int B>
+__device__ __forceinline__ void ludcmp_dev(T *A) {
+    if constexpr (B == 1) {
+        A[0] = T(1) / A[0];
+    } else {
+#pragma unroll
+        for (int row = 1; row < B; ++row) {
+            const int nr = B * row;
+            A[nr] /= A[0];
+#pragma unroll
+            for (int col = 1; col < B; ++col) {
+                T v = T(0);
+                if (row > col) {
+#pragma unroll
+                    for (int k = 0; k < col; ++k) v += A[nr + k] * A[col + B * k];
+                    A[nr + col] = (A[nr + col] - v) / A[(B + 1) * col];
+                } else {
+#pragma unroll
+                    for (int k = 0; k < row; ++k) v += A[nr + k] * A[B * k + col];
+                    A[nr + col] -= v;
+                }
+            }
+        }
+    }
+}
+
+// lusub: src/lusgs/inverse.h:51-80 (unit-lower forward, upper backward).
+template <typename T, int B>
+__device__ __forceinline__ void lusub_dev(const T *LU, T *b) {
+    if constexpr (B == 1) {
+        b[0] *= LU[0];
+    } else {
+#pragma unroll
+        for (int row = 1; row < B; ++row) {
+            T v = T(0);
+#pragma unroll
+            for (int col = 0; col < row; ++col) v += LU[row * B + col] * b[col];
+            b[row] -= v;
+        }
+        b[B - 1] /= LU[B * B - 1];
+#pragma unroll
+        for (int row = B - 2; row > -1; --row) {
+            T v = T(0);
+#pragma unroll
+            for (int col = row + 1; col < B; ++col) v += LU[row * B + col] * b[col];
+            b[row] = (b[row] - v) / LU[row * B + row];
+        }
+    }
+}
+
+// rank_blusgs_pack: blusgs.c:17-45.  rhs goes to the internal SoA arrays,
+// the NS diagonal block starts as (1/dt + a0) I.
+template <typename S>
+__global__ void fs_blusgs_pack_kernel(int neles, int nvars, int B, long long N, double a0,
+                                      const int *cell_ids, const int *iperm, const double *rhs,
+                                      const double *dt, S *rhs_s, double *rhs64, double *D) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= neles) return;
+    const long long k = iperm[cell_ids[idx]];
+    for (int v = 0; v < nvars; ++v) {
+        const double x = rhs[idx + (long long)v * neles];
+        rhs_s[k + v * N] = (S)x;
+        if (rhs64) rhs64[k + v * N] = x;
+    }
+    const double d = 1 / dt[idx] + a0;
+    for (int r = 0; r < B; ++r)
+        for (int c = 0; c < B; ++c) D[(r * B + c) * N + k] = (r == c) ? d : 0.0;
+}
+
+// rank_tblusgs_pack + kwsst/sa source Jacobians: blusgs.c:60-120,
+// source_jacobian.c:6-18.  model 0 = k-omega SST, 1 = Spalart-Allmaras.
+__global__ void fs_tblusgs_pack_kernel(int model, int neles, int nvars, int nt, long long N,
+                                       double a0, double factor, double betast,
+                                       const int *cell_ids, const int *iperm, const double *uptsb,
+                                       const double *dsrc, const double *dt, double *D) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= neles) return;
+    const long long k = iperm[cell_ids[idx]];
+    double A[4] = {0.0, 0.0, 0.0, 0.0};
+    const double u0 = uptsb[idx];
+    if (model == 0) {
+        const double kk = uptsb[idx + (long long)(nvars - 2) * neles] / u0;
+        A[0] += dsrc[idx + (long long)(nvars - 2) * neles];
+        const double bk = betast * kk;
+        A[1] += bk > 0.0 ? bk : 0.0;
+        A[1 + nt] = dsrc[idx + (long long)(nvars - 1) * neles];
+    } else {
+        A[0] += dsrc[idx + (long long)(nvars - 1) * neles];
+    }
+    for (int row = 0; row < nt; ++row) A[row + row * nt] += 1 / (dt[idx] * factor) + a0;
+    for (int e = 0; e < nt * nt; ++e) D[e * N + k] = A[e];
+}
+
+// pre_blusgs: blusgs.c:200-246, plus the gather of each cell-face's
+// off-diagonal block (the half the sweeps use) into the ELL layout.
+template <typename S, int B>
+__global__ void fs_blusgs_prepare_kernel(long long N, int P, long long nF, const int *nei,
+                                         const int *slot, const int8_t *side, const double *fa,
+                                         const double *rv, const double *jmat, double *D,
+                                         double *LU64, S *LU_s, S *J_s, double *J64) {
+    const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    constexpr int B2 = B * B;
+    double dm[B2];
+#pragma unroll
+    for (int e = 0; e < B2; ++e) dm[e] = D[e * N + k];
+    for (int p = 0; p < P; ++p) {
+        if (nei[p * N + k] < 0) break;
+        const long long s = slot[p * N + k];
+        const int sd = side[p * N + k];
+        const double fv = fa[p * N + k] * rv[k];
+#pragma unroll
+        for (int r = 0; r < B; ++r) {
+#pragma unroll
+            for (int c = 0; c < B; ++c) {
+                const long long o = s + c * nF + (long long)r * nF * B;
+                const double h0 = jmat[o], h1 = jmat[o + B2 * nF];
+                const double val = (sd == 1) ? h0 : -h1;
+                dm[c + r * B] += val * fv;
+                const double jv = (sd == 1) ? h1 : -h0;
+                J_s[((long long)p * B2 + r * B + c) * N + k] = (S)jv;
+                if (J64) J64[((long long)p * B2 + r * B + c) * N + k] = jv;
+            }
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < B2; ++e) D[e * N + k] = dm[e];
+    ludcmp_dev<double, B>(dm);
+#pragma unroll
+    for (int e = 0; e < B2; ++e) {
+        LU64[e * N + k] = dm[e];
+        if (LU_s) LU_s[e * N + k] = (S)dm[e];
+    }
+}
+
+// lower_sweep / upper_sweep of blusgs.c:273-373 for one level: every
+// neighbour contributes with its current value (lower levels already
+// updated, higher levels not yet), then the cell solves with its LU.
+template <typename S, int B>
+__global__ void __launch_bounds__(256) fs_blusgs_sweep_kernel(int t0, int t1, long long N, int P,
+                                                              int var0, const int *nei, const S *fa,
+                                                              const S *rv, const S *J, const S *LU,
+                                                              const S *rhs, S *du) {
+    const int k = t0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= t1) return;
+    constexpr int B2 = B * B;
+    S b[B];
+#pragma unroll
+    for (int r = 0; r < B; ++r) b[r] = rhs[(var0 + r) * N + k];
+    const S rvk = rv[k];
+    for (int p = 0; p < P; ++p) {
+        const int nb = __ldg(nei + p * N + k);
+        if (nb < 0) break;
+        const S fv = __ldg(fa + p * N + k) * rvk;
+        S x[B];
+#pragma unroll
+        for (int c = 0; c < B; ++c) x[c] = du[(var0 + c) * N + nb];
+        const S *Jp = J + (long long)p * B2 * N + k;
+#pragma unroll
+        for (int r = 0; r < B; ++r) {
+            S val = S(0);
+#pragma unroll
+            for (int c = 0; c < B; ++c) val += __ldg(Jp + (r * B + c) * N) * x[c];
+            b[r] -= val * fv;
+        }
+    }
+    S lu[B2];
+#pragma unroll
+    for (int e = 0; e < B2; ++e) lu[e] = __ldg(LU + e * N + k);
+    lusub_dev<S, B>(lu, b);
+#pragma unroll
+    for (int r = 0; r < B; ++r) du[(var0 + r) * N + k] = b[r];
+}
+
+// FP64 residual of the packed system: r = rhs - D x - sum_f J x_nb fv.
+// Writes r (as R) when r_out != nullptr and accumulates per-block partial
+// sums of r^2 and rhs^2 into part[2*blockIdx.x + {0,1}].
+template <typename Sx, typename R, int B>
+__global__ void fs_blusgs_residual_kernel(long long N, int P, int var0, int nvars, const int *nei,
+                                          const double *fa, const double *rv, const double *J64,
+                                          const double *D, const double *rhs64, const Sx *x,
+                                          R *r_out, double *part) {
+    const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    double rr = 0.0, bb = 0.0;
+    if (k < N) {
+        constexpr int B2 = B * B;
+        double res[B];
+        double xk[B];
+#pragma unroll
+        for (int c = 0; c < B; ++c) xk[c] = (double)x[(var0 + c) * N + k];
+#pragma unroll
+        for (int r = 0; r < B; ++r) {
+            double v = rhs64[(var0 + r) * N + k];
+            bb += v * v;
+#pragma unroll
+            for (int c = 0; c < B; ++c) v -= D[(r * B + c) * N + k] * xk[c];
+            res[r] = v;
+        }
+        for (int p = 0; p < P; ++p) {
+            const int nb = nei[p * N + k];
+            if (nb < 0) break;
+            const double fv = fa[p * N + k] * rv[k];
+            double xn[B];
+#pragma unroll
+            for (int c = 0; c < B; ++c) xn[c] = (double)x[(var0 + c) * N + nb];
+#pragma unroll
+            for (int r = 0; r < B; ++r) {
+                double val = 0.0;
+#pragma unroll
+                for (int c = 0; c < B; ++c) val += J64[((long long)p * B2 + r * B + c) * N + k] * xn[c];
+                res[r] -= val * fv;
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < B; ++r) {
+            rr += res[r] * res[r];
+            if (r_out) r_out[(var0 + r) * N + k] = (R)res[r];
+        }
+    }
+    rr = block_sum(rr);
+    bb = block_sum(bb);
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = rr;
+        part[2 * blockIdx.x + 1] = bb;
+    }
+}
+
+// rank_sub_residual: blusgs.c:161-185 (per element, SoA internal state).
+template <typename S>
+__global__ void fs_blusgs_subres_kernel(int neles, int nvars, long long N, const int *cell_ids,
+                                        const int *iperm, const double *vol, const S *du, S *dup,
+                                        double *res) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= neles) return;
+    const long long k = iperm[cell_ids[idx]];
+    for (int v = 0; v < nvars; ++v) {
+        const S diff = du[k + v * N] - dup[k + v * N];
+        res[idx + (long long)v * neles] = (double)(diff * diff) * vol[idx];
+        dup[k + v * N] = du[k + v * N];
+    }
+}
+
+// rank_blusgs_update: blusgs.c:126-143.
+template <typename S>
+__global__ void fs_blusgs_update_kernel(int neles, int nvars, long long N, const int *cell_ids,
+                                        const int *iperm, const S *du, double *upts) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= neles) return;
+    const long long k = iperm[cell_ids[idx]];
+    for (int v = 0; v < nvars; ++v) upts[idx + (long long)v * neles] += (double)du[k + v * N];
+}
+
+}  // namespace UCFD_KNS

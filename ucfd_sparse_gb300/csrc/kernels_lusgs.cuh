@@ -1,0 +1,214 @@
+// kernels_lusgs.cuh -- scalar (colored / level-scheduled) LU-SGS kernels.
+//
+// Included by kern_exact.cu (namespace kexact, built with -fmad=false: the
+// FP64 arithmetic of every cell is the reference's, operation by
+// operation) and kern_fast.cu (namespace kfast, FMA contraction on; FP64
+// and FP32 instantiations).
+//
+// One thread per cell.  All per-cell arrays are [..][ld] with the cell
+// index fastest, so a warp's loads of one face/variable are coalesced.
+#pragma once
+
+#include "kernels_common.cuh"
+#include "kargs.h"
+
+namespace UCFD_KNS {
+
+// ns_flux_container: flux.c:29-67.  The pressure floor rewrites the energy
+// of the local copy u (flux.c:51-56), exactly as the reference does.
+template <typename T, int NFV, int NDIMS>
+__device__ __forceinline__ void ns_flux(T gamma, T pmin, T *u, const T *nf, T *f) {
+    T rho = u[0];
+    T et = u[NFV - 1];
+    T temp = T(0), contrav = T(0);
+#pragma unroll
+    for (int i = 0; i < NDIMS; ++i) {
+        contrav += u[i + 1] * nf[i];
+        temp += u[i + 1] * u[i + 1];
+    }
+    contrav /= rho;
+    T p = (gamma - T(1)) * (et - T(0.5) * temp / rho);
+    if (p < pmin) {
+        p = pmin;
+        et = p / (gamma - T(1)) + T(0.5) * temp / rho;
+        u[NFV - 1] = et;
+    }
+    T ht = et + p;
+    f[0] = rho * contrav;
+#pragma unroll
+    for (int i = 0; i < NDIMS; ++i) f[i + 1] = u[i + 1] * contrav + nf[i] * p;
+    f[NFV - 1] = ht * contrav;
+}
+
+// rans_flux_container: flux.c:77-90
+template <typename T, int NFV, int NDIMS, int NT>
+__device__ __forceinline__ void rans_flux(const T *u, const T *nf, T *f) {
+    T rho = u[0];
+    T contrav = T(0);
+#pragma unroll
+    for (int i = 0; i < NDIMS; ++i) contrav += u[i + 1] * nf[i];
+    contrav /= rho;
+#pragma unroll
+    for (int i = 0; i < NT; ++i) f[i] = u[NFV + i] * contrav;
+}
+
+template <typename T>
+using ScalarSweepArgs = ::ucfd::ScalarSweepArgs<T>;
+
+// lower_sweep / upper_sweep of lusgs.c:157-257 for one level (or colour):
+// every cell of the range is independent of the others.
+template <typename T, int NV, int NFV, int NDIMS, bool RANS>
+__global__ void __launch_bounds__(256) scalar_sweep_kernel(ScalarSweepArgs<T> a) {
+    constexpr int NV0 = RANS ? NFV : 0;
+    constexpr int DNV = RANS ? NV - NFV : NFV;
+    const int t = a.t0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.t1) return;
+    const long long ld = a.ld;
+    const int i = a.cells ? __ldg(a.cells + t) : t;
+    const int ci = a.lcolor ? __ldg(a.lcolor + i) : 0;
+
+    T df[DNV];
+#pragma unroll
+    for (int k = 0; k < DNV; ++k) df[k] = T(0);
+
+    for (int f = 0; f < a.nface; ++f) {
+        const int nb = __ldg(a.nei + f * ld + i);
+        bool act;
+        if (a.lcolor) {
+            const int cn = __ldg(a.lcolor + nb);
+            act = a.upper ? (cn > ci) : (cn < ci);
+        } else {
+            act = nb >= 0 && (a.upper ? (nb >= a.hi) : (nb < a.lo));
+        }
+        if (!act) continue;
+
+        T u[NV], du[NV], dn[DNV], nf[NDIMS], f0[DNV], f1[DNV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            // only the variables the flux reads are loaded
+            const bool need = RANS ? (v <= NDIMS || v >= NFV) : (v < NFV);
+            u[v] = need ? __ldg(a.u + v * ld + nb) : T(0);
+            du[v] = T(0);
+        }
+#pragma unroll
+        for (int k = 0; k < DNV; ++k) {
+            dn[k] = a.nbsrc[(k + NV0) * ld + nb];
+            du[k + NV0] = dn[k];
+        }
+#pragma unroll
+        for (int d = 0; d < NDIMS; ++d) nf[d] = __ldg(a.nrm + (f * NDIMS + d) * ld + i);
+        T fv = __ldg(a.fa + f * ld + i);
+        if (a.rv) fv = fv * __ldg(a.rv + i);
+        // diff_flux: lusgs.c:143-155 (du += u before either flux)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) du[v] += u[v];
+        if constexpr (RANS) {
+            rans_flux<T, NFV, NDIMS, NV - NFV>(u, nf, f0);
+            rans_flux<T, NFV, NDIMS, NV - NFV>(du, nf, f1);
+        } else {
+            ns_flux<T, NFV, NDIMS>(a.gamma, a.pmin, u, nf, f0);
+            ns_flux<T, NFV, NDIMS>(a.gamma, a.pmin, du, nf, f1);
+        }
+        const T kl = a.kappa * __ldg(a.lam + f * ld + i);
+#pragma unroll
+        for (int k = 0; k < DNV; ++k) {
+            const T dfj = f1[k] - f0[k];
+            df[k] += (dfj - kl * dn[k]) * fv;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < DNV; ++k) {
+        const long long l = (k + NV0) * ld + i;
+        const T dg = a.diag[(k + NV0) * a.diag_vs + i];
+        if (!a.upper)
+            a.own_out[l] = (a.own_in[l] - T(0.5) * df[k]) / dg;
+        else
+            a.own_out[l] = a.own_in[l] - (T(0.5) * df[k] / dg);
+    }
+}
+
+// {serial,parallel}_pre_lusgs (array layout): lusgs.c:8-37 + 87-113 with
+// kappa = 1, a0 = dsrc = 0, rcp_vol = 1.
+template <typename T>
+__global__ void legacy_pre_kernel(int neles, int nface, T factor, const T *fnorm_vol, const T *dt,
+                                  T *diag, const T *fspr) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= neles) return;
+    T sd = T(0);
+    for (int f = 0; f < nface; ++f) {
+        const T lamf = fspr[(long long)f * neles + i];
+        sd += T(0.5) * lamf * fnorm_vol[(long long)f * neles + i];
+    }
+    diag[i] = T(1) / (dt[i] * factor) + sd;
+}
+
+template <typename T>
+__global__ void legacy_update_kernel(int neles, int k0, int k1, T *upts, const T *rhs) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= neles) return;
+    for (int k = k0; k < k1; ++k) upts[(long long)k * neles + i] += rhs[(long long)k * neles + i];
+}
+
+// ---- FlowSys scalar LU-SGS on the level-major internal layout ---------------
+
+// lusgs_pack: lusgs.c:8-37.  Element idx -> internal cell pos[cell_ids[idx]].
+template <typename T>
+__global__ void fs_lusgs_pack_kernel(int neles, int nvars, int nfvars, long long N,
+                                     double turb_factor, double a0, const int *cell_ids,
+                                     const int *iperm, const double *upts, const double *rhs,
+                                     const double *dt, const double *dsrc, T *u, T *du, T *diag) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= neles) return;
+    const long long k = iperm[cell_ids[idx]];
+    for (int v = 0; v < nvars; ++v) {
+        const long long e = idx + (long long)v * neles;
+        const double factor = v < nfvars ? 1.0 : turb_factor;
+        u[k + v * N] = (T)upts[e];
+        du[k + v * N] = (T)rhs[e];
+        diag[k + v * N] = (T)(1.0 / (dt[idx] * factor) + a0 + dsrc[e]);
+    }
+}
+
+// rank_lusgs_update: lusgs.c:54-70 (uptsb += du over all nvars).
+template <typename T>
+__global__ void fs_lusgs_update_kernel(int neles, int nvars, long long N, const int *cell_ids,
+                                       const int *iperm, const T *du, double *upts) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= neles) return;
+    const long long k = iperm[cell_ids[idx]];
+    for (int v = 0; v < nvars; ++v) upts[idx + (long long)v * neles] += (double)du[k + v * N];
+}
+
+// pre_lusgs: lusgs.c:87-113.  lam is the per cell-face copy of lambdaf.
+// With base != nullptr the result is base + sd (a pseudo-time loop
+// re-preparing from the packed diagonal), otherwise diag += sd.
+template <typename T>
+__global__ void fs_lusgs_prepare_kernel(long long N, int maxdeg, int nv0, int nv1, T kappa,
+                                        const int *nei, const T *fa, const T *rv, const T *lam,
+                                        const T *base, T *diag) {
+    const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    T sd = T(0);
+    for (int p = 0; p < maxdeg; ++p) {
+        if (nei[p * N + k] < 0) break;
+        const T lamf = lam[p * N + k] * kappa;
+        sd += T(0.5) * lamf * fa[p * N + k] * rv[k];
+    }
+    if (base)
+        for (int v = nv0; v < nv1; ++v) diag[k + v * N] = base[k + v * N] + sd;
+    else
+        for (int v = nv0; v < nv1; ++v) diag[k + v * N] += sd;
+}
+
+// dst[i] = src[idx[i]] (0 where idx[i] < 0): per cell-face copies of
+// face-indexed arrays.
+template <typename Td>
+__global__ void gather_idx_kernel(long long n, const int *idx, const double *src, Td *dst) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int j = idx[i];
+        dst[i] = j >= 0 ? (Td)src[j] : Td(0);
+    }
+}
+
+}  // namespace UCFD_KNS

@@ -1,0 +1,661 @@
+// krylov.cpp -- SpMat / Precon / Solver objects (ucfdmat.h, ucfdprecon.h,
+// ucfdsolver.h) on the GPU.
+//
+// Matrices and preconditioners are copied to the device once, into the
+// ELL-of-blocks layout of kernels_krylov.cuh.  GMRES(m) keeps every vector,
+// the Hessenberg matrix and the Givens state on the device; the host reads
+// one residual norm (and the cycle state) per restart.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+
+#include "../../include/ucfdsolver.h"
+#include "graph.h"
+#include "launch.h"
+#include "ucfd_internal.h"
+
+using namespace ucfd;
+
+namespace {
+
+cudaStream_t kstream() {
+    static cudaStream_t s = nullptr;
+    if (!s) {
+        ensure_device();
+        UCFD_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    }
+    return s;
+}
+
+// Row-major CSR-of-blocks (host) -> ELL-of-blocks (device).
+struct EllBlocks {
+    int bn = 0, B = 0, P = 0;
+    DevBuf<int> col;
+    DevBuf<double> val;
+    DevBuf<float> val32;
+
+    // rows: internal row k takes original row perm[k] (perm null: identity);
+    // entries [first[k], last[k]) of that row; columns mapped through iperm.
+    void build(int bn_, int B_, const std::vector<int> &rp, const std::vector<int> &ci,
+               const std::vector<double> &vals, const int *perm, const int *iperm, const std::vector<int> *lo,
+               const std::vector<int> *hi, bool fp32, cudaStream_t s) {
+        bn = bn_;
+        B = B_;
+        const long long B2 = (long long)B * B;
+        P = 0;
+        for (int k = 0; k < bn; ++k) {
+            const int r = perm ? perm[k] : k;
+            const int a = lo ? (*lo)[r] : rp[r], b = hi ? (*hi)[r] : rp[r + 1];
+            P = std::max(P, b - a);
+        }
+        const int Pa = std::max(P, 1);
+        std::vector<int> c((size_t)Pa * bn, -1);
+        std::vector<double> v((size_t)Pa * B2 * bn, 0.0);
+        for (int k = 0; k < bn; ++k) {
+            const int r = perm ? perm[k] : k;
+            const int a = lo ? (*lo)[r] : rp[r], b = hi ? (*hi)[r] : rp[r + 1];
+            for (int p = 0; p < b - a; ++p) {
+                const int q = a + p;
+                c[(size_t)p * bn + k] = iperm ? iperm[ci[q]] : ci[q];
+                for (long long e = 0; e < B2; ++e) v[((size_t)p * B2 + e) * bn + k] = vals[(size_t)q * B2 + e];
+            }
+        }
+        col.upload(c.data(), c.size(), s);
+        val.upload(v.data(), v.size(), s);
+        if (fp32) {
+            std::vector<float> f(v.begin(), v.end());
+            val32.upload(f.data(), f.size(), s);
+        }
+        UCFD_CUDA(cudaStreamSynchronize(s));
+    }
+};
+
+}  // namespace
+
+// ===========================================================================
+// SpMat
+// ===========================================================================
+struct _SpMat {
+    const char *type_name = nullptr;
+    int bn = 0, blk = 0;
+    int *rowptr = nullptr, *colidx = nullptr;
+    double *values = nullptr;
+    EllBlocks ell;
+    bool ready = false;
+    DevBuf<double> sx, sy;
+
+    void load(bool fp32) {
+        std::vector<int> rp, ci;
+        std::vector<double> v;
+        to_host(rowptr, (size_t)bn + 1, rp);
+        UCFD_REQUIRE(rp[0] == 0, "rowptr[0] must be 0");
+        for (int i = 0; i < bn; ++i) UCFD_REQUIRE(rp[i + 1] >= rp[i], "rowptr must be non-decreasing");
+        to_host(colidx, (size_t)rp[bn], ci);
+        for (size_t q = 0; q < ci.size(); ++q)
+            UCFD_REQUIRE(ci[q] >= 0 && ci[q] < bn, "colidx[%zu] = %d out of range", q, ci[q]);
+        to_host(values, (size_t)rp[bn] * blk * blk, v);
+        ell.build(bn, blk, rp, ci, v, nullptr, nullptr, nullptr, nullptr, fp32, kstream());
+        ready = true;
+    }
+    void ensure32() {
+        if (!ell.val32.p) {
+            std::vector<double> v((size_t)ell.P * blk * blk * bn);
+            UCFD_CUDA(cudaMemcpy(v.data(), ell.val.p, v.size() * sizeof(double), cudaMemcpyDeviceToHost));
+            std::vector<float> f(v.begin(), v.end());
+            ell.val32.upload(f.data(), f.size(), kstream());
+            UCFD_CUDA(cudaStreamSynchronize(kstream()));
+        }
+    }
+    // y = alpha A x + beta y on device vectors
+    void mult(double alpha, const double *x, double beta, double *y, bool fp32, cudaStream_t s) {
+        if (fp32) {
+            ensure32();
+            kfast::bsr_spmv<float, float>(blk, bn, ell.P, ell.col.p, ell.val32.p, alpha, x, beta, y, 0, s);
+        } else {
+            kexact::bsr_spmv<double, double>(blk, bn, ell.P, ell.col.p, ell.val.p, alpha, x, beta, y, 0, s);
+        }
+    }
+};
+
+// ===========================================================================
+// Precon
+// ===========================================================================
+struct _Precon {
+    const char *type_name = nullptr;
+    int *rowptr = nullptr, *colidx = nullptr, *diagslots = nullptr;
+    double *values = nullptr;
+    int bn = 0, blk = 0, ncolors = 0;
+    std::vector<int> icolors;
+    bool colored = false, none = false;
+    int prec = UCFD_PREC_FP64;
+    bool prepared = false;
+    Schedule sch;
+    bool identity = true;
+    DevBuf<int> perm;
+    DevBuf<long long> dslot;
+    EllBlocks L, U;
+    DevBuf<double> LU64, tmp64;
+    DevBuf<float> LU32, tmp32;
+    DevBuf<double> stage_b;
+
+    void prepare() {
+        if (none) {
+            prepared = true;
+            return;
+        }
+        UCFD_REQUIRE(bn > 0 && blk > 0, "preconditioner type not set (UCFDPreconSetBLUSGS / SetPBLUSGS)");
+        std::vector<int> rp, ci, ds;
+        std::vector<double> v;
+        to_host(rowptr, (size_t)bn + 1, rp);
+        to_host(colidx, (size_t)rp[bn], ci);
+        to_host(diagslots, (size_t)bn, ds);
+        for (int i = 0; i < bn; ++i) {
+            UCFD_REQUIRE(ds[i] >= rp[i] && ds[i] < rp[i + 1], "diagslots[%d] = %d outside row %d", i, ds[i], i);
+            UCFD_REQUIRE(ci[ds[i]] == i, "diagslots[%d] does not point at the diagonal block", i);
+        }
+        for (size_t q = 0; q < ci.size(); ++q)
+            UCFD_REQUIRE(ci[q] >= 0 && ci[q] < bn, "colidx[%zu] = %d out of range", q, ci[q]);
+        to_host(values, (size_t)rp[bn] * blk * blk, v);
+        if (colored) {
+            // colour c = rows [icolors[c], icolors[c+1]); no row may reference
+            // another row of its own colour (otherwise the reference result
+            // depends on thread timing)
+            UCFD_REQUIRE((int)icolors.size() == ncolors + 1 && icolors[0] == 0 && icolors[ncolors] == bn,
+                         "icolors must run from 0 to bn over ncolors+1 entries");
+            std::vector<int> col(bn);
+            for (int c = 0; c < ncolors; ++c) {
+                UCFD_REQUIRE(icolors[c + 1] >= icolors[c], "icolors must be non-decreasing");
+                for (int i = icolors[c]; i < icolors[c + 1]; ++i) col[i] = c;
+            }
+            sch = schedule_colored(bn, rp.data(), ci.data(), col.data());
+        } else {
+            sch = schedule_natural(bn, rp.data(), ci.data());
+        }
+        identity = true;
+        for (int k = 0; k < bn; ++k)
+            if (sch.perm[k] != k) identity = false;
+        cudaStream_t s = kstream();
+        if (!identity) perm.upload(sch.perm.data(), bn, s);
+        std::vector<int> lo(bn), mid(bn), hi(bn);
+        for (int i = 0; i < bn; ++i) {
+            lo[i] = rp[i];
+            mid[i] = ds[i];
+            hi[i] = ds[i] + 1;
+        }
+        std::vector<int> end(rp.begin() + 1, rp.end());
+        const bool fp32 = prec == UCFD_PREC_FP32;
+        const int *pm = identity ? nullptr : sch.perm.data();
+        const int *ip = identity ? nullptr : sch.iperm.data();
+        L.build(bn, blk, rp, ci, v, pm, ip, &lo, &mid, fp32, s);
+        U.build(bn, blk, rp, ci, v, pm, ip, &hi, &end, fp32, s);
+        std::vector<long long> dsl(ds.begin(), ds.end());
+        dslot.upload(dsl.data(), bn, s);
+        const long long B2 = (long long)blk * blk;
+        LU64.ensure(B2 * bn);
+        // the values for the LU come from the caller's array (device view)
+        DevBuf<double> vals;
+        vals.upload(v.data(), v.size(), s);
+        if (fp32) {
+            LU32.ensure(B2 * bn);
+            kfast::pc_prepare<float>(blk, bn, identity ? nullptr : perm.p, dslot.p, vals.p, LU64.p, LU32.p, s);
+        } else if (prec == UCFD_PREC_FP64) {
+            kexact::pc_prepare<double>(blk, bn, identity ? nullptr : perm.p, dslot.p, vals.p, LU64.p, nullptr, s);
+        } else {
+            kfast::pc_prepare<double>(blk, bn, identity ? nullptr : perm.p, dslot.p, vals.p, LU64.p, nullptr, s);
+        }
+        UCFD_CHECK_LAUNCH();
+        UCFD_CUDA(cudaStreamSynchronize(s));
+        prepared = true;
+    }
+
+    // In-place apply to a device vector b [bn*blk] (FP64).
+    void apply(double *b, cudaStream_t s) {
+        if (none) return;
+        UCFD_REQUIRE(prepared, "UCFDPreconPrepare has not been called");
+        const long long n = (long long)bn * blk;
+        const int L_ = sch.nlev;
+        if (prec == UCFD_PREC_FP32) {
+            float *x = tmp32.ensure(n);
+            kfast::gather_rows<double, float>(bn, blk, identity ? nullptr : perm.p, b, x, s);
+            for (int l = 0; l < L_; ++l)
+                kfast::pc_lower<float>(blk, sch.lev_off[l], sch.lev_off[l + 1], bn, L.P, L.col.p, L.val32.p, LU32.p, x,
+                                       0, s);
+            for (int l = L_ - 1; l >= 0; --l)
+                kfast::pc_upper<float>(blk, sch.lev_off[l], sch.lev_off[l + 1], bn, U.P, U.col.p, U.val32.p, LU32.p, x,
+                                       0, s);
+            kfast::scatter_rows<float, double>(bn, blk, identity ? nullptr : perm.p, x, b, s);
+        } else {
+            double *x = b;
+            if (!identity) {
+                x = tmp64.ensure(n);
+                kfast::gather_rows<double, double>(bn, blk, perm.p, b, x, s);
+            }
+            const bool ex = prec == UCFD_PREC_FP64;
+            for (int l = 0; l < L_; ++l) {
+                if (ex)
+                    kexact::pc_lower<double>(blk, sch.lev_off[l], sch.lev_off[l + 1], bn, L.P, L.col.p, L.val.p,
+                                             LU64.p, x, 0, s);
+                else
+                    kfast::pc_lower<double>(blk, sch.lev_off[l], sch.lev_off[l + 1], bn, L.P, L.col.p, L.val.p,
+                                            LU64.p, x, 0, s);
+            }
+            for (int l = L_ - 1; l >= 0; --l) {
+                if (ex)
+                    kexact::pc_upper<double>(blk, sch.lev_off[l], sch.lev_off[l + 1], bn, U.P, U.col.p, U.val.p,
+                                             LU64.p, x, 0, s);
+                else
+                    kfast::pc_upper<double>(blk, sch.lev_off[l], sch.lev_off[l + 1], bn, U.P, U.col.p, U.val.p,
+                                            LU64.p, x, 0, s);
+            }
+            if (!identity) kfast::scatter_rows<double, double>(bn, blk, perm.p, x, b, s);
+        }
+    }
+};
+
+// ===========================================================================
+// Solver (GMRES)
+// ===========================================================================
+struct _Solver {
+    const char *type_name = nullptr;
+    double tol = 1e-5, haptol = 1e-12;  // solver.c:10-11
+    int maxiter = -1, itnum = 0;
+    double residual = 0.0;
+    int stat = INITIALIZED;
+    bool trace = false;
+    std::vector<double> hist;
+    int n = 0, m = 0;
+    int prec = UCFD_PREC_FP64;
+    long long arnoldi = 0;
+    long long ldv = 0;
+    DevBuf<double> V, w, r, H, cs, sn, y, h2, part, abeta;
+    DevBuf<unsigned char> st;
+    DevBuf<double> sx, sb;
+    PinnedBuf<double> h_abeta;
+    PinnedBuf<unsigned char> h_st;
+
+    void alloc() {
+        ldv = ((long long)n + 31) / 32 * 32;
+        V.ensure((size_t)ldv * (m + 1));
+        w.ensure(n);
+        r.ensure(n);
+        H.ensure((size_t)(m + 1) * m);
+        cs.ensure(m + 1);
+        sn.ensure(m + 1);
+        y.ensure(m + 1);
+        h2.ensure(m + 1);
+        part.ensure((size_t)kfast::gm_blocks(n) * 32 + 64);
+        abeta.ensure(2);
+        st.ensure(kfast::gm_state_bytes());
+        h_abeta.ensure(2);
+        h_st.ensure(kfast::gm_state_bytes());
+    }
+
+    // gmres.c:42-129 on the device.
+    void solve(SpMat A, Precon pc, double *x, const double *b, cudaStream_t s) {
+        const int ld = m + 1;
+        const int nb = kfast::gm_blocks(n);
+        const bool mixed = prec == UCFD_PREC_FP32;
+        UCFD_CUDA(cudaMemsetAsync(st.p, 0, kfast::gm_state_bytes(), s));
+        int iter = 0;
+        double ab = 0.0;
+        bool breakdown = false;
+        if (trace) hist.assign(std::max(maxiter, 0), 0.0);
+        stat = INITIALIZED;
+        while (iter < maxiter) {
+            // r = b - A x, abeta = ||r||  (true residual, FP64 values)
+            UCFD_CUDA(cudaMemcpyAsync(r.p, b, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+            A->mult(-1.0, x, 1.0, r.p, false, s);
+            kfast::norm2_to(n, r.p, part.p, abeta.p, s);
+            UCFD_CUDA(cudaMemcpyAsync(h_abeta.p, abeta.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+            UCFD_CUDA(cudaStreamSynchronize(s));
+            ab = h_abeta.p[0];
+            if (trace && iter < (int)hist.size()) hist[iter] = ab;
+            if (ab <= tol) {
+                stat = CONVERGED;
+                break;
+            }
+            pc->apply(r.p, s);
+            kfast::gm_sumsq(n, r.p, part.p, s);
+            kfast::gm_cycle_begin(nb, part.p, st.p, y.p, nullptr, s);
+            kfast::gm_scale(n, st.p, r.p, V.p, s);
+            for (int j = 0; j < m; ++j) {
+                const double *vj = V.p + (size_t)j * ldv;
+                A->mult(1.0, vj, 0.0, w.p, mixed, s);
+                pc->apply(w.p, s);
+                const int K = j + 1;
+                double *Hc = H.p + (size_t)j * ld;
+                kfast::gm_dots(n, K, V.p, ldv, w.p, part.p, s);
+                kfast::gm_reduce(nb, K, part.p, Hc, 0, s);
+                kfast::gm_update(n, K, V.p, ldv, Hc, w.p, 0, part.p, s);
+                kfast::gm_reduce(nb, K, part.p, h2.p, 0, s);
+                kfast::gm_update(n, K, V.p, ldv, h2.p, w.p, 1, part.p, s);
+                kfast::gm_givens(j, ld, nb, part.p, H.p, h2.p, cs.p, sn.p, y.p, haptol, st.p, s);
+                kfast::gm_scale(n, st.p, w.p, V.p + (size_t)(j + 1) * ldv, s);
+            }
+            kfast::gm_backsub(ld, H.p, y.p, st.p, s);
+            kfast::gm_solution(n, V.p, ldv, y.p, st.p, x, s);
+            UCFD_CHECK_LAUNCH();
+            UCFD_CUDA(cudaMemcpyAsync(h_st.p, st.p, kfast::gm_state_bytes(), cudaMemcpyDeviceToHost, s));
+            UCFD_CUDA(cudaStreamSynchronize(s));
+            const int *sti = (const int *)h_st.p;  // {k, stop, total}
+            if (sti[1]) breakdown = true;
+            arnoldi = sti[2];
+            iter++;
+        }
+        if (iter == maxiter) stat = REACH_ITERMAX;
+        else if (stat != CONVERGED && breakdown) stat = HAPPYBREAKDOWN;
+        residual = ab;
+        itnum = iter;
+    }
+};
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+// ---- SpMat -------------------------------------------------------------------
+ucfd_status_t UCFDMatInit(SpMat *mat) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(mat, "null SpMat pointer");
+    *mat = new _SpMat();
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDMatDestroy(SpMat *mat) {
+    UCFD_API_BEGIN
+    if (!mat || !*mat) return UCFD_SUCCESS;
+    delete *mat;
+    *mat = nullptr;
+    UCFD_API_END
+}
+
+static ucfd_status_t mat_create(SpMat *mat, const char *type, UCFDInt bn, UCFDInt blk, UCFDInt *rowptr,
+                                UCFDInt *colidx, UCFDReal *values) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(mat, "null SpMat pointer");
+    UCFD_REQUIRE(bn > 0 && blk > 0 && blk <= 7, "bad sizes bn=%d blk=%d (blk 1..7)", bn, blk);
+    UCFD_REQUIRE(rowptr && colidx && values, "null matrix array");
+    std::unique_ptr<_SpMat> m(new _SpMat());
+    m->type_name = type;
+    m->bn = bn;
+    m->blk = blk;
+    m->rowptr = rowptr;
+    m->colidx = colidx;
+    m->values = values;
+    m->load(false);
+    *mat = m.release();
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDMatCreateCSR(SpMat *mat, UCFDInt n, UCFDInt *rowptr, UCFDInt *colidx, UCFDReal *values) {
+    return mat_create(mat, CSR, n, 1, rowptr, colidx, values);
+}
+ucfd_status_t UCFDMatCreateBSR(SpMat *mat, UCFDInt bn, UCFDInt blk, UCFDInt *rowptr, UCFDInt *colidx,
+                               UCFDReal *values) {
+    return mat_create(mat, BSR, bn, blk, rowptr, colidx, values);
+}
+ucfd_status_t UCFDMatCreateCUDACSR(SpMat *mat, UCFDInt n, UCFDInt *rowptr, UCFDInt *colidx, UCFDReal *values) {
+    return mat_create(mat, CSRCUDA, n, 1, rowptr, colidx, values);
+}
+ucfd_status_t UCFDMatCreateCUDABSR(SpMat *mat, UCFDInt bn, UCFDInt blk, UCFDInt *rowptr, UCFDInt *colidx,
+                                   UCFDReal *values) {
+    return mat_create(mat, BSRCUDA, bn, blk, rowptr, colidx, values);
+}
+
+ucfd_status_t UCFDMatUpdateValues(SpMat mat) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(mat && mat->type_name, "matrix not created");
+    const bool had32 = mat->ell.val32.p != nullptr;
+    mat->load(had32);
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDMatGetType(SpMat mat, const char **type_name) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(mat && type_name, "null argument");
+    *type_name = mat->type_name;
+    UCFD_API_END
+}
+
+static ucfd_status_t mat_mult(UCFDReal alpha, SpMat mat, UCFDReal *x, UCFDReal beta, UCFDReal *y, bool fp32) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(mat && mat->type_name && mat->ready, "Matrix type must be set");
+    UCFD_REQUIRE(x && y, "null vector");
+    cudaStream_t s = kstream();
+    const size_t n = (size_t)mat->bn * mat->blk;
+    const double *xd = device_view<double>(x, n, mat->sx, s);
+    const bool ydev = is_device_ptr(y);
+    double *yd = ydev ? y : const_cast<double *>(device_view<double>(y, n, mat->sy, s));
+    mat->mult(alpha, xd, beta, yd, fp32, s);
+    UCFD_CHECK_LAUNCH();
+    if (!ydev) UCFD_CUDA(cudaMemcpyAsync(y, yd, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    UCFD_CUDA(cudaStreamSynchronize(s));
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDMatMult(UCFDReal alpha, SpMat mat, UCFDReal *x, UCFDReal beta, UCFDReal *y) {
+    return mat_mult(alpha, mat, x, beta, y, false);
+}
+ucfd_status_t UCFDMatMultFP32(UCFDReal alpha, SpMat mat, UCFDReal *x, UCFDReal beta, UCFDReal *y) {
+    return mat_mult(alpha, mat, x, beta, y, true);
+}
+
+// ---- Precon ------------------------------------------------------------------
+ucfd_status_t UCFDPreconCreatefromArrays(Precon *pc, UCFDInt *rowptr, UCFDInt *colidx, UCFDInt *diagslots,
+                                         UCFDReal *values) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(pc, "null Precon pointer");
+    UCFD_REQUIRE(rowptr && colidx && diagslots && values, "null preconditioner array");
+    std::unique_ptr<_Precon> p(new _Precon());
+    p->rowptr = rowptr;
+    p->colidx = colidx;
+    p->diagslots = diagslots;
+    p->values = values;
+    *pc = p.release();
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDPreconCreateNone(Precon *pc) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(pc, "null Precon pointer");
+    std::unique_ptr<_Precon> p(new _Precon());
+    p->type_name = NONE;
+    p->none = true;
+    *pc = p.release();
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDPreconDestroy(Precon *pc) {
+    UCFD_API_BEGIN
+    if (!pc || !*pc) return UCFD_SUCCESS;
+    delete *pc;
+    *pc = nullptr;
+    UCFD_API_END
+}
+
+static ucfd_status_t pc_set(Precon *pc, const char *type, UCFDInt bn, UCFDInt block, UCFDInt ncolors,
+                            UCFDInt *icolors) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(pc && *pc, "Preconditioner must be initialized");
+    UCFD_REQUIRE(bn > 0 && block > 0 && block <= 7, "bad sizes bn=%d block=%d", bn, block);
+    Precon p = *pc;
+    p->type_name = type;
+    p->bn = bn;
+    p->blk = block;
+    p->colored = icolors != nullptr;
+    if (icolors) {
+        UCFD_REQUIRE(ncolors > 0, "ncolors must be positive");
+        to_host(icolors, (size_t)ncolors + 1, p->icolors);
+        p->ncolors = ncolors;
+    }
+    p->prepared = false;
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDPreconSetBLUSGS(Precon *pc, UCFDInt bn, UCFDInt block) {
+    return pc_set(pc, BLUSGS, bn, block, 0, nullptr);
+}
+ucfd_status_t UCFDPreconSetPBLUSGS(Precon *pc, UCFDInt bn, UCFDInt block, UCFDInt ncolors, UCFDInt *icolors) {
+    if (!icolors) return UCFD_ERR_ARGUMENT;
+    return pc_set(pc, PBLUSGS, bn, block, ncolors, icolors);
+}
+ucfd_status_t UCFDPreconSetCUDABLUSGS(Precon *pc, UCFDInt bn, UCFDInt block, UCFDInt ncolors, UCFDInt *icolors) {
+    if (!icolors) return UCFD_ERR_ARGUMENT;
+    return pc_set(pc, CUDABLUSGS, bn, block, ncolors, icolors);
+}
+
+ucfd_status_t UCFDPreconSetPrecision(Precon pc, int precision) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(pc, "null Precon");
+    UCFD_REQUIRE(precision == UCFD_PREC_FP64 || precision == UCFD_PREC_FP64_FMA || precision == UCFD_PREC_FP32,
+                 "unknown precision %d", precision);
+    pc->prec = precision;
+    pc->prepared = false;
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDPreconPrepare(Precon pc) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(pc && pc->type_name, "Preconditioner type must be set");
+    pc->prepare();
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDPreconGetLevels(Precon pc, UCFDInt *nlevels) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(pc && nlevels, "null argument");
+    UCFD_REQUIRE(pc->prepared, "UCFDPreconPrepare has not been called");
+    *nlevels = pc->sch.nlev;
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDPreconApply(Precon pc, UCFDReal *b) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(pc && pc->type_name, "Preconditioner type must be set");
+    UCFD_REQUIRE(b, "null vector");
+    if (pc->none) return UCFD_SUCCESS;
+    cudaStream_t s = kstream();
+    const size_t n = (size_t)pc->bn * pc->blk;
+    const bool dev = is_device_ptr(b);
+    double *bd = dev ? b : const_cast<double *>(device_view<double>(b, n, pc->stage_b, s));
+    pc->apply(bd, s);
+    UCFD_CHECK_LAUNCH();
+    if (!dev) UCFD_CUDA(cudaMemcpyAsync(b, bd, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    UCFD_CUDA(cudaStreamSynchronize(s));
+    UCFD_API_END
+}
+
+// ---- Solver ------------------------------------------------------------------
+ucfd_status_t UCFDSolverInit(Solver *solver) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(solver, "null Solver pointer");
+    *solver = new _Solver();
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDSolverDestroy(Solver *solver) {
+    UCFD_API_BEGIN
+    if (!solver || !*solver) return UCFD_SUCCESS;
+    delete *solver;
+    *solver = nullptr;
+    UCFD_API_END
+}
+
+static ucfd_status_t gmres_create(Solver *solver, UCFDInt n, UCFDInt m, UCFDInt maxiter, UCFDReal tol) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(solver, "null Solver pointer");
+    UCFD_REQUIRE(n > 0 && m > 0 && m < 32 && maxiter >= 0, "bad GMRES sizes n=%d m=%d (m < 32) maxiter=%d", n, m,
+                 maxiter);
+    ensure_device();
+    std::unique_ptr<_Solver> s(new _Solver());
+    s->type_name = GMRES;
+    s->n = n;
+    s->m = m;
+    s->maxiter = maxiter;
+    s->tol = tol;
+    s->alloc();
+    *solver = s.release();
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDSolverCreateGMRES(Solver *solver, UCFDInt n, UCFDInt m, UCFDInt maxiter, UCFDReal tol) {
+    return gmres_create(solver, n, m, maxiter, tol);
+}
+ucfd_status_t UCFDSolverCreateCUDAGMRES(Solver *solver, UCFDInt n, UCFDInt m, UCFDInt maxiter, UCFDReal tol) {
+    return gmres_create(solver, n, m, maxiter, tol);
+}
+
+ucfd_status_t UCFDSolverSetPrecision(Solver solver, int precision) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(solver, "null Solver");
+    UCFD_REQUIRE(precision == UCFD_PREC_FP64 || precision == UCFD_PREC_FP64_FMA || precision == UCFD_PREC_FP32,
+                 "unknown precision %d", precision);
+    solver->prec = precision;
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDSolverSetHappyTol(Solver solver, UCFDReal haptol) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(solver, "null Solver");
+    solver->haptol = haptol;
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDSolve(Solver solver, Precon pc, SpMat A, UCFDReal *x, UCFDReal *b) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(solver && solver->type_name, "Solver must be initialized");
+    UCFD_REQUIRE(pc && pc->type_name, "Preconditioner must be initialized");
+    UCFD_REQUIRE(A && A->type_name && A->ready, "Matrix must be constructed");
+    UCFD_REQUIRE(x && b, "null vector");
+    UCFD_REQUIRE((long long)A->bn * A->blk == solver->n, "matrix size %lld != solver size %d",
+                 (long long)A->bn * A->blk, solver->n);
+    if (!pc->none) {
+        UCFD_REQUIRE(pc->bn == A->bn && pc->blk == A->blk, "preconditioner and matrix sizes differ");
+        if (!pc->prepared) pc->prepare();
+    }
+    cudaStream_t s = kstream();
+    const size_t n = solver->n;
+    const bool xdev = is_device_ptr(x);
+    double *xd = xdev ? x : const_cast<double *>(device_view<double>(x, n, solver->sx, s));
+    const double *bd = device_view<double>(b, n, solver->sb, s);
+    solver->solve(A, pc, xd, bd, s);
+    if (!xdev) UCFD_CUDA(cudaMemcpyAsync(x, xd, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    UCFD_CUDA(cudaStreamSynchronize(s));
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDSolverGetResult(Solver solver, UCFDInt *stat, UCFDInt *iter, UCFDReal *residual) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(solver, "null Solver");
+    if (stat) *stat = solver->stat;
+    if (iter) *iter = solver->itnum;
+    if (residual) *residual = solver->residual;
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDSolverGetArnoldiSteps(Solver solver, UCFDInt *steps) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(solver && steps, "null argument");
+    *steps = (UCFDInt)solver->arnoldi;
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDSolverTraceResidualHistory(Solver solver) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(solver, "null Solver");
+    solver->trace = true;
+    solver->hist.assign(std::max(solver->maxiter, 0), 0.0);
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDSolverGetResidualHistory(Solver solver, UCFDReal *hist) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(solver && hist, "null argument");
+    UCFD_REQUIRE(solver->trace, "Tracing residual unset");
+    std::memcpy(hist, solver->hist.data(), solver->hist.size() * sizeof(double));
+    UCFD_API_END
+}
+
+}  // extern "C"

@@ -1,0 +1,120 @@
+// launch.h -- host-callable launchers of the device kernels.
+//
+// The same declarations exist in two namespaces, one per build of the
+// kernel source:
+//   kexact  built with -fmad=false (no FMA contraction), FP64 instantiations:
+//           bit-for-bit the reference arithmetic (UCFD_PREC_FP64);
+//   kfast   built with FMA contraction, FP64 and FP32 instantiations
+//           (UCFD_PREC_FP64_FMA, UCFD_PREC_FP32) and the GMRES reductions.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "kargs.h"
+
+#define UCFD_DECLARE_LAUNCHERS                                                                     \
+    /* ---- scalar LU-SGS ---- */                                                                  \
+    template <typename T>                                                                          \
+    void scalar_sweep(const ::ucfd::ScalarSweepArgs<T> &a, int nv, int nfv, int ndims, int rans,   \
+                      int block, cudaStream_t s);                                                  \
+    template <typename T>                                                                          \
+    void legacy_pre(int neles, int nface, T factor, const T *fnorm_vol, const T *dt, T *diag,      \
+                    const T *fspr, cudaStream_t s);                                                \
+    template <typename T>                                                                          \
+    void legacy_update(int neles, int k0, int k1, T *upts, const T *rhs, cudaStream_t s);          \
+    template <typename T>                                                                          \
+    void fs_lusgs_pack(int neles, int nvars, int nfvars, long long N, double turb_factor,          \
+                       double a0, const int *cell_ids, const int *iperm, const double *upts,       \
+                       const double *rhs, const double *dt, const double *dsrc, T *u, T *du,       \
+                       T *diag, cudaStream_t s);                                                   \
+    template <typename T>                                                                          \
+    void fs_lusgs_update(int neles, int nvars, long long N, const int *cell_ids, const int *iperm, \
+                         const T *du, double *upts, cudaStream_t s);                               \
+    template <typename T>                                                                          \
+    void fs_lusgs_prepare(long long N, int maxdeg, int nv0, int nv1, T kappa, const int *nei,      \
+                          const T *fa, const T *rv, const T *lam, const T *base, T *diag,          \
+                          cudaStream_t s);                                                         \
+    template <typename Td>                                                                         \
+    void gather_idx(long long n, const int *idx, const double *src, Td *dst, cudaStream_t s);      \
+    void pair_reduce(int nblocks, const double *part, double *out, cudaStream_t s);                \
+    /* ---- block LU-SGS ---- */                                                                   \
+    template <typename S>                                                                          \
+    void fs_blusgs_pack(int neles, int nvars, int B, long long N, double a0, const int *cell_ids,   \
+                        const int *iperm, const double *rhs, const double *dt, S *rhs_s,           \
+                        double *rhs64, double *D, cudaStream_t s);                                 \
+    void fs_tblusgs_pack(int model, int neles, int nvars, int nt, long long N, double a0,          \
+                         double factor, double betast, const int *cell_ids, const int *iperm,      \
+                         const double *uptsb, const double *dsrc, const double *dt, double *D,     \
+                         cudaStream_t s);                                                          \
+    template <typename S>                                                                          \
+    void fs_blusgs_prepare(int B, long long N, int P, long long nF, const int *nei,               \
+                           const int *slot, const int8_t *side, const double *fa,                  \
+                           const double *rv, const double *jmat, double *D, double *LU64,          \
+                           S *LU_s, S *J_s, double *J64, cudaStream_t s);                          \
+    template <typename S>                                                                          \
+    void fs_blusgs_sweep(int B, int t0, int t1, long long N, int P, int var0, const int *nei,      \
+                         const S *fa, const S *rv, const S *J, const S *LU, const S *rhs, S *du,   \
+                         int block, cudaStream_t s);                                               \
+    template <typename Sx, typename R>                                                             \
+    void fs_blusgs_residual(int B, long long N, int P, int var0, int nvars, const int *nei,        \
+                            const double *fa, const double *rv, const double *J64,                 \
+                            const double *D, const double *rhs64, const Sx *x, R *r_out,           \
+                            double *part, int nblocks_max, int *nblocks_used, cudaStream_t s);     \
+    template <typename S>                                                                          \
+    void fs_blusgs_subres(int neles, int nvars, long long N, const int *cell_ids,                  \
+                          const int *iperm, const double *vol, const S *du, S *dup, double *res,   \
+                          cudaStream_t s);                                                         \
+    template <typename S>                                                                          \
+    void fs_blusgs_update(int neles, int nvars, long long N, const int *cell_ids,                  \
+                          const int *iperm, const S *du, double *upts, cudaStream_t s);            \
+    /* ---- Krylov ---- */                                                                         \
+    template <typename Tv, typename Ta>                                                            \
+    void bsr_spmv(int B, int bn, int P, const int *col, const Tv *val, double alpha,               \
+                  const double *x, double beta, double *y, int block, cudaStream_t s);             \
+    template <typename Tl>                                                                         \
+    void pc_prepare(int B, int bn, const int *perm, const long long *dslot, const double *values,  \
+                    double *LU64, Tl *LU_l, cudaStream_t s);                                       \
+    template <typename T>                                                                          \
+    void pc_lower(int B, int t0, int t1, int bn, int PL, const int *Lcol, const T *Lval,           \
+                  const T *LU, T *b, int block, cudaStream_t s);                                   \
+    template <typename T>                                                                          \
+    void pc_upper(int B, int t0, int t1, int bn, int PU, const int *Ucol, const T *Uval,           \
+                  const T *LU, T *b, int block, cudaStream_t s);                                   \
+    template <typename Ts, typename Td>                                                            \
+    void gather_rows(int bn, int B, const int *perm, const Ts *src, Td *dst, cudaStream_t s);      \
+    template <typename Ts, typename Td>                                                            \
+    void scatter_rows(int bn, int B, const int *perm, const Ts *src, Td *dst, cudaStream_t s);     \
+    template <typename Ts, typename Td>                                                            \
+    void convert(long long n, const Ts *src, Td *dst, cudaStream_t s);                             \
+    template <typename Ts>                                                                         \
+    void axpy_into(long long n, const Ts *x, double *y, cudaStream_t s);                           \
+    template <typename S>                                                                          \
+    void axpy_norm(long long n, const S *x, S *y, double *part, double *out, cudaStream_t s);      \
+    /* ---- GMRES pieces ---- */                                                                   \
+    int gm_blocks(long long n);                                                                    \
+    void gm_dots(long long n, int K, const double *V, long long ldv, const double *w,              \
+                 double *part, cudaStream_t s);                                                    \
+    void gm_update(long long n, int K, const double *V, long long ldv, const double *h, double *w, \
+                   int mode, double *part, cudaStream_t s);                                        \
+    void gm_reduce(int nblocks, int K, const double *part, double *out, int accumulate,            \
+                   cudaStream_t s);                                                                \
+    void gm_sumsq(long long n, const double *x, double *part, cudaStream_t s);                     \
+    void gm_cycle_begin(int nblocks, const double *part, void *st, double *y, double *out_norm,    \
+                        cudaStream_t s);                                                           \
+    void gm_scale(long long n, const void *st, const double *src, double *dst, cudaStream_t s);    \
+    void gm_givens(int j, int ld, int nblocks, const double *part_norm, double *H,                 \
+                   const double *h2, double *cs, double *sn, double *y, double haptol, void *st,   \
+                   cudaStream_t s);                                                                \
+    void gm_backsub(int ld, const double *H, double *y, const void *st, cudaStream_t s);           \
+    void gm_solution(long long n, const double *V, long long ldv, const double *y,                 \
+                     const void *st, double *x, cudaStream_t s);                                   \
+    size_t gm_state_bytes();                                                                       \
+    void norm2_to(long long n, const double *x, double *part, double *out, cudaStream_t s);
+
+namespace kexact {
+UCFD_DECLARE_LAUNCHERS
+}
+namespace kfast {
+UCFD_DECLARE_LAUNCHERS
+}

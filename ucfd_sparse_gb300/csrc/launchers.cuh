@@ -1,0 +1,353 @@
+// launchers.cuh -- definitions of the launch.h declarations for the
+// namespace UCFD_KNS; included once by each kernel translation unit.
+#pragma once
+
+#include "launch.h"
+#include "kernels_lusgs.cuh"
+#include "kernels_blusgs.cuh"
+#include "kernels_krylov.cuh"
+#include "ucfd_internal.h"
+
+namespace UCFD_KNS {
+
+// ---- scalar LU-SGS ---------------------------------------------------------
+template <typename T, int NV, int NFV, int NDIMS, bool RANS>
+static void sweep_go(const ::ucfd::ScalarSweepArgs<T> &a, int block, cudaStream_t s) {
+    const long long n = a.t1 - a.t0;
+    if (n <= 0) return;
+    scalar_sweep_kernel<T, NV, NFV, NDIMS, RANS><<<grid_for(n, block), block, 0, s>>>(a);
+}
+
+template <typename T>
+void scalar_sweep(const ::ucfd::ScalarSweepArgs<T> &a, int nv, int nfv, int ndims, int rans,
+                  int block, cudaStream_t s) {
+    if (block <= 0) block = kBlock;
+#define UCFD_SW(NV, NFV, ND)                                                   \
+    if (nv == NV && nfv == NFV && ndims == ND) {                               \
+        if (rans) {                                                            \
+            if constexpr (NV > NFV) return sweep_go<T, NV, NFV, ND, true>(a, block, s); \
+        } else {                                                               \
+            return sweep_go<T, NV, NFV, ND, false>(a, block, s);               \
+        }                                                                      \
+    }
+    UCFD_SW(5, 5, 3)
+    UCFD_SW(6, 5, 3)
+    UCFD_SW(7, 5, 3)
+    UCFD_SW(4, 4, 2)
+    UCFD_SW(5, 4, 2)
+    UCFD_SW(6, 4, 2)
+#undef UCFD_SW
+    ::ucfd::fail(UCFD_ERR_UNSUPPORTED,
+                 "scalar sweep for nvars=%d nfvars=%d ndims=%d (%s) is not built (supported: "
+                 "ndims 3 with nfvars 5, ndims 2 with nfvars 4, up to 2 turbulence variables)",
+                 nv, nfv, ndims, rans ? "RANS" : "NS");
+}
+
+template <typename T>
+void legacy_pre(int neles, int nface, T factor, const T *fnorm_vol, const T *dt, T *diag,
+                const T *fspr, cudaStream_t s) {
+    if (neles <= 0) return;
+    legacy_pre_kernel<T><<<grid_for(neles), kBlock, 0, s>>>(neles, nface, factor, fnorm_vol, dt, diag, fspr);
+}
+
+template <typename T>
+void legacy_update(int neles, int k0, int k1, T *upts, const T *rhs, cudaStream_t s) {
+    if (neles <= 0 || k1 <= k0) return;
+    legacy_update_kernel<T><<<grid_for(neles), kBlock, 0, s>>>(neles, k0, k1, upts, rhs);
+}
+
+template <typename T>
+void fs_lusgs_pack(int neles, int nvars, int nfvars, long long N, double turb_factor, double a0,
+                   const int *cell_ids, const int *iperm, const double *upts, const double *rhs,
+                   const double *dt, const double *dsrc, T *u, T *du, T *diag, cudaStream_t s) {
+    if (neles <= 0) return;
+    fs_lusgs_pack_kernel<T><<<grid_for(neles), kBlock, 0, s>>>(neles, nvars, nfvars, N, turb_factor, a0,
+                                                                cell_ids, iperm, upts, rhs, dt, dsrc, u,
+                                                                du, diag);
+}
+
+template <typename T>
+void fs_lusgs_update(int neles, int nvars, long long N, const int *cell_ids, const int *iperm,
+                     const T *du, double *upts, cudaStream_t s) {
+    if (neles <= 0) return;
+    fs_lusgs_update_kernel<T><<<grid_for(neles), kBlock, 0, s>>>(neles, nvars, N, cell_ids, iperm, du, upts);
+}
+
+template <typename T>
+void fs_lusgs_prepare(long long N, int maxdeg, int nv0, int nv1, T kappa, const int *nei,
+                      const T *fa, const T *rv, const T *lam, const T *base, T *diag, cudaStream_t s) {
+    if (N <= 0) return;
+    fs_lusgs_prepare_kernel<T><<<grid_for(N), kBlock, 0, s>>>(N, maxdeg, nv0, nv1, kappa, nei, fa, rv, lam,
+                                                              base, diag);
+}
+
+template <typename Td>
+void gather_idx(long long n, const int *idx, const double *src, Td *dst, cudaStream_t s) {
+    if (n <= 0) return;
+    gather_idx_kernel<Td><<<grid_for(n < (1ll << 24) ? n : (1ll << 24)), kBlock, 0, s>>>(n, idx, src, dst);
+}
+
+__global__ void pair_reduce_kernel(int nblocks, const double *part, double *out) {
+    double a = 0.0, b = 0.0;
+    for (int i = 0; i < nblocks; ++i) {
+        a += part[2 * i];
+        b += part[2 * i + 1];
+    }
+    out[0] = a;
+    out[1] = b;
+}
+
+// out[0], out[1] = sums of the (r^2, rhs^2) pairs written by the residual kernel.
+void pair_reduce(int nblocks, const double *part, double *out, cudaStream_t s) {
+    pair_reduce_kernel<<<1, 1, 0, s>>>(nblocks, part, out);
+}
+
+// ---- block LU-SGS ----------------------------------------------------------
+#define UCFD_BSW(B, CALL)                 \
+    switch (B) {                          \
+        case 1: { constexpr int BB = 1; CALL; break; } \
+        case 2: { constexpr int BB = 2; CALL; break; } \
+        case 4: { constexpr int BB = 4; CALL; break; } \
+        case 5: { constexpr int BB = 5; CALL; break; } \
+        default: ::ucfd::fail(UCFD_ERR_UNSUPPORTED, "block size %d not built (1, 2, 4, 5)", B); \
+    }
+
+template <typename S>
+void fs_blusgs_pack(int neles, int nvars, int B, long long N, double a0, const int *cell_ids,
+                    const int *iperm, const double *rhs, const double *dt, S *rhs_s, double *rhs64,
+                    double *D, cudaStream_t s) {
+    if (neles <= 0) return;
+    fs_blusgs_pack_kernel<S><<<grid_for(neles), kBlock, 0, s>>>(neles, nvars, B, N, a0, cell_ids, iperm,
+                                                                 rhs, dt, rhs_s, rhs64, D);
+}
+
+void fs_tblusgs_pack(int model, int neles, int nvars, int nt, long long N, double a0, double factor,
+                     double betast, const int *cell_ids, const int *iperm, const double *uptsb,
+                     const double *dsrc, const double *dt, double *D, cudaStream_t s) {
+    if (neles <= 0) return;
+    fs_tblusgs_pack_kernel<<<grid_for(neles), kBlock, 0, s>>>(model, neles, nvars, nt, N, a0, factor, betast,
+                                                              cell_ids, iperm, uptsb, dsrc, dt, D);
+}
+
+template <typename S>
+void fs_blusgs_prepare(int B, long long N, int P, long long nF, const int *nei, const int *slot,
+                       const int8_t *side, const double *fa, const double *rv, const double *jmat,
+                       double *D, double *LU64, S *LU_s, S *J_s, double *J64, cudaStream_t s) {
+    if (N <= 0) return;
+    UCFD_BSW(B, (fs_blusgs_prepare_kernel<S, BB><<<grid_for(N, 128), 128, 0, s>>>(
+                    N, P, nF, nei, slot, side, fa, rv, jmat, D, LU64, LU_s, J_s, J64)));
+}
+
+template <typename S>
+void fs_blusgs_sweep(int B, int t0, int t1, long long N, int P, int var0, const int *nei, const S *fa,
+                     const S *rv, const S *J, const S *LU, const S *rhs, S *du, int block,
+                     cudaStream_t s) {
+    if (t1 <= t0) return;
+    if (block <= 0) block = kBlock;
+    UCFD_BSW(B, (fs_blusgs_sweep_kernel<S, BB><<<grid_for(t1 - t0, block), block, 0, s>>>(
+                    t0, t1, N, P, var0, nei, fa, rv, J, LU, rhs, du)));
+}
+
+template <typename Sx, typename R>
+void fs_blusgs_residual(int B, long long N, int P, int var0, int nvars, const int *nei,
+                        const double *fa, const double *rv, const double *J64, const double *D,
+                        const double *rhs64, const Sx *x, R *r_out, double *part, int nblocks_max,
+                        int *nblocks_used, cudaStream_t s) {
+    const unsigned g = grid_for(N);
+    if ((int)g > nblocks_max) ::ucfd::fail(UCFD_ERR_ARGUMENT, "residual partial buffer too small");
+    *nblocks_used = (int)g;
+    UCFD_BSW(B, (fs_blusgs_residual_kernel<Sx, R, BB><<<g, kBlock, 0, s>>>(
+                    N, P, var0, nvars, nei, fa, rv, J64, D, rhs64, x, r_out, part)));
+}
+
+template <typename S>
+void fs_blusgs_subres(int neles, int nvars, long long N, const int *cell_ids, const int *iperm,
+                      const double *vol, const S *du, S *dup, double *res, cudaStream_t s) {
+    if (neles <= 0) return;
+    fs_blusgs_subres_kernel<S><<<grid_for(neles), kBlock, 0, s>>>(neles, nvars, N, cell_ids, iperm, vol, du,
+                                                                   dup, res);
+}
+
+template <typename S>
+void fs_blusgs_update(int neles, int nvars, long long N, const int *cell_ids, const int *iperm,
+                      const S *du, double *upts, cudaStream_t s) {
+    if (neles <= 0) return;
+    fs_blusgs_update_kernel<S><<<grid_for(neles), kBlock, 0, s>>>(neles, nvars, N, cell_ids, iperm, du, upts);
+}
+
+// ---- Krylov ----------------------------------------------------------------
+#define UCFD_KSW(B, CALL)                 \
+    switch (B) {                          \
+        case 1: { constexpr int BB = 1; CALL; break; } \
+        case 2: { constexpr int BB = 2; CALL; break; } \
+        case 3: { constexpr int BB = 3; CALL; break; } \
+        case 4: { constexpr int BB = 4; CALL; break; } \
+        case 5: { constexpr int BB = 5; CALL; break; } \
+        case 6: { constexpr int BB = 6; CALL; break; } \
+        case 7: { constexpr int BB = 7; CALL; break; } \
+        default: ::ucfd::fail(UCFD_ERR_UNSUPPORTED, "block size %d not built (1..7)", B); \
+    }
+
+template <typename Tv, typename Ta>
+void bsr_spmv(int B, int bn, int P, const int *col, const Tv *val, double alpha, const double *x,
+              double beta, double *y, int block, cudaStream_t s) {
+    if (bn <= 0) return;
+    if (block <= 0) block = kBlock;
+    UCFD_KSW(B, (bsr_spmv_kernel<Tv, Ta, BB><<<grid_for(bn, block), block, 0, s>>>(bn, P, col, val, alpha, x,
+                                                                                   beta, y)));
+}
+
+template <typename Tl>
+void pc_prepare(int B, int bn, const int *perm, const long long *dslot, const double *values,
+                double *LU64, Tl *LU_l, cudaStream_t s) {
+    if (bn <= 0) return;
+    UCFD_KSW(B, (pc_prepare_kernel<Tl, BB><<<grid_for(bn, 128), 128, 0, s>>>(bn, perm, dslot, values, LU64,
+                                                                             LU_l)));
+}
+
+template <typename T>
+void pc_lower(int B, int t0, int t1, int bn, int PL, const int *Lcol, const T *Lval, const T *LU, T *b,
+              int block, cudaStream_t s) {
+    if (t1 <= t0) return;
+    if (block <= 0) block = kBlock;
+    UCFD_KSW(B, (pc_lower_kernel<T, BB><<<grid_for(t1 - t0, block), block, 0, s>>>(t0, t1, bn, PL, Lcol, Lval,
+                                                                                   LU, b)));
+}
+
+template <typename T>
+void pc_upper(int B, int t0, int t1, int bn, int PU, const int *Ucol, const T *Uval, const T *LU, T *b,
+              int block, cudaStream_t s) {
+    if (t1 <= t0) return;
+    if (block <= 0) block = kBlock;
+    UCFD_KSW(B, (pc_upper_kernel<T, BB><<<grid_for(t1 - t0, block), block, 0, s>>>(t0, t1, bn, PU, Ucol, Uval,
+                                                                                   LU, b)));
+}
+
+template <typename Ts, typename Td>
+void gather_rows(int bn, int B, const int *perm, const Ts *src, Td *dst, cudaStream_t s) {
+    const long long n = (long long)bn * B;
+    if (n <= 0) return;
+    gather_rows_kernel<Ts, Td><<<grid_for(n), kBlock, 0, s>>>(bn, B, perm, src, dst);
+}
+
+template <typename Ts, typename Td>
+void scatter_rows(int bn, int B, const int *perm, const Ts *src, Td *dst, cudaStream_t s) {
+    const long long n = (long long)bn * B;
+    if (n <= 0) return;
+    scatter_rows_kernel<Ts, Td><<<grid_for(n), kBlock, 0, s>>>(bn, B, perm, src, dst);
+}
+
+template <typename Ts, typename Td>
+__global__ void convert_kernel(long long n, const Ts *src, Td *dst) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        dst[i] = (Td)src[i];
+}
+
+template <typename Ts, typename Td>
+void convert(long long n, const Ts *src, Td *dst, cudaStream_t s) {
+    if (n <= 0) return;
+    convert_kernel<Ts, Td><<<grid_for(n < (1ll << 24) ? n : (1ll << 24)), kBlock, 0, s>>>(n, src, dst);
+}
+
+template <typename Ts>
+__global__ void axpy_into_kernel(long long n, const Ts *x, double *y) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        y[i] += (double)x[i];
+}
+
+template <typename Ts>
+void axpy_into(long long n, const Ts *x, double *y, cudaStream_t s) {
+    if (n <= 0) return;
+    axpy_into_kernel<Ts><<<grid_for(n < (1ll << 24) ? n : (1ll << 24)), kBlock, 0, s>>>(n, x, y);
+}
+
+// y += x and out = ||x||_2 accumulated in FP64 (pseudo-time update).
+template <typename S>
+__global__ void axpy_norm_kernel(long long n, const S *x, S *y, double *part) {
+    double t = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const S xv = x[i];
+        y[i] += xv;
+        t += (double)xv * (double)xv;
+    }
+    t = block_sum(t);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+__global__ void sqrt_sum_kernel(int nb, const double *part, double *out) {
+    double t = 0.0;
+    for (int b = 0; b < nb; ++b) t += part[b];
+    *out = sqrt(t);
+}
+
+// ---- GMRES pieces ----------------------------------------------------------
+// Reduction grids are capped so the per-block partial buffers stay small.
+constexpr int kRedBlocks = 1216;  // 8 x 152 SMs
+
+int gm_blocks(long long n) {
+    long long g = (n + kBlock - 1) / kBlock;
+    return (int)(g < kRedBlocks ? (g > 0 ? g : 1) : kRedBlocks);
+}
+
+void gm_dots(long long n, int K, const double *V, long long ldv, const double *w, double *part,
+             cudaStream_t s) {
+    gm_dots_kernel<<<gm_blocks(n), kBlock, 0, s>>>(n, K, V, ldv, w, part);
+}
+
+void gm_update(long long n, int K, const double *V, long long ldv, const double *h, double *w, int mode,
+               double *part, cudaStream_t s) {
+    gm_update_kernel<<<gm_blocks(n), kBlock, 0, s>>>(n, K, V, ldv, h, w, mode, part);
+}
+
+void gm_reduce(int nblocks, int K, const double *part, double *out, int accumulate, cudaStream_t s) {
+    gm_reduce_kernel<<<1, kMaxK, 0, s>>>(nblocks, K, part, out, accumulate);
+}
+
+void gm_sumsq(long long n, const double *x, double *part, cudaStream_t s) {
+    gm_sumsq_kernel<<<gm_blocks(n), kBlock, 0, s>>>(n, x, part);
+}
+
+void gm_cycle_begin(int nblocks, const double *part, void *st, double *y, double *out_norm, cudaStream_t s) {
+    gm_cycle_begin_kernel<<<1, 1, 0, s>>>(nblocks, part, (GmState *)st, y, out_norm);
+}
+
+void gm_scale(long long n, const void *st, const double *src, double *dst, cudaStream_t s) {
+    gm_scale_kernel<<<gm_blocks(n), kBlock, 0, s>>>(n, (const GmState *)st, src, dst);
+}
+
+void gm_givens(int j, int ld, int nblocks, const double *part_norm, double *H, const double *h2, double *cs,
+               double *sn, double *y, double haptol, void *st, cudaStream_t s) {
+    gm_givens_kernel<<<1, 1, 0, s>>>(j, ld, nblocks, part_norm, H, h2, cs, sn, y, haptol, (GmState *)st);
+}
+
+void gm_backsub(int ld, const double *H, double *y, const void *st, cudaStream_t s) {
+    gm_backsub_kernel<<<1, 1, 0, s>>>(ld, H, y, (const GmState *)st);
+}
+
+void gm_solution(long long n, const double *V, long long ldv, const double *y, const void *st, double *x,
+                 cudaStream_t s) {
+    gm_solution_kernel<<<gm_blocks(n), kBlock, 0, s>>>(n, V, ldv, y, (const GmState *)st, x);
+}
+
+size_t gm_state_bytes() { return sizeof(GmState); }
+
+template <typename S>
+void axpy_norm(long long n, const S *x, S *y, double *part, double *out, cudaStream_t s) {
+    const int nb = gm_blocks(n);
+    axpy_norm_kernel<S><<<nb, kBlock, 0, s>>>(n, x, y, part);
+    sqrt_sum_kernel<<<1, 1, 0, s>>>(nb, part, out);
+}
+
+__global__ void norm_finalize_kernel(int nblocks, const double *part, double *out) {
+    double t = 0.0;
+    for (int b = 0; b < nblocks; ++b) t += part[(long long)b * kMaxK];
+    *out = sqrt(t);
+}
+
+// out = ||x||_2 (two-pass, fixed order).
+void norm2_to(long long n, const double *x, double *part, double *out, cudaStream_t s) {
+    gm_sumsq_kernel<<<gm_blocks(n), kBlock, 0, s>>>(n, x, part);
+    norm_finalize_kernel<<<1, 1, 0, s>>>(gm_blocks(n), part, out);
+}
+
+}  // namespace UCFD_KNS
