@@ -1,0 +1,411 @@
+#!/usr/bin/env python
+"""Benchmark of the block LU-SGS hot path on one GB300.
+
+Workload (the 2.1M-cell hex configuration): 128^3 hexahedra on the unit
+cube, interior nodes jittered by +-0.2h, cell numbering randomly permuted
+(seed 0), greedy first-fit colouring, 5x5 face Jacobians A+ = sigma I + E,
+A- = -sigma I + E (E ~ N(0, 0.05^2), sigma ~ U[0.5, 2]), FP64 diagonal-block
+LU.  One step = one pseudo-time step of the FlowSys BLU-SGS API: Pack, NS
+Prepare (FP64 LU), Reset, solve of the block system to a 1e-10 relative
+residual, Update.  The solve runs FP32 sweeps inside FP64 iterative
+refinement; the same step with plain FP64 sweeps is timed for comparison.
+
+Metric: cell-updates/s, one cell-update = one cell visited by one symmetric
+(lower + upper) sweep pair; value = cells * pairs / step time, summed over
+ranks (replicas) for --gpus N.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "LU-SGS cell-updates/s & HBM GB/s @2.1M cells; FP32+refine vs FP64 @1e-10"
+UNIT = "cell-updates/s"
+
+
+# ---------------------------------------------------------------------------
+# multi-rank plumbing (replicas: no data-path collective)
+# ---------------------------------------------------------------------------
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def dist_init(backend):
+    import torch.distributed as dist
+    ws, rank, _ = dist_env()
+    if ws > 1 and not dist.is_initialized():
+        dist.init_process_group(backend=backend)
+    return dist if ws > 1 else None
+
+
+def reduce_max(x: float, dist, device=None) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(x: float, dist, device=None) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier(dist, device=None):
+    if dist is not None:
+        if device is not None and device.type == "cuda":
+            dist.barrier(device_ids=[device.index])
+        else:
+            dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.proc = None
+        self.path = os.path.join(tempfile.gettempdir(), f"ucfd_clocks_{os.getpid()}.csv")
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) >= 9:
+                rows.append(p)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+def make_case(m: int, seed: int = 0):
+    from ucfd_sparse_gb300 import meshgen as mg
+    return mg.blusgs_case(m, seed=seed)
+
+
+def sweep_bytes(rowptr: np.ndarray, elt: int, B: int = 5, lu_elt: int | None = None) -> int:
+    """Algorithmic bytes of one lower (or upper) BLU-SGS sweep over all
+    cells: per cell-face its neighbour index (4), face area (elt) and block
+    (B*B*elt); per cell rcp_vol, the LU block, rhs, and du read (as the
+    neighbours' data, once) and written."""
+    lu_elt = elt if lu_elt is None else lu_elt
+    nnz = int(rowptr[-1])
+    N = rowptr.shape[0] - 1
+    return nnz * (4 + elt + B * B * elt) + N * (elt + B * B * lu_elt + 3 * B * elt)
+
+
+class Problem:
+    """FlowSys objects on device-resident inputs (torch CUDA tensors)."""
+
+    def __init__(self, case, colour, prec, stream, device, host_inputs=False):
+        import torch
+
+        from ucfd_sparse_gb300.flowsys import FlowSys
+        self.case = case
+        if host_inputs:
+            conv = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        else:
+            conv = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(device)
+        m = {k: conv(case[k]) for k in ("rowptr", "colidx", "slots", "sides", "face_area", "face_normal",
+                                         "rcp_vol")}
+        self.S = FlowSys(case["nlocal"], 5, 5, 3, case["nfaces"], 1, m["rowptr"], m["colidx"], m["slots"],
+                         m["sides"], m["face_area"], m["face_normal"], m["rcp_vol"])
+        self.S.set_coloring(colour)
+        self.S.set_precision(prec)
+        if stream is not None and not host_inputs:
+            self.S.set_stream(stream.cuda_stream, True)
+        self.e = {k: conv(case[k]) for k in ("rhs", "dt", "cell_ids", "vol", "jmat")}
+        self.e["upts"] = conv(np.array(case["upts"]))
+        self.e["dsrc"] = conv(np.zeros_like(case["rhs"]))
+        self.e["res"] = conv(np.zeros_like(case["rhs"]))
+        e = self.e
+        self.S.set_element(0, case["neles"], 6, e["cell_ids"], e["upts"], e["rhs"], e["dt"], e["dsrc"], e["vol"],
+                           e["res"])
+        self.S.set_blusgs(e["jmat"])
+        self.nlev = self.S.levels()
+
+    def step(self, rtol, max_pairs, inner):
+        S = self.S
+        S.blusgs_pack(0, 0.0)
+        S.blusgs_ns_prepare()
+        S.blusgs_reset()
+        pairs, rel = S.blusgs_solve(rtol, max_pairs, inner)
+        S.blusgs_update(0)
+        return pairs, rel
+
+    def h2d_bytes(self):
+        c = self.case
+        return sum(np.asarray(c[k]).nbytes for k in ("rhs", "dt", "cell_ids", "jmat", "upts"))
+
+    def d2h_bytes(self):
+        return np.asarray(self.case["upts"]).nbytes
+
+
+def launches_per_step(nlev, pairs, inner, mixed):
+    outer = math.ceil(pairs / inner) if pairs else 0
+    n = 1 + 1 + 1                                  # pack, prepare, update
+    n += 2                                         # initial residual + reduction
+    n += outer * 2 + pairs * 2 * nlev              # residual per outer loop, sweeps
+    if mixed:
+        n += 2 + outer                             # conversions, x += delta
+    return n
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (the oracle: the reference's CPU path restated, or the
+# reference itself where it was compiled on this machine)
+# ---------------------------------------------------------------------------
+def cpu_baseline(case, pairs=1, repeats=1):
+    """One bounded sample: Pack, NS Prepare, `pairs` sweep pairs with
+    SubResidual, Update on the full mesh, with the reference's CPU code
+    (sweeps serial, update/sub-residual OpenMP as in blusgs.c)."""
+    from oracle import oracle as orc
+    kind = "reference" if orc.ref_available() else "port"
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    best = float("inf")
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        if kind == "reference":
+            orc.Ref(fast=True).flowsys_blusgs(case, case["rhs"], case["dt"], case["jmat"], case["vol"], case["upts"],
+                                             nsweeps=pairs)
+        else:
+            orc.Port(fast=True).flowsys_blusgs(case, case["rhs"], case["dt"], case["jmat"], case["vol"],
+                                              case["upts"], nsweeps=pairs)
+        best = min(best, time.perf_counter() - t0)
+    N = case["nlocal"]
+    return {"value": N * pairs / best, "unit": UNIT, "cores": threads, "kind": kind,
+            "sample": f"Pack+NSPrepare+{pairs} lower/upper sweep pair(s)+SubResidual+Update on all {N} cells, "
+                      f"FP64, best of {repeats}; sweeps serial as in the reference, {threads} OpenMP threads "
+                      f"available", "seconds": best}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    dist = dist_init("gloo")
+    if rank != 0:
+        barrier(dist)
+        return
+    case = make_case(args.mesh)
+    N = case["nlocal"]
+    for _ in range(max(args.warmup, 0)):
+        cpu_baseline(case, pairs=args.ref_pairs)
+    times = []
+    for _ in range(args.steps):
+        r = cpu_baseline(case, pairs=args.ref_pairs)
+        times.append(r["seconds"])
+    T = max(statistics.median(times), 1e-12)
+    val = N * args.ref_pairs / T
+    out = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": T * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"BLU-SGS 5x5, {args.mesh}^3 jittered permuted hex ({N} cells), CPU sample of "
+                                  f"{args.ref_pairs} sweep pair(s) per step", "cells": N},
+           "cpu_baseline": {"value": val, "unit": UNIT, "cores": r["cores"], "kind": r["kind"], "sample": r["sample"]},
+           "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+    barrier(dist)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    dist = dist_init("nccl")
+    from ucfd_sparse_gb300 import _build, lib
+    _build.build()
+    lib.load()
+    from ucfd_sparse_gb300 import coloredlusgs as cl
+
+    case = make_case(args.mesh, seed=args.seed + rank)
+    N = case["nlocal"]
+    ic, rg, lc = cl.greedy_coloring_csr(case["rowptr"], case["colidx"])
+    stream = torch.cuda.Stream(device=device)
+    P32 = Problem(case, lc, 2, stream, device)
+    P64 = Problem(case, lc, 1, stream, device)
+    nlev = P32.nlev
+
+    def timed(P, steps, warm):
+        for _ in range(warm):
+            P.step(args.rtol, args.max_pairs, args.inner)
+        torch.cuda.synchronize()
+        barrier(dist, device)
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        pairs_all, rels = [], []
+        ev0.record(stream)
+        for _ in range(steps):
+            p, r = P.step(args.rtol, args.max_pairs, args.inner)
+            pairs_all.append(p)
+            rels.append(r)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier(dist, device)
+        ms = ev0.elapsed_time(ev1) / steps
+        return reduce_max(ms, dist, device), pairs_all, rels
+
+    with ClockSampler(local) as clk:
+        ms32, pairs32, rel32 = timed(P32, args.steps, args.warmup)
+    clocks = clk.summary()
+    ms64, pairs64, rel64 = timed(P64, max(2, args.steps // 2), max(args.warmup, 3))
+    pairs_mean = statistics.mean(pairs32)
+    value_rank = N * pairs_mean / (ms32 * 1e-3)
+    value = reduce_sum(value_rank, dist, device) if dist else value_rank
+
+    # ---- dominant kernel: the FP32 sweep (roofline) -------------------------
+    P32.S.blusgs_pack(0, 0.0)
+    P32.S.blusgs_ns_prepare()
+    P32.S.blusgs_reset()
+    torch.cuda.synchronize()
+    nk = 20
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(nk):
+        P32.S.blusgs_ns_lower()
+        P32.S.blusgs_ns_upper()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    sweep_ms = ev0.elapsed_time(ev1) / (2 * nk)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    bytes_sweep = sweep_bytes(case["rowptr"], 4, 5, 4)
+    achieved = bytes_sweep / (sweep_ms * 1e-3) / 1e9
+    launch_bytes = bytes_sweep / nlev
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tf):
+        t = json.load(open(tf)).get("fs_blusgs_sweep_kernel<float,5>")
+        if t:
+            traffic = t["bytes_per_cell"] * N / nlev
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": traffic, "kernel": "fs_blusgs_sweep_kernel<float,5>",
+                "algorithmic_bytes_per_launch": launch_bytes, "launch_ms": sweep_ms / nlev,
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s"}
+
+    # ---- end to end through the C-ABI with pinned host buffers -------------
+    Ph = Problem(case, lc, 2, None, device, host_inputs=True)
+    for _ in range(max(1, args.warmup // 2)):
+        Ph.step(args.rtol, args.max_pairs, args.inner)
+    torch.cuda.synchronize()
+    barrier(dist, device)
+    t0 = time.perf_counter()
+    pe = []
+    for _ in range(args.steps):
+        pe.append(Ph.step(args.rtol, args.max_pairs, args.inner)[0])
+    torch.cuda.synchronize()
+    e2e_s = reduce_max((time.perf_counter() - t0) / args.steps, dist, device)
+    e2e_val = reduce_sum(N * statistics.mean(pe) / e2e_s, dist, device) if dist else N * statistics.mean(pe) / e2e_s
+
+    out = None
+    if rank == 0:
+        cpu = cpu_baseline(case, pairs=1) if ws == 1 else None
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 sweeps + f64 refinement/LU/residual", "data": "synthetic",
+            "config": {"workload": f"BLU-SGS 5x5 face Jacobians, {args.mesh}^3 jittered (+-0.2h) randomly permuted "
+                                   f"hex ({N} cells), greedy colouring ({len(rg)} colours), solve to rtol "
+                                   f"{args.rtol:g} per pseudo-time step", "cells": N, "colors": len(rg),
+                       "inner_sweeps": args.inner, "l2": "inputs larger than L2 (no flush needed)",
+                       "parallelism": f"replicas x{ws}"},
+            "pairs_per_step": pairs_mean, "relres": max(rel32),
+            "fp64": {"ms_per_step": ms64, "pairs_per_step": statistics.mean(pairs64), "relres": max(rel64),
+                     "value": N * statistics.mean(pairs64) / (ms64 * 1e-3)},
+            "speedup_fp32_refined_vs_fp64": ms64 / ms32,
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": Ph.h2d_bytes(),
+                    "d2h_bytes_per_step": Ph.d2h_bytes(), "ms_per_step": e2e_s * 1e3},
+            "gpu_launches": launches_per_step(nlev, int(round(pairs_mean)), args.inner, True) * args.steps,
+            "clocks": clocks,
+        }
+        print(json.dumps(out))
+    barrier(dist, device)
+    return out
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mesh", type=int, default=128)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--rtol", type=float, default=1e-10)
+    ap.add_argument("--inner", type=int, default=8)
+    ap.add_argument("--max-pairs", type=int, default=400)
+    ap.add_argument("--ref-pairs", type=int, default=1)
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,421 @@
+"""Test infrastructure: ctypes drivers of the CPU oracle.
+
+Two CPU implementations of the hot path are wrapped here, both used only as
+checkers by tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+bench.py:
+
+* ``Port``  -- oracle/ucfd_oracle.c, the C restatement of the reference
+  algorithm (built by ``make -C oracle port`` into oracle/_build/);
+* ``Ref``   -- the reference library itself, compiled from the reference
+  sources by ``make -C oracle ref`` into oracle/_ref/ (only where the
+  reference source tree is present).
+
+The functions below drive whole steps (pre/lower/upper/update, BLU-SGS
+sweeps, BSR/GMRES solves) on numpy arrays and return numpy results.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from ctypes import POINTER, byref, c_double, c_int, c_int8, c_void_p
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+REF = os.path.join(HERE, "_ref")
+REF_SRC = os.environ.get("UCFD_REFERENCE_SRC", "/root/reference")
+
+_I, _D, _P = c_int, c_double, c_void_p
+
+
+def build_port() -> None:
+    subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+
+
+def build_ref() -> bool:
+    """Compile the reference sources into oracle/_ref (False if absent)."""
+    if not os.path.isdir(os.path.join(REF_SRC, "src", "lusgs")):
+        return False
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"], check=True)
+    return True
+
+
+def ref_available() -> bool:
+    return os.path.exists(os.path.join(REF, "liblusgs_ref.so")) and os.path.exists(
+        os.path.join(REF, "libkrylov_ref.so"))
+
+
+def P(a):
+    return None if a is None else a.ctypes.data
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+# ---------------------------------------------------------------------------
+# the C restatement
+# ---------------------------------------------------------------------------
+class Port:
+    def __init__(self, fast: bool = False):
+        name = "liboracle_fast.so" if fast else "liboracle_pin.so"
+        path = os.path.join(BUILD, name)
+        if not os.path.exists(path):
+            build_port()
+        L = ctypes.CDLL(path)
+        sig = {
+            "oracle_set_constants": (None, [_D, _D]),
+            "oracle_lusgs_pack": (None, [_I, _I, _I, _I, _D, _D] + [_P] * 8),
+            "oracle_lusgs_update": (None, [_I, _I, _I, _P, _P, _P]),
+            "oracle_lusgs_prepare": (None, [_I, _I, _I, _D, _P, _P, _P, _P, _P, _P]),
+            "oracle_lusgs_lower": (None, [_I, _I, _I, _D, _P, _I, _I, _I, _I, _I] + [_P] * 10),
+            "oracle_lusgs_upper": (None, [_I, _I, _I, _D, _P, _I, _I, _I, _I, _I] + [_P] * 10),
+            "oracle_legacy_pre": (None, [_I, _I, _D, _P, _P, _P, _P]),
+            "oracle_legacy_sweep": (None, [_I, _I, _I, _I, _I, _I, _I, _I, _I] + [_P] * 10),
+            "oracle_legacy_serial_sweep": (None, [_I, _I, _I, _I, _I, _I, _I] + [_P] * 8),
+            "oracle_legacy_update": (None, [_I, _I, _I, _I, _P, _P]),
+            "oracle_ludcmp": (None, [_I, _P]),
+            "oracle_lusub": (None, [_I, _P, _P]),
+            "oracle_blusgs_pack": (None, [_I, _I, _I, _I, _D, _P, _P, _P, _P, _P]),
+            "oracle_tblusgs_pack": (None, [_I, _I, _I, _I, _I, _D, _D, _P, _P, _P, _P, _P]),
+            "oracle_blusgs_update": (None, [_I, _I, _I, _P, _P, _P]),
+            "oracle_blusgs_sub_residual": (None, [_I, _I, _I, _P, _P, _P, _P, _P]),
+            "oracle_blusgs_prepare": (None, [_I, _I, _I] + [_P] * 7),
+            "oracle_blusgs_lower": (None, [_I, _I, _I, _I, _I] + [_P] * 10),
+            "oracle_blusgs_upper": (None, [_I, _I, _I, _I, _I] + [_P] * 10),
+            "oracle_bsr_spmv": (None, [_I, _I, _P, _P, _P, _D, _P, _D, _P]),
+            "oracle_blusgs_precon_prepare": (None, [_I, _I, _P, _P, _P]),
+            "oracle_blusgs_precon_apply": (None, [_I, _I, _P, _P, _P, _P, _P, _P]),
+            "oracle_pblusgs_precon_apply": (None, [_I, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
+            "oracle_gmres": (_I, [_I, _I, _P, _P, _P, _I, _I, _P, _P, _P, _I, _I, _D, _D, _P, _P,
+                                  POINTER(c_int), POINTER(c_double), _P]),
+        }
+        for n, (r, a) in sig.items():
+            f = getattr(L, n)
+            f.restype = r
+            f.argtypes = a
+        self.L = L
+
+    # ---- colored array API ------------------------------------------------
+    def legacy_step(self, c: dict, icolor, ranges, lcolor, nsteps: int = 1, rans: bool = False,
+                    nfvars: int = 5, ndims: int = 3):
+        """nsteps colored LU-SGS steps; returns (upts, rhs, dub, diag)."""
+        N, nf, nv = c["neles"], c["nface"], c["nvars"]
+        upts, rhs = c["upts"].copy(), c["rhs"].copy()
+        dub = np.zeros_like(rhs)
+        diag = np.zeros(N)
+        icolor, lcolor = _i32(icolor), _i32(lcolor)
+        nei, fnv, vec, fspr, dt = _i32(c["nei_ele"]), _f64(c["fnorm_vol"]), _f64(c["vec_fnorm"]), _f64(
+            c["fspr"]), _f64(c["dt"])
+        bounds = [0] + list(ranges)
+        for _ in range(nsteps):
+            rhs[:] = c["rhs"]
+            self.L.oracle_legacy_pre(N, nf, 1.0, P(fnv), P(dt), P(diag), P(fspr))
+            for k in range(len(ranges)):
+                self.L.oracle_legacy_sweep(0, int(rans), bounds[k], bounds[k + 1], N, nf, nv, nfvars, ndims, P(nei),
+                                           P(icolor), P(lcolor), P(fnv), P(vec), P(upts), P(rhs), P(dub), P(diag),
+                                           P(fspr))
+            for k in reversed(range(len(ranges))):
+                self.L.oracle_legacy_sweep(1, int(rans), bounds[k], bounds[k + 1], N, nf, nv, nfvars, ndims, P(nei),
+                                           P(icolor), P(lcolor), P(fnv), P(vec), P(upts), P(rhs), P(dub), P(diag),
+                                           P(fspr))
+            self.L.oracle_legacy_update(int(rans), N, nv, nfvars, P(upts), P(rhs))
+        return upts, rhs, dub, diag
+
+    def legacy_serial_step(self, c: dict, nfvars=5, ndims=3, rans=False):
+        N, nf, nv = c["neles"], c["nface"], c["nvars"]
+        upts, rhs = c["upts"].copy(), c["rhs"].copy()
+        dub = np.zeros_like(rhs)
+        diag = np.zeros(N)
+        nei, fnv, vec, fspr, dt = _i32(c["nei_ele"]), _f64(c["fnorm_vol"]), _f64(c["vec_fnorm"]), _f64(
+            c["fspr"]), _f64(c["dt"])
+        self.L.oracle_legacy_pre(N, nf, 1.0, P(fnv), P(dt), P(diag), P(fspr))
+        for up in (0, 1):
+            self.L.oracle_legacy_serial_sweep(up, int(rans), N, nf, nv, nfvars, ndims, P(nei), P(fnv), P(vec),
+                                              P(upts), P(rhs), P(dub), P(diag), P(fspr))
+        self.L.oracle_legacy_update(int(rans), N, nv, nfvars, P(upts), P(rhs))
+        return upts, rhs, dub, diag
+
+    # ---- FlowSys scalar LU-SGS --------------------------------------------
+    def flowsys_lusgs_step(self, fs: dict, upts, rhs, dt, dsrc, fspr, tfspr=None, kappa=1.0, a0=0.0,
+                           turb_factor=1.0, rans=False, nsteps=1):
+        """Pack / NSPrepare / NS lower / NS upper [/ RANS ...] / Update."""
+        N, nv, nfv = fs["nlocal"], fs["nvars"], fs["nfvars"]
+        ndims, nF = fs.get("ndims", 3), fs["nfaces"]
+        neles = dt.shape[0]
+        ids = _i32(fs["cell_ids"])
+        upts = _f64(upts).copy()
+        u = np.zeros(nv * N)
+        du = np.zeros(nv * N)
+        diag = np.zeros(nv * N)
+        rp, ci, sl, sd = _i32(fs["rowptr"]), _i32(fs["colidx"]), _i32(fs["slots"]), np.ascontiguousarray(
+            fs["sides"], dtype=np.int8)
+        fa, fn, rv = _f64(fs["face_area"]), _f64(fs["face_normal"]), _f64(fs["rcp_vol"])
+        rhs, dt, dsrc, fspr = _f64(rhs), _f64(dt), _f64(dsrc), _f64(fspr)
+        tf = _f64(tfspr) if tfspr is not None else None
+        for _ in range(nsteps):
+            self.L.oracle_lusgs_pack(N, neles, nv, nfv, turb_factor, a0, P(ids), P(upts), P(rhs), P(dt), P(dsrc),
+                                     P(u), P(du), P(diag))
+            self.L.oracle_lusgs_prepare(N, 0, nfv, kappa, P(rp), P(sl), P(fa), P(rv), P(fspr), P(diag))
+            g = (P(rp), P(ci), P(sd), P(sl), P(fa), P(fn), P(rv), P(diag), P(u), P(du))
+            self.L.oracle_lusgs_lower(0, 0, nfv, kappa, P(fspr), N, nv, nfv, ndims, nF, *g)
+            self.L.oracle_lusgs_upper(0, 0, nfv, kappa, P(fspr), N, nv, nfv, ndims, nF, *g)
+            if rans:
+                self.L.oracle_lusgs_prepare(N, nfv, nv, kappa, P(rp), P(sl), P(fa), P(rv), P(tf), P(diag))
+                self.L.oracle_lusgs_lower(1, nfv, nv, kappa, P(tf), N, nv, nfv, ndims, nF, *g)
+                self.L.oracle_lusgs_upper(1, nfv, nv, kappa, P(tf), N, nv, nfv, ndims, nF, *g)
+            self.L.oracle_lusgs_update(N, neles, nv, P(ids), P(du), P(upts))
+        return upts, du.reshape(nv, N), diag.reshape(nv, N)
+
+    # ---- FlowSys BLU-SGS ---------------------------------------------------
+    def flowsys_blusgs(self, fs: dict, rhs, dt, jmat, vol, upts, nsweeps=1, a0=0.0):
+        """Pack / NSPrepare / Reset / (lower, upper, SubResidual) x nsweeps /
+        Update.  Returns (upts, du [N][nv] AoS, resid [nv][neles], LU diag)."""
+        N, nv, nfv, nF = fs["nlocal"], fs["nvars"], fs["nfvars"], fs["nfaces"]
+        neles = dt.shape[0]
+        ids = _i32(fs["cell_ids"])
+        rp, ci, sl, sd = _i32(fs["rowptr"]), _i32(fs["colidx"]), _i32(fs["slots"]), np.ascontiguousarray(
+            fs["sides"], dtype=np.int8)
+        fa, rv = _f64(fs["face_area"]), _f64(fs["rcp_vol"])
+        rhs, dt, jmat, vol = _f64(rhs), _f64(dt), _f64(jmat), _f64(vol)
+        upts = _f64(upts).copy()
+        rrhs = np.zeros(N * nv)
+        diag = np.zeros(N * nfv * nfv)
+        du = np.zeros(N * nv)
+        dup = np.zeros(N * nv)
+        res = np.zeros(nv * neles)
+        self.L.oracle_blusgs_pack(N, neles, nv, nfv, a0, P(ids), P(rhs), P(dt), P(rrhs), P(diag))
+        self.L.oracle_blusgs_prepare(N, nfv, nF, P(rp), P(sl), P(sd), P(fa), P(rv), P(diag), P(jmat))
+        for _ in range(nsweeps):
+            g = (P(rp), P(ci), P(sd), P(sl), P(fa), P(rv), P(rrhs), P(diag), P(jmat), P(du))
+            self.L.oracle_blusgs_lower(0, nfv, N, nv, nF, *g)
+            self.L.oracle_blusgs_upper(0, nfv, N, nv, nF, *g)
+            self.L.oracle_blusgs_sub_residual(N, neles, nv, P(ids), P(vol), P(du), P(dup), P(res))
+        self.L.oracle_blusgs_update(N, neles, nv, P(ids), P(du), P(upts))
+        return upts, du.reshape(N, nv), res.reshape(nv, neles), diag.reshape(N, nfv, nfv)
+
+    # ---- Krylov -------------------------------------------------------------
+    def bsr_spmv(self, s: dict, x, alpha=1.0, beta=0.0, y=None):
+        bn, blk = s["bn"], s["blk"]
+        y = np.zeros(bn * blk) if y is None else _f64(y).copy()
+        x = _f64(x)
+        self.L.oracle_bsr_spmv(bn, blk, P(_i32(s["rowptr"])), P(_i32(s["colidx"])), P(_f64(s["values"])), alpha,
+                               P(x), beta, P(y))
+        return y
+
+    def precon_diag(self, s: dict):
+        bn, blk = s["bn"], s["blk"]
+        d = np.zeros(bn * blk * blk)
+        self.L.oracle_blusgs_precon_prepare(bn, blk, P(_i32(s["diagslots"])), P(_f64(s["values"])), P(d))
+        return d
+
+    def precon_apply(self, s: dict, b, icolors=None):
+        bn, blk = s["bn"], s["blk"]
+        d = self.precon_diag(s)
+        b = _f64(b).copy()
+        args = (P(_i32(s["rowptr"])), P(_i32(s["colidx"])), P(_i32(s["diagslots"])), P(_f64(s["values"])), P(d),
+                P(b))
+        if icolors is None:
+            self.L.oracle_blusgs_precon_apply(bn, blk, *args)
+        else:
+            ic = _i32(icolors)
+            self.L.oracle_pblusgs_precon_apply(bn, blk, len(ic) - 1, P(ic), *args)
+        return b
+
+    def gmres(self, s: dict, b, m=30, maxiter=50, tol=1e-10, pc="blusgs", icolors=None, haptol=1e-12, x0=None):
+        bn, blk = s["bn"], s["blk"]
+        kind = {"none": 0, "blusgs": 1, "pblusgs": 2}[pc]
+        d = self.precon_diag(s) if kind else np.zeros(1)
+        ic = _i32(icolors) if icolors is not None else np.zeros(1, dtype=np.int32)
+        x = np.zeros(bn * blk) if x0 is None else _f64(x0).copy()
+        it, res = c_int(), c_double()
+        hist = np.zeros(maxiter + 1)
+        st = self.L.oracle_gmres(bn, blk, P(_i32(s["rowptr"])), P(_i32(s["colidx"])), P(_f64(s["values"])), kind,
+                                 len(ic) - 1, P(ic), P(_i32(s["diagslots"])), P(d), m, maxiter, tol, haptol, P(x),
+                                 P(_f64(b)), byref(it), byref(res), P(hist))
+        return x, st, it.value, res.value, hist[:it.value + 1]
+
+
+# ---------------------------------------------------------------------------
+# the reference library compiled from its own sources
+# ---------------------------------------------------------------------------
+class Ref:
+    def __init__(self, fast: bool = False):
+        sfx = "_fast" if fast else ""
+        self.lus = ctypes.CDLL(os.path.join(REF, f"liblusgs_ref{sfx}.so"))
+        self.kry = ctypes.CDLL(os.path.join(REF, f"libkrylov_ref{sfx}.so"))
+        H = POINTER(c_void_p)
+        for n, a in {
+            "UCFDFlowSysCreate": [H, _I, _I, _I, _I, _I, _I] + [_P] * 7,
+            "UCFDFlowSysSetElement": [H, _I, _I, _I] + [_P] * 7,
+            "UCFDFlowSysDestroy": [H],
+            "UCFDFlowSysSetLUSGS": [H, _P, _P],
+            "UCFDFlowSysSetBLUSGS": [H, _P, _P],
+            "UCFDLUSGS_Pack": [_P, _I, _D, _D],
+            "UCFDLUSGS_Update": [_P, _I],
+            "UCFDLUSGS_NSPrepare": [_P, _D],
+            "UCFDLUSGS_RANSPrepare": [_P, _D],
+            "UCFDLUSGS_NSLowerSweep": [_P, _D],
+            "UCFDLUSGS_NSUpperSweep": [_P, _D],
+            "UCFDLUSGS_RANSLowerSweep": [_P, _D],
+            "UCFDLUSGS_RANSUpperSweep": [_P, _D],
+            "UCFDBLUSGS_Pack": [_P, _I, _D],
+            "UCFDBLUSGS_KWSST_Pack": [_P, _I, _D, _D],
+            "UCFDBLUSGS_SA_Pack": [_P, _I, _D, _D],
+            "UCFDBLUSGS_NSPrepare": [_P],
+            "UCFDBLUSGS_RANSPrepare": [_P],
+            "UCFDBLUSGS_NSLowerSweep": [_P],
+            "UCFDBLUSGS_NSUpperSweep": [_P],
+            "UCFDBLUSGS_RANSLowerSweep": [_P],
+            "UCFDBLUSGS_RANSUpperSweep": [_P],
+            "UCFDBLUSGS_SubResidual": [_P, _I],
+            "UCFDBLUSGS_Update": [_P, _I],
+            "UCFDBLUSGS_Reset": [_P],
+        }.items():
+            f = getattr(self.lus, n)
+            f.restype = _I
+            f.argtypes = a
+        for n, a in {
+            "UCFDMatCreateBSR": [H, _I, _I, _P, _P, _P],
+            "UCFDMatMult": [_D, _P, _P, _D, _P],
+            "UCFDMatDestroy": [H],
+            "UCFDPreconCreatefromArrays": [H, _P, _P, _P, _P],
+            "UCFDPreconSetBLUSGS": [H, _I, _I],
+            "UCFDPreconSetPBLUSGS": [H, _I, _I, _I, _P],
+            "UCFDPreconPrepare": [_P],
+            "UCFDPreconDestroy": [H],
+            "UCFDSolverCreateGMRES": [H, _I, _I, _I, _D],
+            "UCFDSolve": [_P, _P, _P, _P, _P],
+            "UCFDSolverGetResult": [_P, POINTER(c_int), POINTER(c_int), POINTER(c_double)],
+            "UCFDSolverTraceResidualHistory": [_P],
+            "UCFDSolverGetResidualHistory": [_P, _P],
+            "UCFDSolverDestroy": [H],
+        }.items():
+            f = getattr(self.kry, n)
+            f.restype = _I
+            f.argtypes = a
+
+    def _sys(self, fs, nelem=1):
+        h = c_void_p()
+        keep = [_i32(fs["rowptr"]), _i32(fs["colidx"]), _i32(fs["slots"]),
+                np.ascontiguousarray(fs["sides"], dtype=np.int8), _f64(fs["face_area"]), _f64(fs["face_normal"]),
+                _f64(fs["rcp_vol"])]
+        self.lus.UCFDFlowSysCreate(byref(h), fs["nlocal"], fs["nvars"], fs["nfvars"], fs.get("ndims", 3),
+                                   fs["nfaces"], nelem, *[P(a) for a in keep])
+        return h, keep
+
+    def flowsys_lusgs_step(self, fs, upts, rhs, dt, dsrc, fspr, tfspr=None, kappa=1.0, a0=0.0, turb_factor=1.0,
+                           rans=False, nsteps=1):
+        h, keep = self._sys(fs)
+        upts = _f64(upts).copy()
+        rhs, dt, dsrc, fspr = _f64(rhs), _f64(dt), _f64(dsrc), _f64(fspr)
+        tf = _f64(tfspr) if tfspr is not None else None
+        ids = _i32(fs["cell_ids"])
+        neles = dt.shape[0]
+        res = np.zeros_like(upts)
+        vol = np.ones(neles)
+        self.lus.UCFDFlowSysSetLUSGS(byref(h), P(fspr), P(tf))
+        self.lus.UCFDFlowSysSetElement(byref(h), 0, neles, 6, P(ids), P(upts), P(rhs), P(dt), P(dsrc), P(vol),
+                                       P(res))
+        for _ in range(nsteps):
+            self.lus.UCFDLUSGS_Pack(h, 0, turb_factor, a0)
+            self.lus.UCFDLUSGS_NSPrepare(h, kappa)
+            self.lus.UCFDLUSGS_NSLowerSweep(h, kappa)
+            self.lus.UCFDLUSGS_NSUpperSweep(h, kappa)
+            if rans:
+                self.lus.UCFDLUSGS_RANSPrepare(h, kappa)
+                self.lus.UCFDLUSGS_RANSLowerSweep(h, kappa)
+                self.lus.UCFDLUSGS_RANSUpperSweep(h, kappa)
+            self.lus.UCFDLUSGS_Update(h, 0)
+        self.lus.UCFDFlowSysDestroy(byref(h))
+        return upts
+
+    def flowsys_blusgs(self, fs, rhs, dt, jmat, vol, upts, nsweeps=1, a0=0.0):
+        h, keep = self._sys(fs)
+        upts = _f64(upts).copy()
+        rhs, dt, jmat, vol = _f64(rhs), _f64(dt), _f64(jmat), _f64(vol)
+        ids = _i32(fs["cell_ids"])
+        neles = dt.shape[0]
+        res = np.zeros_like(upts)
+        dsrc = np.zeros_like(upts)
+        self.lus.UCFDFlowSysSetBLUSGS(byref(h), P(jmat), None)
+        self.lus.UCFDFlowSysSetElement(byref(h), 0, neles, 6, P(ids), P(upts), P(rhs), P(dt), P(dsrc), P(vol),
+                                       P(res))
+        self.lus.UCFDBLUSGS_Pack(h, 0, a0)
+        self.lus.UCFDBLUSGS_NSPrepare(h)
+        self.lus.UCFDBLUSGS_Reset(h)
+        for _ in range(nsweeps):
+            self.lus.UCFDBLUSGS_NSLowerSweep(h)
+            self.lus.UCFDBLUSGS_NSUpperSweep(h)
+            self.lus.UCFDBLUSGS_SubResidual(h, 0)
+        self.lus.UCFDBLUSGS_Update(h, 0)
+        self.lus.UCFDFlowSysDestroy(byref(h))
+        return upts, res
+
+    def bsr_spmv(self, s, x, alpha=1.0, beta=0.0, y=None):
+        h = c_void_p()
+        rp, ci, v = _i32(s["rowptr"]), _i32(s["colidx"]), _f64(s["values"])
+        self.kry.UCFDMatCreateBSR(byref(h), s["bn"], s["blk"], P(rp), P(ci), P(v))
+        y = np.zeros(s["bn"] * s["blk"]) if y is None else _f64(y).copy()
+        x = _f64(x)
+        self.kry.UCFDMatMult(alpha, h, P(x), beta, P(y))
+        self.kry.UCFDMatDestroy(byref(h))
+        return y
+
+    def gmres(self, s, b, m=30, maxiter=50, tol=1e-10):
+        """Natural-order BLU-SGS preconditioned GMRES of the reference."""
+        A, pc, sv = c_void_p(), c_void_p(), c_void_p()
+        rp, ci, v, ds = _i32(s["rowptr"]), _i32(s["colidx"]), _f64(s["values"]), _i32(s["diagslots"])
+        self.kry.UCFDMatCreateBSR(byref(A), s["bn"], s["blk"], P(rp), P(ci), P(v))
+        self.kry.UCFDPreconCreatefromArrays(byref(pc), P(rp), P(ci), P(ds), P(v))
+        self.kry.UCFDPreconSetBLUSGS(byref(pc), s["bn"], s["blk"])
+        self.kry.UCFDPreconPrepare(pc)
+        n = s["bn"] * s["blk"]
+        self.kry.UCFDSolverCreateGMRES(byref(sv), n, m, maxiter, tol)
+        self.kry.UCFDSolverTraceResidualHistory(sv)
+        x = np.zeros(n)
+        b = _f64(b)
+        self.kry.UCFDSolve(sv, pc, A, P(x), P(b))
+        st, it, res = c_int(), c_int(), c_double()
+        self.kry.UCFDSolverGetResult(sv, byref(st), byref(it), byref(res))
+        hist = np.zeros(maxiter)
+        self.kry.UCFDSolverGetResidualHistory(sv, P(hist))
+        self.kry.UCFDSolverDestroy(byref(sv))
+        self.kry.UCFDPreconDestroy(byref(pc))
+        self.kry.UCFDMatDestroy(byref(A))
+        return x, st.value, it.value, res.value, hist
+
+
+# ---------------------------------------------------------------------------
+# colored array layout -> FlowSys layout (the colour-renumbered mesh)
+# ---------------------------------------------------------------------------
+def legacy_to_flowsys(c: dict, icolor, nfvars: int = 5, ndims: int = 3) -> dict:
+    """FlowSys arrays equal to the colored array API on a colour-renumbered
+    mesh: rank k = position of the cell in icolor, rowptr = nf*k, one CSR
+    entry per cell face (self entries at the boundary), slots = f*N + cell,
+    sides = +1, face_area = fnorm_vol, rcp_vol = 1, face_normal[d][f*N+i] =
+    vec_fnorm[f][d][i].  With kappa = 1, a0 = 0, dsrc = 0 and the element
+    cell_ids = new rank of each cell, the reference's natural-order FlowSys
+    sweeps perform exactly the colored sweeps' arithmetic."""
+    N, nf = c["neles"], c["nface"]
+    icolor = np.asarray(icolor, dtype=np.int64)
+    newid = np.empty(N, dtype=np.int64)
+    newid[icolor] = np.arange(N)
+    nei = np.asarray(c["nei_ele"], dtype=np.int64)
+    rowptr = (np.arange(N + 1) * nf).astype(np.int32)
+    colidx = newid[nei[:, icolor]].T.reshape(-1).astype(np.int32)          # [k][f]
+    slots = (np.arange(nf)[None, :] * N + icolor[:, None]).reshape(-1).astype(np.int32)
+    sides = np.ones(N * nf, dtype=np.int8)
+    face_area = np.ascontiguousarray(np.asarray(c["fnorm_vol"]).reshape(-1))
+    vec = np.asarray(c["vec_fnorm"])                                        # [f][d][i]
+    face_normal = np.ascontiguousarray(vec.transpose(1, 0, 2).reshape(ndims, nf * N))
+    return dict(nlocal=N, nvars=c["nvars"], nfvars=nfvars, ndims=ndims, nfaces=nf * N, rowptr=rowptr,
+                colidx=colidx, slots=slots, sides=sides, face_area=face_area, face_normal=face_normal,
+                rcp_vol=np.ones(N), cell_ids=newid.astype(np.int32),
+                fspr=np.ascontiguousarray(np.asarray(c["fspr"]).reshape(-1)))

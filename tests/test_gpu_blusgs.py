@@ -1,0 +1,160 @@
+"""GPU parity of the block LU-SGS FlowSys path against the oracle, and the
+mixed-precision (FP32 sweeps + FP64 refinement) solve to 1e-10."""
+import numpy as np
+import pytest
+import torch
+
+from tests.golden import cases
+
+pytestmark = pytest.mark.gpu
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def make(b, prec=0, on_device=False, colored=None, nvars=None):
+    from ucfd_sparse_gb300.flowsys import FlowSys
+    conv = dev if on_device else np.ascontiguousarray
+    m = {k: conv(b[k]) for k in ("rowptr", "colidx", "slots", "sides", "face_area", "face_normal", "rcp_vol")}
+    nv = b["nvars"] if nvars is None else nvars
+    S = FlowSys(b["nlocal"], nv, b["nfvars"], 3, b["nfaces"], 1, m["rowptr"], m["colidx"], m["slots"], m["sides"],
+                m["face_area"], m["face_normal"], m["rcp_vol"])
+    if colored is not None:
+        S.set_coloring(np.ascontiguousarray(colored, dtype=np.int32))
+    S.set_precision(prec)
+    e = dict(upts=conv(np.array(b["upts"])), rhs=conv(b["rhs"]), dt=conv(b["dt"]), ids=conv(b["cell_ids"]),
+             vol=conv(b["vol"]), dsrc=conv(b.get("dsrc", np.zeros_like(b["rhs"]))),
+             res=conv(np.zeros_like(b["rhs"])))
+    S.set_element(0, b["neles"], 6, e["ids"], e["upts"], e["rhs"], e["dt"], e["dsrc"], e["vol"], e["res"])
+    S.set_blusgs(conv(b["jmat"]), conv(b["tjmat"]) if "tjmat" in b else None)
+    return S, e
+
+
+def host(x):
+    return x.cpu().numpy() if hasattr(x, "cpu") else x
+
+
+def run_sweeps(S, nsweeps):
+    S.blusgs_pack(0, 0.0)
+    S.blusgs_ns_prepare()
+    S.blusgs_reset()
+    for _ in range(nsweeps):
+        S.blusgs_ns_lower()
+        S.blusgs_ns_upper()
+        S.blusgs_sub_residual(0)
+    S.blusgs_update(0)
+
+
+@pytest.mark.parametrize("name", sorted(cases.BLUSGS))
+@pytest.mark.parametrize("on_device", [False, True])
+def test_blusgs_natural_order_bitexact(name, on_device, golden, ucfd):
+    meta, arr = golden
+    kw = cases.BLUSGS[name]
+    b = cases.blusgs_case(**kw)
+    S, e = make(b, on_device=on_device)
+    run_sweeps(S, kw["nsweeps"])
+    np.testing.assert_array_equal(host(e["upts"]), arr[f"{name}_upts"])
+    np.testing.assert_array_equal(host(e["res"]), arr[f"{name}_resid"])
+
+
+def test_blusgs_colored_equals_renumbered(port, ucfd):
+    from ucfd_sparse_gb300 import coloredlusgs as cl
+    from ucfd_sparse_gb300 import meshgen as mg
+    b = cases.blusgs_case(m=9, seed=5)
+    ic, rg, lc = cl.greedy_coloring_csr(b["rowptr"], b["colidx"])
+    S, e = make(b, colored=lc)
+    assert S.levels() == len(rg)
+    run_sweeps(S, 3)
+    new = np.empty(b["nlocal"], dtype=np.int64)
+    new[ic] = np.arange(b["nlocal"])
+    br = mg.renumber_flowsys(b, new)
+    up, du, res, _ = port.flowsys_blusgs(br, b["rhs"], b["dt"], b["jmat"], b["vol"], b["upts"], nsweeps=3)
+    np.testing.assert_array_equal(e["upts"], up)
+    np.testing.assert_array_equal(e["res"], res)
+
+
+def test_blusgs_fp64_fma_within_tolerance(golden, ucfd):
+    meta, arr = golden
+    b = cases.blusgs_case(**cases.BLUSGS["blu10"])
+    S, e = make(b, prec=1, on_device=True)
+    run_sweeps(S, 2)
+    ref = arr["blu10_upts"]
+    d = host(e["upts"]) - b["upts"]
+    r = ref - b["upts"]
+    assert np.abs(d - r).max() <= 1e-12 * np.abs(r).max()
+
+
+@pytest.mark.parametrize("prec", [0, 2])
+def test_blusgs_solve_reaches_1e10(prec, port, ucfd):
+    """Plain FP64 sweeps and FP32 sweeps + FP64 refinement both reach a
+    1e-10 relative residual; their solutions agree with the oracle run to
+    convergence."""
+    from ucfd_sparse_gb300 import coloredlusgs as cl
+    from ucfd_sparse_gb300 import meshgen as mg
+    b = cases.blusgs_case(m=12, seed=1)
+    ic, rg, lc = cl.greedy_coloring_csr(b["rowptr"], b["colidx"])
+    S, e = make(b, prec=prec, on_device=True, colored=lc)
+    S.blusgs_pack(0, 0.0)
+    S.blusgs_ns_prepare()
+    S.blusgs_reset()
+    n, rel = S.blusgs_solve(1e-10, 400, 8)
+    assert rel <= 1e-10, (n, rel)
+    assert S.blusgs_residual() <= 1e-10
+    S.blusgs_update(0)
+    new = np.empty(b["nlocal"], dtype=np.int64)
+    new[ic] = np.arange(b["nlocal"])
+    br = mg.renumber_flowsys(b, new)
+    up = port.flowsys_blusgs(br, b["rhs"], b["dt"], b["jmat"], b["vol"], b["upts"], nsweeps=n + 20)[0]
+    dq = up - b["upts"]
+    assert np.abs(host(e["upts"]) - up).max() <= 1e-8 * np.abs(dq).max()
+
+
+def test_blusgs_turbulence_packs_and_sweeps(port, ucfd):
+    """k-omega SST pack + RANS prepare/sweeps (blusgs.c:60-120, 260-270,
+    388-429) on a 7-variable system against the oracle."""
+    from oracle.oracle import P
+    from ucfd_sparse_gb300 import meshgen as mg
+    b = mg.blusgs_case(5, nvars=7, seed=3)
+    b["nfvars"] = 5
+    rng = np.random.default_rng(4)
+    N, nF = b["nlocal"], b["nfaces"]
+    b["upts"][5:] = rng.uniform(0.1, 1.0, (2, N))
+    b["dsrc"] = rng.uniform(0.0, 1.0, (7, N))
+    t = rng.normal(0.0, 0.05, (2, 2, 2, nF))
+    t[0, 0, 0] += 1.0; t[0, 1, 1] += 1.0; t[1, 0, 0] -= 1.0; t[1, 1, 1] -= 1.0
+    b["tjmat"] = t
+    b["jmat"] = np.ascontiguousarray(b["jmat"][:, :5, :5])
+    S, e = make(b)
+    S.blusgs_pack(0, 0.0)
+    S.blusgs_kwsst_pack(0, 1.5, 0.3)
+    S.blusgs_ns_prepare()
+    S.blusgs_rans_prepare()
+    S.blusgs_reset()
+    for _ in range(2):
+        S.blusgs_ns_lower(); S.blusgs_ns_upper()
+        S.blusgs_rans_lower(); S.blusgs_rans_upper()
+    S.blusgs_update(0)
+    # oracle
+    L = port.L
+    i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+    f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    rp, ci, sl = i32(b["rowptr"]), i32(b["colidx"]), i32(b["slots"])
+    sd = np.ascontiguousarray(b["sides"], dtype=np.int8)
+    fa, rv, ids = f64(b["face_area"]), f64(b["rcp_vol"]), i32(b["cell_ids"])
+    rhs, dt, up0, ds = f64(b["rhs"]), f64(b["dt"]), f64(b["upts"]), f64(b["dsrc"])
+    jm, tj = f64(b["jmat"]), f64(t)
+    rr, dg, tdg = np.zeros(N * 7), np.zeros(N * 25), np.zeros(N * 4)
+    du = np.zeros(N * 7)
+    upts = up0.copy()
+    L.oracle_blusgs_pack(N, N, 7, 5, 0.0, P(ids), P(rhs), P(dt), P(rr), P(dg))
+    L.oracle_tblusgs_pack(0, N, N, 7, 5, 0.3, 1.5, P(ids), P(up0), P(ds), P(dt), P(tdg))
+    L.oracle_blusgs_prepare(N, 5, nF, P(rp), P(sl), P(sd), P(fa), P(rv), P(dg), P(jm))
+    L.oracle_blusgs_prepare(N, 2, nF, P(rp), P(sl), P(sd), P(fa), P(rv), P(tdg), P(tj))
+    for _ in range(2):
+        for fn in (L.oracle_blusgs_lower, L.oracle_blusgs_upper):
+            fn(0, 5, N, 7, nF, P(rp), P(ci), P(sd), P(sl), P(fa), P(rv), P(rr), P(dg), P(jm), P(du))
+        for fn in (L.oracle_blusgs_lower, L.oracle_blusgs_upper):
+            fn(5, 2, N, 7, nF, P(rp), P(ci), P(sd), P(sl), P(fa), P(rv), P(rr), P(tdg), P(tj), P(du))
+    L.oracle_blusgs_update(N, N, 7, P(ids), P(du), P(upts))
+    np.testing.assert_array_equal(e["upts"], upts)

@@ -1,0 +1,130 @@
+"""GPU parity of the Krylov path: BSR SpMV, BLU-SGS preconditioners (natural
+and coloured) and GMRES(m), against the oracle."""
+import numpy as np
+import pytest
+import torch
+
+from tests.golden import cases
+
+pytestmark = pytest.mark.gpu
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def colour_renumbered(s):
+    from ucfd_sparse_gb300 import coloredlusgs as cl
+    from ucfd_sparse_gb300 import meshgen as mg
+    tab = np.where(s["nei"] >= 0, s["nei"], np.arange(s["bn"])[None, :]).astype(np.int32)
+    ic, rg, lc = cl.greedy_coloring(tab)
+    new = np.empty(s["bn"], dtype=np.int64)
+    new[ic] = np.arange(s["bn"])
+    return mg.renumber_bsr(s, new), [0] + rg
+
+
+@pytest.mark.parametrize("name", sorted(cases.KRYLOV))
+@pytest.mark.parametrize("on_device", [False, True])
+def test_spmv_bitexact(name, on_device, golden, ucfd):
+    from ucfd_sparse_gb300.krylov import SpMat
+    meta, arr = golden
+    s = cases.bsr_case(**cases.KRYLOV[name])
+    conv = dev if on_device else np.ascontiguousarray
+    A = SpMat(s["bn"], s["blk"], conv(s["rowptr"]), conv(s["colidx"]), conv(s["values"]), cuda=on_device)
+    x = cases.spmv_x(s)
+    y = conv(x.copy())
+    A.mult(1.5, conv(x), -0.5, y)
+    y = y.cpu().numpy() if on_device else y
+    np.testing.assert_array_equal(y, arr[f"{name}_spmv"])
+
+
+def test_spmv_fp32_values(golden, ucfd):
+    from ucfd_sparse_gb300.krylov import SpMat
+    meta, arr = golden
+    s = cases.bsr_case(**cases.KRYLOV["kry6"])
+    A = SpMat(s["bn"], s["blk"], s["rowptr"], s["colidx"], s["values"])
+    x = cases.spmv_x(s)
+    y = x.copy()
+    A.mult(1.5, x, -0.5, y, fp32=True)
+    ref = arr["kry6_spmv"]
+    assert np.abs(y - ref).max() <= 2e-6 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("coloured", [False, True])
+def test_precon_apply_bitexact(coloured, port, ucfd):
+    from ucfd_sparse_gb300.krylov import Precon
+    s0 = cases.bsr_case(mesh=5, seed=3)
+    s, ic = colour_renumbered(s0)
+    b = np.random.default_rng(5).standard_normal(s["bn"] * 5)
+    pc = Precon(s["rowptr"], s["colidx"], s["diagslots"], s["values"])
+    if coloured:
+        pc.set_pblusgs(s["bn"], 5, len(ic) - 1, np.array(ic, dtype=np.int32))
+    else:
+        pc.set_blusgs(s["bn"], 5)
+    pc.prepare()
+    x = b.copy()
+    pc.apply(x)
+    ref = port.precon_apply(s, b, icolors=ic if coloured else None)
+    np.testing.assert_array_equal(x, ref)
+    assert pc.levels() <= len(ic) - 1
+
+
+def test_precon_natural_order_unrenumbered(port, ucfd):
+    """Natural-order BLU-SGS on a matrix whose numbering is not colour-major:
+    level scheduling reproduces the sequential sweep exactly."""
+    from ucfd_sparse_gb300.krylov import Precon
+    s = cases.bsr_case(mesh=4, seed=8)
+    b = np.random.default_rng(6).standard_normal(s["bn"] * 5)
+    pc = Precon(s["rowptr"], s["colidx"], s["diagslots"], s["values"])
+    pc.set_blusgs(s["bn"], 5)
+    pc.prepare()
+    assert pc.levels() > 4
+    x = dev(b)
+    pc.apply(x)
+    np.testing.assert_array_equal(x.cpu().numpy(), port.precon_apply(s, b))
+
+
+@pytest.mark.parametrize("name", sorted(cases.KRYLOV))
+def test_gmres_matches_oracle(name, golden, port, ucfd):
+    from ucfd_sparse_gb300.krylov import Precon, Solver, SpMat
+    meta, arr = golden
+    kw = cases.KRYLOV[name]
+    s = cases.bsr_case(**kw)
+    g = meta[f"{name}_gmres"]
+    A = SpMat(s["bn"], 5, s["rowptr"], s["colidx"], s["values"])
+    pc = Precon(s["rowptr"], s["colidx"], s["diagslots"], s["values"])
+    pc.set_blusgs(s["bn"], 5)
+    pc.prepare()
+    sv = Solver(s["bn"] * 5, kw["m"], 20, g["tol"])
+    sv.trace()
+    x = np.zeros(s["bn"] * 5)
+    sv.solve(pc, A, x, s["rhs"])
+    st, it, res = sv.result()
+    assert (st, it) == (g["stat"], g["iters"])
+    ref = arr[f"{name}_gmres_x"]
+    assert np.abs(x - ref).max() <= 1e-10 * np.abs(ref).max()
+    assert res <= g["tol"]
+
+
+@pytest.mark.parametrize("prec", [0, 2])
+def test_gmres_coloured_and_mixed_reach_1e10(prec, port, ucfd):
+    from ucfd_sparse_gb300.krylov import Precon, Solver, SpMat
+    s0 = cases.bsr_case(mesh=8, seed=2)
+    s, ic = colour_renumbered(s0)
+    n = s["bn"] * 5
+    d = {k: dev(s[k]) for k in ("rowptr", "colidx", "values", "diagslots", "rhs")}
+    A = SpMat(s["bn"], 5, d["rowptr"], d["colidx"], d["values"], cuda=True)
+    pc = Precon(d["rowptr"], d["colidx"], d["diagslots"], d["values"])
+    pc.set_pblusgs(s["bn"], 5, len(ic) - 1, np.array(ic, dtype=np.int32), cuda=True)
+    pc.set_precision(prec)
+    pc.prepare()
+    tol = 1e-10 * float(np.linalg.norm(s["rhs"]))
+    sv = Solver(n, 30, 50, tol, cuda=True)
+    sv.set_precision(prec)
+    x = torch.zeros(n, dtype=torch.float64, device="cuda")
+    sv.solve(pc, A, x, d["rhs"])
+    st, it, res = sv.result()
+    assert st == 0 and res <= tol
+    xr, st_o, it_o, res_o, _ = port.gmres(s, s["rhs"], m=30, maxiter=50, tol=tol, pc="pblusgs", icolors=ic)
+    assert st_o == 0
+    assert np.abs(x.cpu().numpy() - xr).max() <= 1e-8 * np.abs(xr).max()

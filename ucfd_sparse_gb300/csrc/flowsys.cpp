@@ -78,6 +78,7 @@ struct _FlowSys {
     cudaGraphExec_t run_exec = nullptr;
     int run_rans = -1;
     double run_kappa = 0;
+    bool run_state = false;  // set by UCFDLUSGS_Run, cleared by Pack
 
     cudaStream_t stream() const { return user ? user : own; }
 };
@@ -535,6 +536,7 @@ ucfd_status_t UCFDLUSGS_Pack(FlowSys s, UCFDInt eidx, UCFDReal turb_factor, UCFD
         UCFD_CUDA(cudaMemcpyAsync(w.base.p, w.diag.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
         UCFD_CUDA(cudaMemcpyAsync(w.rhs0.p, w.du.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
     });
+    s->run_state = false;
     finish(s, !is_device_ptr(e.uptsb));
     UCFD_API_END
 }
@@ -553,7 +555,9 @@ ucfd_status_t UCFDLUSGS_Update(FlowSys s, UCFDInt eidx) {
     dispatch(s, [&]<typename S, bool EX>() {
         Work<S> &w = work<S>(s);
         UCFD_REQUIRE(w.du.p, "Update before Pack");
-        KCALL(EX, fs_lusgs_update<S>, e.neles, s->nvars, s->N, ids, s->d_iperm.p, w.du.p, up, st);
+        // after UCFDLUSGS_Run the device-resident state itself is written back
+        KCALL(EX, fs_lusgs_update<S>, e.neles, s->nvars, s->N, ids, s->d_iperm.p, s->run_state ? w.u.p : w.du.p,
+              up, s->run_state ? 1 : 0, st);
     });
     if (!dev) UCFD_CUDA(cudaMemcpyAsync(e.uptsb, up, nv * sizeof(double), cudaMemcpyDeviceToHost, st));
     finish(s, !dev);
@@ -658,6 +662,7 @@ ucfd_status_t UCFDLUSGS_Run(FlowSys s, UCFDInt niter, UCFDReal kappa, int rans, 
     });
     if (resid && niter > 0)
         UCFD_CUDA(cudaMemcpyAsync(resid, s->resid.p, niter * sizeof(double), cudaMemcpyDefault, st));
+    s->run_state = true;
     finish(s, resid != nullptr);
     UCFD_API_END
 }

@@ -11,7 +11,7 @@ namespace kfast {
     template void fs_lusgs_pack<T>(int, int, int, long long, double, double, const int *, const int *,         \
                                    const double *, const double *, const double *, const double *, T *, T *,   \
                                    T *, cudaStream_t);                                                         \
-    template void fs_lusgs_update<T>(int, int, long long, const int *, const int *, const T *, double *,       \
+    template void fs_lusgs_update<T>(int, int, long long, const int *, const int *, const T *, double *, int,  \
                                      cudaStream_t);                                                            \
     template void fs_lusgs_prepare<T>(long long, int, int, int, T, const int *, const T *, const T *,          \
                                       const T *, const T *, T *, cudaStream_t);                                \

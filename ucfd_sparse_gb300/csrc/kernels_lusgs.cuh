@@ -169,14 +169,19 @@ __global__ void fs_lusgs_pack_kernel(int neles, int nvars, int nfvars, long long
     }
 }
 
-// rank_lusgs_update: lusgs.c:54-70 (uptsb += du over all nvars).
+// rank_lusgs_update: lusgs.c:54-70 (uptsb += du over all nvars).  With
+// assign != 0 the element state is overwritten by src instead (writing the
+// device-resident state of a pseudo-time loop back).
 template <typename T>
 __global__ void fs_lusgs_update_kernel(int neles, int nvars, long long N, const int *cell_ids,
-                                       const int *iperm, const T *du, double *upts) {
+                                       const int *iperm, const T *src, double *upts, int assign) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= neles) return;
     const long long k = iperm[cell_ids[idx]];
-    for (int v = 0; v < nvars; ++v) upts[idx + (long long)v * neles] += (double)du[k + v * N];
+    for (int v = 0; v < nvars; ++v) {
+        if (assign) upts[idx + (long long)v * neles] = (double)src[k + v * N];
+        else upts[idx + (long long)v * neles] += (double)src[k + v * N];
+    }
 }
 
 // pre_lusgs: lusgs.c:87-113.  lam is the per cell-face copy of lambdaf.

@@ -30,7 +30,7 @@
                        T *diag, cudaStream_t s);                                                   \
     template <typename T>                                                                          \
     void fs_lusgs_update(int neles, int nvars, long long N, const int *cell_ids, const int *iperm, \
-                         const T *du, double *upts, cudaStream_t s);                               \
+                         const T *du, double *upts, int assign, cudaStream_t s);                   \
     template <typename T>                                                                          \
     void fs_lusgs_prepare(long long N, int maxdeg, int nv0, int nv1, T kappa, const int *nei,      \
                           const T *fa, const T *rv, const T *lam, const T *base, T *diag,          \

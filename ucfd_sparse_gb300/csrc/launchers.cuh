@@ -68,9 +68,9 @@ void fs_lusgs_pack(int neles, int nvars, int nfvars, long long N, double turb_fa
 
 template <typename T>
 void fs_lusgs_update(int neles, int nvars, long long N, const int *cell_ids, const int *iperm,
-                     const T *du, double *upts, cudaStream_t s) {
+                     const T *du, double *upts, int assign, cudaStream_t s) {
     if (neles <= 0) return;
-    fs_lusgs_update_kernel<T><<<grid_for(neles), kBlock, 0, s>>>(neles, nvars, N, cell_ids, iperm, du, upts);
+    fs_lusgs_update_kernel<T><<<grid_for(neles), kBlock, 0, s>>>(neles, nvars, N, cell_ids, iperm, du, upts, assign);
 }
 
 template <typename T>

@@ -1,0 +1,124 @@
+"""Python mirror of the Krylov API (``ucfdmat.h``, ``ucfdprecon.h``,
+``ucfdsolver.h``): BSR matrices, BLU-SGS preconditioners and GMRES(m)."""
+from __future__ import annotations
+
+from ctypes import byref, c_double, c_int, c_void_p
+
+import numpy as np
+
+from .lib import PREC_FP32, PREC_FP64, PREC_FP64_FMA, call, load, ptr
+
+__all__ = ["SpMat", "Precon", "Solver"]
+
+
+class SpMat:
+    def __init__(self, bn, blk, rowptr, colidx, values, cuda=False):
+        load()
+        self._h = c_void_p()
+        self._keep = [rowptr, colidx, values]
+        self.bn, self.blk = bn, blk
+        call("UCFDMatCreateCUDABSR" if cuda else "UCFDMatCreateBSR", byref(self._h), bn, blk, ptr(rowptr),
+             ptr(colidx), ptr(values))
+
+    def mult(self, alpha, x, beta, y, fp32=False):
+        call("UCFDMatMultFP32" if fp32 else "UCFDMatMult", alpha, self._h, ptr(x), beta, ptr(y))
+
+    def update_values(self):
+        call("UCFDMatUpdateValues", self._h)
+
+    def destroy(self):
+        if self._h:
+            call("UCFDMatDestroy", byref(self._h))
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class Precon:
+    def __init__(self, rowptr=None, colidx=None, diagslots=None, values=None, none=False):
+        load()
+        self._h = c_void_p()
+        self._keep = [rowptr, colidx, diagslots, values]
+        if none:
+            call("UCFDPreconCreateNone", byref(self._h))
+        else:
+            call("UCFDPreconCreatefromArrays", byref(self._h), ptr(rowptr), ptr(colidx), ptr(diagslots),
+                 ptr(values))
+
+    def set_blusgs(self, bn, block):
+        call("UCFDPreconSetBLUSGS", byref(self._h), bn, block)
+
+    def set_pblusgs(self, bn, block, ncolors, icolors, cuda=False):
+        icolors = np.ascontiguousarray(icolors, dtype=np.int32)
+        self._keep.append(icolors)
+        call("UCFDPreconSetCUDABLUSGS" if cuda else "UCFDPreconSetPBLUSGS", byref(self._h), bn, block, ncolors,
+             ptr(icolors))
+
+    def set_precision(self, prec):
+        call("UCFDPreconSetPrecision", self._h, prec)
+
+    def prepare(self):
+        call("UCFDPreconPrepare", self._h)
+
+    def apply(self, b):
+        call("UCFDPreconApply", self._h, ptr(b))
+
+    def levels(self) -> int:
+        n = c_int()
+        call("UCFDPreconGetLevels", self._h, byref(n))
+        return n.value
+
+    def destroy(self):
+        if self._h:
+            call("UCFDPreconDestroy", byref(self._h))
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class Solver:
+    def __init__(self, n, m, maxiter, tol, cuda=False):
+        load()
+        self._h = c_void_p()
+        call("UCFDSolverCreateCUDAGMRES" if cuda else "UCFDSolverCreateGMRES", byref(self._h), n, m, maxiter, tol)
+        self.maxiter = maxiter
+
+    def set_precision(self, prec):
+        call("UCFDSolverSetPrecision", self._h, prec)
+
+    def trace(self):
+        call("UCFDSolverTraceResidualHistory", self._h)
+
+    def solve(self, pc: Precon, A: SpMat, x, b):
+        call("UCFDSolve", self._h, pc._h, A._h, ptr(x), ptr(b))
+
+    def result(self):
+        st, it, res = c_int(), c_int(), c_double()
+        call("UCFDSolverGetResult", self._h, byref(st), byref(it), byref(res))
+        return st.value, it.value, res.value
+
+    def history(self):
+        h = np.zeros(self.maxiter)
+        call("UCFDSolverGetResidualHistory", self._h, ptr(h))
+        return h
+
+    def arnoldi_steps(self) -> int:
+        n = c_int()
+        call("UCFDSolverGetArnoldiSteps", self._h, byref(n))
+        return n.value
+
+    def destroy(self):
+        if self._h:
+            call("UCFDSolverDestroy", byref(self._h))
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass

@@ -311,7 +311,8 @@ def blusgs_case(m: int, nvars: int = 5, jitter: float = 0.2, permute: bool = Tru
     rhs = rng.standard_normal((nvars, N))
     upts = free_stream(nvars, N)
     vol = mesh.vol.copy()
-    fs.update(dict(nvars=nvars, jmat=np.ascontiguousarray(jmat), fspr_face=sigma, neles=N,
+    fs.update(dict(nvars=nvars, nfvars=min(nvars, 5), ndims=3, jmat=np.ascontiguousarray(jmat), fspr_face=sigma,
+                   neles=N,
                    cell_ids=perm.astype(np.int32), dt=dt, rhs=rhs, upts=upts, vol=vol,
                    mesh=mesh))
     return fs
