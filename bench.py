@@ -283,9 +283,9 @@ def run_gpu(args):
     P64 = Problem(case, lc, 1, stream, device)
     nlev = P32.nlev
 
-    def timed(P, steps, warm):
+    def timed(P, steps, warm, inner):
         for _ in range(warm):
-            P.step(args.rtol, args.max_pairs, args.inner)
+            P.step(args.rtol, args.max_pairs, inner)
         torch.cuda.synchronize()
         barrier(dist, device)
         torch.cuda.synchronize()
@@ -293,7 +293,7 @@ def run_gpu(args):
         pairs_all, rels = [], []
         ev0.record(stream)
         for _ in range(steps):
-            p, r = P.step(args.rtol, args.max_pairs, args.inner)
+            p, r = P.step(args.rtol, args.max_pairs, inner)
             pairs_all.append(p)
             rels.append(r)
         ev1.record(stream)
@@ -303,9 +303,9 @@ def run_gpu(args):
         return reduce_max(ms, dist, device), pairs_all, rels
 
     with ClockSampler(local) as clk:
-        ms32, pairs32, rel32 = timed(P32, args.steps, args.warmup)
+        ms32, pairs32, rel32 = timed(P32, args.steps, args.warmup, args.inner)
     clocks = clk.summary()
-    ms64, pairs64, rel64 = timed(P64, max(2, args.steps // 2), max(args.warmup, 3))
+    ms64, pairs64, rel64 = timed(P64, max(2, args.steps // 2), max(args.warmup, 3), args.check)
     pairs_mean = statistics.mean(pairs32)
     value_rank = N * pairs_mean / (ms32 * 1e-3)
     value = reduce_sum(value_rank, dist, device) if dist else value_rank
@@ -368,7 +368,7 @@ def run_gpu(args):
             "config": {"workload": f"BLU-SGS 5x5 face Jacobians, {args.mesh}^3 jittered (+-0.2h) randomly permuted "
                                    f"hex ({N} cells), greedy colouring ({len(rg)} colours), solve to rtol "
                                    f"{args.rtol:g} per pseudo-time step", "cells": N, "colors": len(rg),
-                       "inner_sweeps": args.inner, "l2": "inputs larger than L2 (no flush needed)",
+                       "inner_sweeps": args.inner, "fp64_check_every": args.check, "l2": "inputs larger than L2 (no flush needed)",
                        "parallelism": f"replicas x{ws}"},
             "pairs_per_step": pairs_mean, "relres": max(rel32),
             "fp64": {"ms_per_step": ms64, "pairs_per_step": statistics.mean(pairs64), "relres": max(rel64),
@@ -395,7 +395,8 @@ def main(argv=None):
     ap.add_argument("--mesh", type=int, default=128)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--rtol", type=float, default=1e-10)
-    ap.add_argument("--inner", type=int, default=8)
+    ap.add_argument("--inner", type=int, default=20, help="FP32 sweep pairs per FP64 refinement step")
+    ap.add_argument("--check", type=int, default=4, help="FP64 solve: pairs between residual checks")
     ap.add_argument("--max-pairs", type=int, default=400)
     ap.add_argument("--ref-pairs", type=int, default=1)
     args = ap.parse_args(argv)

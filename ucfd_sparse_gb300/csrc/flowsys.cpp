@@ -69,7 +69,7 @@ struct _FlowSys {
 
     Work<double> w64;
     Work<float> w32;
-    DevBuf<double> D, LU64, tD, tLU64, J64, rhs64, x64;  // FP64 block arrays
+    DevBuf<double> D, dd, LU64, tD, tLU64, J64, rhs64, x64;  // FP64 block arrays
     bool du64_valid = false;
     DevBuf<double> part, red, resid;
     PinnedBuf<double> h_red;
@@ -116,6 +116,9 @@ void build_topology(FlowSys s) {
 
     s->sch = s->colored ? schedule_colored(n, rp.data(), ci.data(), s->color.data())
                         : schedule_natural(n, rp.data(), ci.data());
+    // spatial locality inside each level (the cells of a level are
+    // independent, so the order does not change any result)
+    sort_levels_by(s->sch, bfs_rank(n, rp.data(), ci.data()));
     const Schedule &sch = s->sch;
     int P = 0;
     for (int i = 0; i < n; ++i) P = std::max(P, rp[i + 1] - rp[i]);
@@ -274,6 +277,7 @@ void blusgs_alloc(FlowSys s) {
     w.dup.ensure(nv * N);
     const long long b2 = (long long)s->nfvars * s->nfvars;
     s->D.ensure(b2 * N);
+    s->dd.ensure(N);
     s->LU64.ensure(b2 * N);
     w.J.ensure((long long)s->P * b2 * N);
     if (std::is_same<S, float>::value) {
@@ -695,7 +699,7 @@ ucfd_status_t UCFDBLUSGS_Pack(FlowSys s, UCFDInt eidx, UCFDReal a0) {
         blusgs_alloc<S>(s);
         double *r64 = std::is_same<S, float>::value ? s->rhs64.p : nullptr;
         KCALL(EX, fs_blusgs_pack<S>, e.neles, s->nvars, s->nfvars, s->N, a0, ids, s->d_iperm.p, rh, dt,
-              blu_rhs<S>(s), r64, s->D.p, st);
+              blu_rhs<S>(s), r64, s->dd.p, st);
     });
     finish(s, !is_device_ptr(e.rhs));
     UCFD_API_END
@@ -745,15 +749,18 @@ static ucfd_status_t blusgs_prepare_api(FlowSys s, bool turb) {
         Work<S> &w = work<S>(s);
         UCFD_REQUIRE(w.rhs.p, "Prepare before Pack");
         double *D = turb ? s->tD.p : s->D.p;
+        const double *dd = turb ? nullptr : s->dd.p;
         double *LU64 = turb ? s->tLU64.p : s->LU64.p;
         S *LU_s = nullptr;
         double *J64 = nullptr;
         if constexpr (std::is_same<S, float>::value) {
+            // FP32 sweeps read the rounded factors only
             LU_s = turb ? w.tLU.p : w.LU.p;
+            LU64 = nullptr;
             if (!turb) J64 = s->J64.ensure((size_t)s->P * B * B * s->N);
         }
         KCALL(EX, fs_blusgs_prepare<S>, B, s->N, s->P, (long long)s->nfaces, s->d_nei.p, s->d_slot.p, s->d_side.p,
-              s->fa64.p, s->rv64.p, jd, D, LU64, LU_s, turb ? w.tJ.p : w.J.p, J64, st);
+              s->fa64.p, s->rv64.p, jd, dd, D, LU64, LU_s, turb ? w.tJ.p : w.J.p, J64, st);
     });
     finish(s, !is_device_ptr(jm));
     UCFD_API_END

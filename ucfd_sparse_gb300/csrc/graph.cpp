@@ -98,6 +98,54 @@ Schedule schedule_colored(int n, const int *rowptr, const int *colidx, const int
     return from_levels(n, lev, (int)vals.size());
 }
 
+static int bfs_from(int start, const std::vector<int> &srp, const std::vector<int> &sci, std::vector<int> &dist,
+                    std::vector<int> &order) {
+    // returns the last cell reached (a far cell); appends the visit order
+    size_t head = order.size();
+    order.push_back(start);
+    dist[start] = 0;
+    int last = start;
+    while (head < order.size()) {
+        const int i = order[head++];
+        last = i;
+        for (int p = srp[i]; p < srp[i + 1]; ++p) {
+            const int j = sci[p];
+            if (dist[j] < 0) {
+                dist[j] = dist[i] + 1;
+                order.push_back(j);
+            }
+        }
+    }
+    return last;
+}
+
+std::vector<int> bfs_rank(int n, const int *rowptr, const int *colidx) {
+    std::vector<int> srp, sci;
+    symmetrize(n, rowptr, colidx, srp, sci);
+    std::vector<int> dist(n, -1), order;
+    order.reserve(n);
+    std::vector<int> scratch_dist(n, -1), scratch;
+    for (int s = 0; s < n; ++s) {
+        if (dist[s] >= 0) continue;
+        // pseudo-peripheral start: the cell farthest from s in its component
+        scratch.clear();
+        const int far = bfs_from(s, srp, sci, scratch_dist, scratch);
+        for (int v : scratch) scratch_dist[v] = -1;
+        bfs_from(far, srp, sci, dist, order);
+    }
+    std::vector<int> rank(n);
+    for (int k = 0; k < n; ++k) rank[order[k]] = k;
+    return rank;
+}
+
+void sort_levels_by(Schedule &s, const std::vector<int> &key) {
+    for (int l = 0; l < s.nlev; ++l) {
+        auto b = s.perm.begin() + s.lev_off[l], e = s.perm.begin() + s.lev_off[l + 1];
+        std::sort(b, e, [&](int a, int c) { return key[a] < key[c]; });
+    }
+    for (int k = 0; k < (int)s.perm.size(); ++k) s.iperm[s.perm[k]] = k;
+}
+
 std::vector<int> greedy_color_csr(int n, const int *rowptr, const int *colidx, int *ncolors) {
     std::vector<int> srp, sci;
     symmetrize(n, rowptr, colidx, srp, sci);

@@ -30,6 +30,17 @@ Schedule schedule_colored(int n, const int *rowptr, const int *colidx, const int
 // symmetrised graph); returns 0-based colours and the colour count.
 std::vector<int> greedy_color_csr(int n, const int *rowptr, const int *colidx, int *ncolors);
 
+// Breadth-first order of the symmetrised graph started from a
+// pseudo-peripheral cell (each connected component in turn): rank[i] is
+// the position of cell i.  Graph neighbours get nearby ranks, so sorting
+// the cells of each level by it makes neighbour gathers of consecutive
+// threads hit nearby memory.
+std::vector<int> bfs_rank(int n, const int *rowptr, const int *colidx);
+
+// Reorder the cells inside every level by key (does not change results:
+// the cells of a level are independent).
+void sort_levels_by(Schedule &s, const std::vector<int> &key);
+
 // Symmetrised adjacency (CSR, no self entries, no duplicates).
 void symmetrize(int n, const int *rowptr, const int *colidx, std::vector<int> &srp,
                 std::vector<int> &sci);

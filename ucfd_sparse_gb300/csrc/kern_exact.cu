@@ -17,8 +17,8 @@ template void gather_idx<double>(long long, const int *, const double *, double 
 template void fs_blusgs_pack<double>(int, int, int, long long, double, const int *, const int *, const double *,
                                      const double *, double *, double *, double *, cudaStream_t);
 template void fs_blusgs_prepare<double>(int, long long, int, long long, const int *, const int *, const int8_t *,
-                                        const double *, const double *, const double *, double *, double *, double *,
-                                        double *, double *, cudaStream_t);
+                                        const double *, const double *, const double *, const double *, double *,
+                                        double *, double *, double *, double *, cudaStream_t);
 template void fs_blusgs_sweep<double>(int, int, int, long long, int, int, const int *, const double *, const double *,
                                       const double *, const double *, const double *, double *, int, cudaStream_t);
 template void fs_blusgs_residual<double, double>(int, long long, int, int, int, const int *, const double *,

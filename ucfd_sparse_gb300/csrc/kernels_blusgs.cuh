@@ -65,12 +65,13 @@ __device__ __forceinline__ void lusub_dev(const T *LU, T *b) {
     }
 }
 
-// rank_blusgs_pack: blusgs.c:17-45.  rhs goes to the internal SoA arrays,
-// the NS diagonal block starts as (1/dt + a0) I.
+// rank_blusgs_pack: blusgs.c:17-45.  rhs goes to the internal SoA arrays;
+// the NS diagonal block starts as (1/dt + a0) I, of which only the scalar
+// dd = 1/dt + a0 is stored (the prepare kernel expands it).
 template <typename S>
 __global__ void fs_blusgs_pack_kernel(int neles, int nvars, int B, long long N, double a0,
                                       const int *cell_ids, const int *iperm, const double *rhs,
-                                      const double *dt, S *rhs_s, double *rhs64, double *D) {
+                                      const double *dt, S *rhs_s, double *rhs64, double *dd) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= neles) return;
     const long long k = iperm[cell_ids[idx]];
@@ -79,9 +80,7 @@ __global__ void fs_blusgs_pack_kernel(int neles, int nvars, int B, long long N, 
         rhs_s[k + v * N] = (S)x;
         if (rhs64) rhs64[k + v * N] = x;
     }
-    const double d = 1 / dt[idx] + a0;
-    for (int r = 0; r < B; ++r)
-        for (int c = 0; c < B; ++c) D[(r * B + c) * N + k] = (r == c) ? d : 0.0;
+    dd[k] = 1 / dt[idx] + a0;
 }
 
 // rank_tblusgs_pack + kwsst/sa source Jacobians: blusgs.c:60-120,
@@ -110,17 +109,24 @@ __global__ void fs_tblusgs_pack_kernel(int model, int neles, int nvars, int nt, 
 
 // pre_blusgs: blusgs.c:200-246, plus the gather of each cell-face's
 // off-diagonal block (the half the sweeps use) into the ELL layout.
+// The block starts from dd[k] I when dd is given (NS pack), else from D.
 template <typename S, int B>
 __global__ void fs_blusgs_prepare_kernel(long long N, int P, long long nF, const int *nei,
                                          const int *slot, const int8_t *side, const double *fa,
-                                         const double *rv, const double *jmat, double *D,
-                                         double *LU64, S *LU_s, S *J_s, double *J64) {
+                                         const double *rv, const double *jmat, const double *dd,
+                                         double *D, double *LU64, S *LU_s, S *J_s, double *J64) {
     const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (k >= N) return;
     constexpr int B2 = B * B;
     double dm[B2];
+    if (dd) {
+        const double d = dd[k];
 #pragma unroll
-    for (int e = 0; e < B2; ++e) dm[e] = D[e * N + k];
+        for (int e = 0; e < B2; ++e) dm[e] = (e % (B + 1) == 0) ? d : 0.0;
+    } else {
+#pragma unroll
+        for (int e = 0; e < B2; ++e) dm[e] = D[e * N + k];
+    }
     for (int p = 0; p < P; ++p) {
         if (nei[p * N + k] < 0) break;
         const long long s = slot[p * N + k];
@@ -145,7 +151,7 @@ __global__ void fs_blusgs_prepare_kernel(long long N, int P, long long nF, const
     ludcmp_dev<double, B>(dm);
 #pragma unroll
     for (int e = 0; e < B2; ++e) {
-        LU64[e * N + k] = dm[e];
+        if (LU64) LU64[e * N + k] = dm[e];
         if (LU_s) LU_s[e * N + k] = (S)dm[e];
     }
 }

@@ -87,19 +87,23 @@ void gather_idx(long long n, const int *idx, const double *src, Td *dst, cudaStr
     gather_idx_kernel<Td><<<grid_for(n < (1ll << 24) ? n : (1ll << 24)), kBlock, 0, s>>>(n, idx, src, dst);
 }
 
-__global__ void pair_reduce_kernel(int nblocks, const double *part, double *out) {
+__global__ void __launch_bounds__(1024) pair_reduce_kernel(int nblocks, const double *part, double *out) {
     double a = 0.0, b = 0.0;
-    for (int i = 0; i < nblocks; ++i) {
+    for (int i = threadIdx.x; i < nblocks; i += blockDim.x) {
         a += part[2 * i];
         b += part[2 * i + 1];
     }
-    out[0] = a;
-    out[1] = b;
+    a = block_sum(a);
+    b = block_sum(b);
+    if (threadIdx.x == 0) {
+        out[0] = a;
+        out[1] = b;
+    }
 }
 
 // out[0], out[1] = sums of the (r^2, rhs^2) pairs written by the residual kernel.
 void pair_reduce(int nblocks, const double *part, double *out, cudaStream_t s) {
-    pair_reduce_kernel<<<1, 1, 0, s>>>(nblocks, part, out);
+    pair_reduce_kernel<<<1, 1024, 0, s>>>(nblocks, part, out);
 }
 
 // ---- block LU-SGS ----------------------------------------------------------
@@ -132,10 +136,11 @@ void fs_tblusgs_pack(int model, int neles, int nvars, int nt, long long N, doubl
 template <typename S>
 void fs_blusgs_prepare(int B, long long N, int P, long long nF, const int *nei, const int *slot,
                        const int8_t *side, const double *fa, const double *rv, const double *jmat,
-                       double *D, double *LU64, S *LU_s, S *J_s, double *J64, cudaStream_t s) {
+                       const double *dd, double *D, double *LU64, S *LU_s, S *J_s, double *J64,
+                       cudaStream_t s) {
     if (N <= 0) return;
     UCFD_BSW(B, (fs_blusgs_prepare_kernel<S, BB><<<grid_for(N, 128), 128, 0, s>>>(
-                    N, P, nF, nei, slot, side, fa, rv, jmat, D, LU64, LU_s, J_s, J64)));
+                    N, P, nF, nei, slot, side, fa, rv, jmat, dd, D, LU64, LU_s, J_s, J64)));
 }
 
 template <typename S>
@@ -274,10 +279,11 @@ __global__ void axpy_norm_kernel(long long n, const S *x, S *y, double *part) {
     if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
-__global__ void sqrt_sum_kernel(int nb, const double *part, double *out) {
+__global__ void __launch_bounds__(1024) sqrt_sum_kernel(int nb, const double *part, double *out) {
     double t = 0.0;
-    for (int b = 0; b < nb; ++b) t += part[b];
-    *out = sqrt(t);
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) t += part[b];
+    t = block_sum(t);
+    if (threadIdx.x == 0) *out = sqrt(t);
 }
 
 // ---- GMRES pieces ----------------------------------------------------------
@@ -335,7 +341,7 @@ template <typename S>
 void axpy_norm(long long n, const S *x, S *y, double *part, double *out, cudaStream_t s) {
     const int nb = gm_blocks(n);
     axpy_norm_kernel<S><<<nb, kBlock, 0, s>>>(n, x, y, part);
-    sqrt_sum_kernel<<<1, 1, 0, s>>>(nb, part, out);
+    sqrt_sum_kernel<<<1, 1024, 0, s>>>(nb, part, out);
 }
 
 __global__ void norm_finalize_kernel(int nblocks, const double *part, double *out) {
