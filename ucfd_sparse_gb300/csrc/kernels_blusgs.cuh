@@ -159,7 +159,14 @@ __global__ void fs_blusgs_prepare_kernel(long long N, int P, long long nF, const
 // lower_sweep / upper_sweep of blusgs.c:273-373 for one level: every
 // neighbour contributes with its current value (lower levels already
 // updated, higher levels not yet), then the cell solves with its LU.
-template <typename S, int B>
+//
+// PW > 0: the ELL width is the compile-time constant PW and the face loop
+// is fully unrolled: every neighbour index, then every neighbour increment
+// and block value, is requested before the first product, so one thread
+// keeps all of its memory traffic in flight (the reference's per-face
+// order of the products and subtractions is kept; padding entries only
+// skip their contribution).  PW == 0 is the generic runtime-width loop.
+template <typename S, int B, int PW>
 __global__ void __launch_bounds__(256) fs_blusgs_sweep_kernel(int t0, int t1, long long N, int P,
                                                               int var0, const int *nei, const S *fa,
                                                               const S *rv, const S *J, const S *LU,
@@ -171,20 +178,53 @@ __global__ void __launch_bounds__(256) fs_blusgs_sweep_kernel(int t0, int t1, lo
 #pragma unroll
     for (int r = 0; r < B; ++r) b[r] = rhs[(var0 + r) * N + k];
     const S rvk = rv[k];
-    for (int p = 0; p < P; ++p) {
-        const int nb = __ldg(nei + p * N + k);
-        if (nb < 0) break;
-        const S fv = __ldg(fa + p * N + k) * rvk;
-        S x[B];
+    if constexpr (PW > 0) {
+        int nb[PW];
+        S fv[PW];
 #pragma unroll
-        for (int c = 0; c < B; ++c) x[c] = du[(var0 + c) * N + nb];
-        const S *Jp = J + (long long)p * B2 * N + k;
+        for (int p = 0; p < PW; ++p) {
+            nb[p] = __ldg(nei + p * N + k);
+            fv[p] = __ldg(fa + p * N + k) * rvk;
+        }
+        S x[PW][B];
 #pragma unroll
-        for (int r = 0; r < B; ++r) {
-            S val = S(0);
+        for (int p = 0; p < PW; ++p) {
+            const int g = nb[p] >= 0 ? nb[p] : k;  // padding: any valid address
 #pragma unroll
-            for (int c = 0; c < B; ++c) val += __ldg(Jp + (r * B + c) * N) * x[c];
-            b[r] -= val * fv;
+            for (int c = 0; c < B; ++c) x[p][c] = du[(var0 + c) * N + g];
+        }
+#pragma unroll
+        for (int p = 0; p < PW; ++p) {
+            const S *Jp = J + (long long)p * B2 * N + k;
+            S jv[B2];
+#pragma unroll
+            for (int e = 0; e < B2; ++e) jv[e] = __ldg(Jp + e * N);
+            if (nb[p] >= 0) {
+#pragma unroll
+                for (int r = 0; r < B; ++r) {
+                    S val = S(0);
+#pragma unroll
+                    for (int c = 0; c < B; ++c) val += jv[r * B + c] * x[p][c];
+                    b[r] -= val * fv[p];
+                }
+            }
+        }
+    } else {
+        for (int p = 0; p < P; ++p) {
+            const int nb = __ldg(nei + p * N + k);
+            if (nb < 0) break;
+            const S fv = __ldg(fa + p * N + k) * rvk;
+            S x[B];
+#pragma unroll
+            for (int c = 0; c < B; ++c) x[c] = du[(var0 + c) * N + nb];
+            const S *Jp = J + (long long)p * B2 * N + k;
+#pragma unroll
+            for (int r = 0; r < B; ++r) {
+                S val = S(0);
+#pragma unroll
+                for (int c = 0; c < B; ++c) val += __ldg(Jp + (r * B + c) * N) * x[c];
+                b[r] -= val * fv;
+            }
         }
     }
     S lu[B2];
@@ -219,19 +259,35 @@ __global__ void fs_blusgs_residual_kernel(long long N, int P, int var0, int nvar
             for (int c = 0; c < B; ++c) v -= D[(r * B + c) * N + k] * xk[c];
             res[r] = v;
         }
-        for (int p = 0; p < P; ++p) {
-            const int nb = nei[p * N + k];
-            if (nb < 0) break;
-            const double fv = fa[p * N + k] * rv[k];
-            double xn[B];
+        // fixed trip count (6 = hex ELL width) so all gathers are issued
+        // up front; padding entries contribute nothing
+        constexpr int PU = 6;
+        for (int p0 = 0; p0 < P; p0 += PU) {
+            int nbv[PU];
+            double xn[PU][B];
 #pragma unroll
-            for (int c = 0; c < B; ++c) xn[c] = (double)x[(var0 + c) * N + nb];
+            for (int q = 0; q < PU; ++q) {
+                const int p = p0 + q;
+                nbv[q] = p < P ? nei[p * N + k] : -1;
+            }
 #pragma unroll
-            for (int r = 0; r < B; ++r) {
-                double val = 0.0;
+            for (int q = 0; q < PU; ++q) {
+                const int g = nbv[q] >= 0 ? nbv[q] : (int)k;
 #pragma unroll
-                for (int c = 0; c < B; ++c) val += J64[((long long)p * B2 + r * B + c) * N + k] * xn[c];
-                res[r] -= val * fv;
+                for (int c = 0; c < B; ++c) xn[q][c] = (double)x[(var0 + c) * N + g];
+            }
+#pragma unroll
+            for (int q = 0; q < PU; ++q) {
+                if (nbv[q] < 0) continue;
+                const int p = p0 + q;
+                const double fv = fa[p * N + k] * rv[k];
+#pragma unroll
+                for (int r = 0; r < B; ++r) {
+                    double val = 0.0;
+#pragma unroll
+                    for (int c = 0; c < B; ++c) val += J64[((long long)p * B2 + r * B + c) * N + k] * xn[q][c];
+                    res[r] -= val * fv;
+                }
             }
         }
 #pragma unroll

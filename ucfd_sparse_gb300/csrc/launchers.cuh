@@ -149,8 +149,17 @@ void fs_blusgs_sweep(int B, int t0, int t1, long long N, int P, int var0, const 
                      cudaStream_t s) {
     if (t1 <= t0) return;
     if (block <= 0) block = kBlock;
-    UCFD_BSW(B, (fs_blusgs_sweep_kernel<S, BB><<<grid_for(t1 - t0, block), block, 0, s>>>(
-                    t0, t1, N, P, var0, nei, fa, rv, J, LU, rhs, du)));
+    const unsigned g = grid_for(t1 - t0, block);
+    if (P == 6) {
+        UCFD_BSW(B, (fs_blusgs_sweep_kernel<S, BB, 6><<<g, block, 0, s>>>(t0, t1, N, P, var0, nei, fa, rv, J, LU,
+                                                                          rhs, du)));
+    } else if (P == 4) {
+        UCFD_BSW(B, (fs_blusgs_sweep_kernel<S, BB, 4><<<g, block, 0, s>>>(t0, t1, N, P, var0, nei, fa, rv, J, LU,
+                                                                          rhs, du)));
+    } else {
+        UCFD_BSW(B, (fs_blusgs_sweep_kernel<S, BB, 0><<<g, block, 0, s>>>(t0, t1, N, P, var0, nei, fa, rv, J, LU,
+                                                                          rhs, du)));
+    }
 }
 
 template <typename Sx, typename R>
