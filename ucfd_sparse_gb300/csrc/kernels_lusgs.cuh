@@ -70,50 +70,71 @@ __global__ void __launch_bounds__(256) scalar_sweep_kernel(ScalarSweepArgs<T> a)
     T df[DNV];
 #pragma unroll
     for (int k = 0; k < DNV; ++k) df[k] = T(0);
+    const T rvi = a.rv ? __ldg(a.rv + i) : T(1);
 
-    for (int f = 0; f < a.nface; ++f) {
-        const int nb = __ldg(a.nei + f * ld + i);
-        bool act;
-        if (a.lcolor) {
-            const int cn = __ldg(a.lcolor + nb);
-            act = a.upper ? (cn > ci) : (cn < ci);
-        } else {
-            act = nb >= 0 && (a.upper ? (nb >= a.hi) : (nb < a.lo));
+    // Faces are handled FB at a time: the neighbour indices, then the
+    // colour tests, then every gather of the batch are issued before any
+    // flux is evaluated (latency hiding); the accumulation into df keeps
+    // the reference's face order.
+    constexpr int FB = sizeof(T) == 4 ? 6 : 3;
+    for (int f0 = 0; f0 < a.nface; f0 += FB) {
+        int nb[FB];
+        bool act[FB];
+#pragma unroll
+        for (int q = 0; q < FB; ++q) nb[q] = (f0 + q < a.nface) ? __ldg(a.nei + (f0 + q) * ld + i) : -1;
+#pragma unroll
+        for (int q = 0; q < FB; ++q) {
+            if (a.lcolor) {
+                const int cn = nb[q] >= 0 ? __ldg(a.lcolor + nb[q]) : ci;
+                act[q] = a.upper ? (cn > ci) : (cn < ci);
+            } else {
+                act[q] = nb[q] >= 0 && (a.upper ? (nb[q] >= a.hi) : (nb[q] < a.lo));
+            }
         }
-        if (!act) continue;
-
-        T u[NV], du[NV], dn[DNV], nf[NDIMS], f0[DNV], f1[DNV];
+        T uu[FB][NV], dn[FB][DNV], nf[FB][NDIMS], fv[FB], kl[FB];
 #pragma unroll
-        for (int v = 0; v < NV; ++v) {
-            // only the variables the flux reads are loaded
-            const bool need = RANS ? (v <= NDIMS || v >= NFV) : (v < NFV);
-            u[v] = need ? __ldg(a.u + v * ld + nb) : T(0);
-            du[v] = T(0);
+        for (int q = 0; q < FB; ++q) {
+            const int g = act[q] ? nb[q] : i;
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+                // only the variables the flux reads are loaded
+                const bool need = RANS ? (v <= NDIMS || v >= NFV) : (v < NFV);
+                uu[q][v] = need ? __ldg(a.u + v * ld + g) : T(0);
+            }
+#pragma unroll
+            for (int k = 0; k < DNV; ++k) dn[q][k] = a.nbsrc[(k + NV0) * ld + g];
+            const int f = act[q] ? f0 + q : 0;
+#pragma unroll
+            for (int d = 0; d < NDIMS; ++d) nf[q][d] = __ldg(a.nrm + (f * NDIMS + d) * ld + i);
+            fv[q] = __ldg(a.fa + f * ld + i);
+            kl[q] = __ldg(a.lam + f * ld + i);
         }
 #pragma unroll
-        for (int k = 0; k < DNV; ++k) {
-            dn[k] = a.nbsrc[(k + NV0) * ld + nb];
-            du[k + NV0] = dn[k];
-        }
+        for (int q = 0; q < FB; ++q) {
+            if (!act[q]) continue;
+            T *u = uu[q];
+            T du[NV], f0v[DNV], f1v[DNV];
 #pragma unroll
-        for (int d = 0; d < NDIMS; ++d) nf[d] = __ldg(a.nrm + (f * NDIMS + d) * ld + i);
-        T fv = __ldg(a.fa + f * ld + i);
-        if (a.rv) fv = fv * __ldg(a.rv + i);
-        // diff_flux: lusgs.c:143-155 (du += u before either flux)
+            for (int v = 0; v < NV; ++v) du[v] = T(0);
 #pragma unroll
-        for (int v = 0; v < NV; ++v) du[v] += u[v];
-        if constexpr (RANS) {
-            rans_flux<T, NFV, NDIMS, NV - NFV>(u, nf, f0);
-            rans_flux<T, NFV, NDIMS, NV - NFV>(du, nf, f1);
-        } else {
-            ns_flux<T, NFV, NDIMS>(a.gamma, a.pmin, u, nf, f0);
-            ns_flux<T, NFV, NDIMS>(a.gamma, a.pmin, du, nf, f1);
-        }
-        const T kl = a.kappa * __ldg(a.lam + f * ld + i);
+            for (int k = 0; k < DNV; ++k) du[k + NV0] = dn[q][k];
+            const T fvq = a.rv ? fv[q] * rvi : fv[q];
+            // diff_flux: lusgs.c:143-155 (du += u before either flux)
 #pragma unroll
-        for (int k = 0; k < DNV; ++k) {
-            const T dfj = f1[k] - f0[k];
-            df[k] += (dfj - kl * dn[k]) * fv;
+            for (int v = 0; v < NV; ++v) du[v] += u[v];
+            if constexpr (RANS) {
+                rans_flux<T, NFV, NDIMS, NV - NFV>(u, nf[q], f0v);
+                rans_flux<T, NFV, NDIMS, NV - NFV>(du, nf[q], f1v);
+            } else {
+                ns_flux<T, NFV, NDIMS>(a.gamma, a.pmin, u, nf[q], f0v);
+                ns_flux<T, NFV, NDIMS>(a.gamma, a.pmin, du, nf[q], f1v);
+            }
+            const T klq = a.kappa * kl[q];
+#pragma unroll
+            for (int k = 0; k < DNV; ++k) {
+                const T dfj = f1v[k] - f0v[k];
+                df[k] += (dfj - klq * dn[q][k]) * fvq;
+            }
         }
     }
 #pragma unroll
