@@ -35,6 +35,7 @@ UNITS = [
     ("flowsys.cpp", []),
     ("legacy.cpp", []),
     ("krylov.cpp", []),
+    ("noalloc.cu", []),
 ]
 
 

@@ -937,3 +937,35 @@ ucfd_status_t UCFDBLUSGS_Solve(FlowSys s, UCFDReal rtol, UCFDInt max_sweeps, UCF
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// read-only view for allocation-free entry points (flowsys_view.h)
+// ---------------------------------------------------------------------------
+#include "flowsys_view.h"
+
+bool ucfd::flowsys_block_view(FlowSys s, BlockSystemView &v) {
+    if (!s || s->mode != MODE_BLUSGS || !s->topo || !s->D.p) return false;
+    BlockSystemView t;
+    t.N = s->N;
+    t.P = s->P;
+    t.B = s->nfvars;
+    t.nei = s->d_nei.p;
+    t.fa = s->fa64.p;
+    t.rv = s->rv64.p;
+    t.D = s->D.p;
+    if (s->prec == UCFD_PREC_FP32) {
+        if (!s->J64.p || !s->rhs64.p) return false;
+        t.J64 = s->J64.p;
+        t.rhs64 = s->rhs64.p;
+        if (s->du64_valid) t.x64 = s->x64.p;
+        else t.x32 = s->w32.bdu.p;
+    } else {
+        if (!s->w64.J.p || !s->w64.rhs.p) return false;
+        t.J64 = s->w64.J.p;
+        t.rhs64 = s->w64.rhs.p;
+        t.x64 = s->w64.bdu.p;
+    }
+    t.stream = (void *)s->stream();
+    v = t;
+    return true;
+}

@@ -67,6 +67,7 @@ SIGNATURES = {
     "UCFDLUSGS_Run": (_I, [_P, _I, _D, _I, _I, _P]),
     "UCFDBLUSGS_Solve": (_I, [_P, _D, _I, _I, POINTER(c_int), POINTER(c_double)]),
     "UCFDBLUSGS_Residual": (_I, [_P, POINTER(c_double)]),
+    "UCFDBLUSGS_ResidualNoAlloc": (_I, [_P, _P]),
     # coloredlusgs.h
     "UCFDLegacySetDims": (_I, [_I, _I, _I]),
     "UCFDLegacySetPrecision": (_I, [_I]),
