@@ -28,4 +28,11 @@ struct ScalarSweepArgs {
     int upper;
 };
 
+// One colour of a transposed (adjoint) colored LU-SGS sweep.
+struct AdjArgs {
+    int t0, t1;          // icolor slots of the colour
+    int neles, nface;
+    const int *icolor, *lcolor, *nei, *rface;
+};
+
 }  // namespace ucfd

@@ -41,6 +41,16 @@ namespace kfast {
 UCFD_INST_T(double)
 UCFD_INST_T(float)
 #undef UCFD_INST_T
+#define UCFD_INST_ADJ(T)                                                                                       \
+    template void adj_upper<T>(const ::ucfd::AdjArgs &, int, int, T, T, const T *, const T *, const T *,      \
+                               const T *, const T *, const T *, const T *, const T *, T *, T *, T *,          \
+                               cudaStream_t);                                                                 \
+    template void adj_lower<T>(const ::ucfd::AdjArgs &, int, int, T, T, T, const T *, const T *, const T *,    \
+                               const T *, const T *, const T *, const T *, const T *, T *, const T *, T *,    \
+                               T *, T *, cudaStream_t);
+UCFD_INST_ADJ(double)
+UCFD_INST_ADJ(float)
+#undef UCFD_INST_ADJ
 template void fs_blusgs_residual<double, float>(int, long long, int, int, int, const int *, const double *,
                                                 const double *, const double *, const double *, const double *,
                                                 const double *, float *, double *, int, int *, cudaStream_t);

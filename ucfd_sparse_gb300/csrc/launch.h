@@ -91,6 +91,16 @@
     void axpy_into(long long n, const Ts *x, double *y, cudaStream_t s);                           \
     template <typename S>                                                                          \
     void axpy_norm(long long n, const S *x, S *y, double *part, double *out, cudaStream_t s);      \
+    /* ---- adjoint of the colored LU-SGS step ---- */                                            \
+    template <typename T>                                                                          \
+    void adj_upper(const ::ucfd::AdjArgs &a, int nfv, int ndims, T gamma, T pmin, const T *fnv,    \
+                   const T *vec, const T *fspr, const T *upts, const T *diag, const T *dub,        \
+                   const T *dq, const T *gdq, T *qbar, T *dbar, T *gfspr, cudaStream_t s);         \
+    template <typename T>                                                                          \
+    void adj_lower(const ::ucfd::AdjArgs &a, int nfv, int ndims, T gamma, T pmin, T factor,        \
+                   const T *fnv, const T *vec, const T *fspr, const T *dt, const T *upts,          \
+                   const T *diag, const T *dub, const T *qbar, T *wbuf, const T *dbar, T *grhs,    \
+                   T *gdt, T *gfspr, cudaStream_t s);                                              \
     /* ---- GMRES pieces ---- */                                                                   \
     int gm_blocks(long long n);                                                                    \
     void gm_dots(long long n, int K, const double *V, long long ldv, const double *w,              \

@@ -6,9 +6,43 @@
 #include "kernels_lusgs.cuh"
 #include "kernels_blusgs.cuh"
 #include "kernels_krylov.cuh"
+#include "kernels_adjoint.cuh"
 #include "ucfd_internal.h"
 
 namespace UCFD_KNS {
+
+// ---- adjoint of the colored LU-SGS step --------------------------------------
+template <typename T>
+void adj_upper(const ::ucfd::AdjArgs &a, int nfv, int ndims, T gamma, T pmin, const T *fnv, const T *vec,
+               const T *fspr, const T *upts, const T *diag, const T *dub, const T *dq, const T *gdq, T *qbar, T *dbar,
+               T *gfspr, cudaStream_t s) {
+    const int n = a.t1 - a.t0;
+    if (n <= 0) return;
+    if (nfv == 5 && ndims == 3)
+        adj_upper_kernel<T, 5, 5, 3><<<grid_for(n), kBlock, 0, s>>>(a, gamma, pmin, fnv, vec, fspr, upts, diag, dub,
+                                                                     dq, gdq, qbar, dbar, gfspr);
+    else if (nfv == 4 && ndims == 2)
+        adj_upper_kernel<T, 4, 4, 2><<<grid_for(n), kBlock, 0, s>>>(a, gamma, pmin, fnv, vec, fspr, upts, diag, dub,
+                                                                     dq, gdq, qbar, dbar, gfspr);
+    else
+        ::ucfd::fail(UCFD_ERR_UNSUPPORTED, "adjoint built for nfvars/ndims 5/3 and 4/2 only");
+}
+
+template <typename T>
+void adj_lower(const ::ucfd::AdjArgs &a, int nfv, int ndims, T gamma, T pmin, T factor, const T *fnv, const T *vec,
+               const T *fspr, const T *dt, const T *upts, const T *diag, const T *dub, const T *qbar, T *wbuf,
+               const T *dbar, T *grhs, T *gdt, T *gfspr, cudaStream_t s) {
+    const int n = a.t1 - a.t0;
+    if (n <= 0) return;
+    if (nfv == 5 && ndims == 3)
+        adj_lower_kernel<T, 5, 5, 3><<<grid_for(n), kBlock, 0, s>>>(a, gamma, pmin, factor, fnv, vec, fspr, dt, upts,
+                                                                     diag, dub, qbar, wbuf, dbar, grhs, gdt, gfspr);
+    else if (nfv == 4 && ndims == 2)
+        adj_lower_kernel<T, 4, 4, 2><<<grid_for(n), kBlock, 0, s>>>(a, gamma, pmin, factor, fnv, vec, fspr, dt, upts,
+                                                                     diag, dub, qbar, wbuf, dbar, grhs, gdt, gfspr);
+    else
+        ::ucfd::fail(UCFD_ERR_UNSUPPORTED, "adjoint built for nfvars/ndims 5/3 and 4/2 only");
+}
 
 // ---- scalar LU-SGS ---------------------------------------------------------
 template <typename T, int NV, int NFV, int NDIMS, bool RANS>

@@ -91,6 +91,10 @@ SIGNATURES = {
     "serial_ns_lusgs_update": (None, [_I, _P, _P]),
     "parallel_ns_lower_sweep": (None, [_I, _I, _I, _I] + [_P] * 9),
     "parallel_ns_upper_sweep": (None, [_I, _I, _I, _I] + [_P] * 9),
+    # ucfdadjoint.h
+    "UCFDReverseFaces": (_I, [_I, _I, _P, _P]),
+    "UCFDColoredStep": (_I, [_I, _I, _I, _I, _I, _I, _P, _P, _I, _P, _P, _D] + [_P] * 10),
+    "UCFDColoredStepAdjoint": (_I, [_I, _I, _I, _I, _I, _I, _P, _P, _P, _I, _P, _P, _D] + [_P] * 14),
     # ucfdmat.h
     "UCFDMatInit": (_I, [POINTER(c_void_p)]),
     "UCFDMatDestroy": (_I, [POINTER(c_void_p)]),
