@@ -386,6 +386,258 @@ def run_gpu(args):
     return out
 
 
+# ---------------------------------------------------------------------------
+# secondary workloads (one JSON line each; the default run is the BLU-SGS one)
+# ---------------------------------------------------------------------------
+def _events(stream):
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def lusgs_iter_bytes(rowptr, elt, nfv=5, nt=1):
+    """Algorithmic bytes of one scalar LU-SGS pseudo-time iteration per
+    UCFDLUSGS_Run (NS + RANS prepare, lower and upper sweeps, update), FlowSys
+    layout: per face its index, area, spectral radius and (once, in the sweep
+    where it is active) its normal; per cell the packed diagonal, the state
+    and increment of every variable read/written once."""
+    nnz = int(rowptr[-1])
+    N = rowptr.shape[0] - 1
+    nv = nfv + nt
+    per_face = (4 + 2 * elt) * 2 + (4 + 3 * elt + 2 * elt)   # NS prepare + sweeps
+    per_face += (4 + 2 * elt) + (4 + 3 * elt + 2 * elt)      # RANS prepare + sweeps
+    per_cell = 2 * nv * elt                                    # du = rhs copy
+    per_cell += elt + 2 * nfv * elt + elt + 2 * nt * elt       # rcp_vol, diag from base (NS, RANS)
+    per_cell += 2 * (elt + 5 * elt + 3 * nfv * elt)            # NS sweeps: rv, u, du own r/w + nbr, diag
+    per_cell += 2 * (elt + 5 * elt + 3 * nt * elt)             # RANS sweeps
+    per_cell += 3 * nv * elt                                   # u += du
+    return nnz * per_face + N * per_cell
+
+
+def run_lusgs(args):
+    """Steady pseudo-time loop: jittered, permuted hex, nvars = 5 + 1 RANS,
+    FP32 state, greedy colouring; args.iters iterations as a captured CUDA
+    graph (mode 0) and with persistent grid-synchronised sweeps (mode 1)."""
+    import torch
+
+    from ucfd_sparse_gb300 import _build, lib
+    from ucfd_sparse_gb300 import coloredlusgs as cl
+    from ucfd_sparse_gb300 import meshgen as mg
+    from ucfd_sparse_gb300.flowsys import FlowSys
+    _build.build()
+    lib.load()
+    m = args.mesh
+    t0 = time.perf_counter()
+    c = mg.lusgs_flowsys_case(m, nvars=6, seed=args.seed)
+    gen_s = time.perf_counter() - t0
+    N = c["nlocal"]
+    ic, rg, lc = cl.greedy_coloring_csr(c["rowptr"], c["colidx"])
+    dev = torch.device("cuda:0")
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    g = {k: T(c[k]) for k in ("rowptr", "colidx", "slots", "sides", "face_area", "face_normal", "rcp_vol", "fspr",
+                              "tfspr", "dt", "rhs", "cell_ids", "vol")}
+    up = T(c["upts"])
+    stream = torch.cuda.Stream(device=dev)
+    res = {}
+    for mode in (0, 1):
+        S = FlowSys(N, 6, 5, 3, c["nfaces"], 1, g["rowptr"], g["colidx"], g["slots"], g["sides"], g["face_area"],
+                    g["face_normal"], g["rcp_vol"])
+        S.set_coloring(lc)
+        S.set_precision(2)
+        S.set_stream(stream.cuda_stream, True)
+        uu = up.clone()
+        S.set_element(0, N, 6, g["cell_ids"], uu, g["rhs"], g["dt"], torch.zeros_like(uu), g["vol"],
+                      torch.zeros_like(uu))
+        S.set_lusgs(g["fspr"], g["tfspr"])
+        S.lusgs_pack(0, 1.0, 0.0)
+        hist = np.zeros(args.iters)
+        S.lusgs_run(3, 1.0, True, mode, None)          # warm-up (graph capture / occupancy query)
+        S.lusgs_pack(0, 1.0, 0.0)
+        torch.cuda.synchronize()
+        e0, e1 = _events(stream)
+        with ClockSampler(0) as clk:
+            e0.record(stream)
+            S.lusgs_run(args.iters, 1.0, True, mode, None)
+            e1.record(stream)
+            torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        S.lusgs_pack(0, 1.0, 0.0)
+        S.lusgs_run(args.iters, 1.0, True, mode, hist)
+        res[mode] = dict(ms=ms, clocks=clk.summary(), resid_first=float(hist[0]), resid_last=float(hist[-1]))
+        # scalar sweep kernel alone (per-level launches): NS lower sweep
+        if mode == 0:
+            S.lusgs_ns_prepare(1.0)
+            torch.cuda.synchronize()
+            e0, e1 = _events(stream)
+            e0.record(stream)
+            for _ in range(10):
+                S.lusgs_ns_lower(1.0)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            res["sweep_ms"] = e0.elapsed_time(e1) / 10
+        del S
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    bytes_iter = lusgs_iter_bytes(c["rowptr"], 4)
+    best = min(res[0]["ms"], res[1]["ms"])
+    rp = c["rowptr"]
+    nnz = int(rp[-1])
+    # NS lower sweep algorithmic bytes: faces' index + active half of the geometry, own/nbr state
+    sweep_bytes_ = nnz * 4 + (nnz // 2) * (5 * 4) + N * (4 + 5 * 4 + 3 * 5 * 4 + 5 * 4)
+    out = {"workload": "lusgs", "metric": METRIC, "unit": UNIT,
+           "config": {"workload": f"scalar LU-SGS pseudo-time loop, {m}^3 jittered permuted hex ({N} cells), "
+                                  f"nvars 5 + 1 RANS, FP32, greedy colouring ({len(rg)} colours), "
+                                  f"{args.iters} iterations", "cells": N, "colors": len(rg)},
+           "value": N * args.iters / (best * 1e-3),
+           "graph": {"ms": res[0]["ms"], "cell_updates_per_s": N * args.iters / (res[0]["ms"] * 1e-3),
+                     "GBps": bytes_iter * args.iters / (res[0]["ms"] * 1e-3) / 1e9},
+           "persistent": {"ms": res[1]["ms"], "cell_updates_per_s": N * args.iters / (res[1]["ms"] * 1e-3),
+                          "GBps": bytes_iter * args.iters / (res[1]["ms"] * 1e-3) / 1e9},
+           "bytes_per_cell_iteration": bytes_iter / N,
+           "roofline": {"bound": "hbm", "kernel": "scalar_sweep_kernel<float,6,5,3,false>",
+                        "achieved": sweep_bytes_ / (res["sweep_ms"] * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                        "frac": sweep_bytes_ / (res["sweep_ms"] * 1e-3) / 1e9 / peak,
+                        "sweep_ms": res["sweep_ms"], "algorithmic_bytes_per_sweep": sweep_bytes_},
+           "loop_frac_of_peak": bytes_iter * args.iters / (best * 1e-3) / 1e9 / peak,
+           "resid_fp64": [res[0]["resid_first"], res[0]["resid_last"]],
+           "clocks": res[0]["clocks"], "generation_s": gen_s}
+    print(json.dumps(out))
+
+
+def run_gmres(args):
+    """GMRES(30) with the coloured BLU-SGS preconditioner on the Kuhn-tet
+    BSR 5x5 system, to a 1e-10 relative residual: FP64 and mixed
+    (FP32 matvec + FP32 preconditioner inside FP64 Arnoldi/refinement)."""
+    import torch
+
+    from ucfd_sparse_gb300 import _build, lib
+    from ucfd_sparse_gb300 import coloredlusgs as cl
+    from ucfd_sparse_gb300 import meshgen as mg
+    from ucfd_sparse_gb300.krylov import Precon, Solver, SpMat
+    _build.build()
+    lib.load()
+    t0 = time.perf_counter()
+    s0 = mg.bsr_case(args.mesh, seed=args.seed)
+    tab = np.where(s0["nei"] >= 0, s0["nei"], np.arange(s0["bn"])[None, :]).astype(np.int32)
+    ic, rg, lc = cl.greedy_coloring(tab)
+    new = np.empty(s0["bn"], dtype=np.int64)
+    new[ic] = np.arange(s0["bn"])
+    s = mg.renumber_bsr(s0, new)
+    del s0
+    gen_s = time.perf_counter() - t0
+    bn = s["bn"]
+    n = bn * 5
+    dev = torch.device("cuda:0")
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    d = {k: T(s[k]) for k in ("rowptr", "colidx", "values", "diagslots", "rhs")}
+    icolors = np.array([0] + rg, dtype=np.int32)
+    A = SpMat(bn, 5, d["rowptr"], d["colidx"], d["values"], cuda=True)
+    tol = 1e-10 * float(np.linalg.norm(s["rhs"]))
+    res = {}
+    for prec in (1, 2):
+        pc = Precon(d["rowptr"], d["colidx"], d["diagslots"], d["values"])
+        pc.set_pblusgs(bn, 5, len(rg), icolors, cuda=True)
+        pc.set_precision(prec)
+        pc.prepare()
+        sv = Solver(n, 30, 100, tol, cuda=True)
+        sv.set_precision(prec)
+        x = torch.zeros(n, dtype=torch.float64, device=dev)
+        sv.solve(pc, A, x, d["rhs"])  # warm-up
+        x.zero_()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        sv.solve(pc, A, x, d["rhs"])
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t
+        st, it, r = sv.result()
+        res[prec] = dict(s=el, stat=st, restarts=it, resid=r / (tol / 1e-10), arnoldi=sv.arnoldi_steps())
+        # preconditioner apply alone
+        w = torch.randn(n, dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(10):
+            pc.apply(w)
+        torch.cuda.synchronize()
+        res[prec]["precon_ms"] = (time.perf_counter() - t) / 10 * 1e3
+        del pc, sv
+    # SpMV kernel alone (FP64 and FP32 values)
+    x = torch.randn(n, dtype=torch.float64, device=dev)
+    y = torch.zeros(n, dtype=torch.float64, device=dev)
+    sp = {}
+    for fp32 in (False, True):
+        A.mult(1.0, x, 0.0, y, fp32=fp32)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(20):
+            A.mult(1.0, x, 0.0, y, fp32=fp32)
+        torch.cuda.synchronize()
+        sp[fp32] = (time.perf_counter() - t) / 20 * 1e3
+    nnzb = int(s["rowptr"][-1])
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    b64 = nnzb * (4 + 25 * 8) + bn * (40 + 40)
+    b32 = nnzb * (4 + 25 * 4) + bn * (40 + 40)
+    out = {"workload": "gmres", "unit": "s to 1e-10",
+           "config": {"workload": f"GMRES(30) + coloured BLU-SGS, Kuhn tets of a {args.mesh}^3 box ({bn} cells, "
+                                  f"5x5 BSR, {nnzb} blocks), {len(rg)} colours, tol 1e-10 relative", "cells": bn},
+           "fp64": res[1], "mixed": res[2], "speedup_mixed_vs_fp64": res[1]["s"] / res[2]["s"],
+           "spmv": {"fp64_ms": sp[False], "fp32_ms": sp[True],
+                    "fp64_GBps": b64 / (sp[False] * 1e-3) / 1e9, "fp32_GBps": b32 / (sp[True] * 1e-3) / 1e9,
+                    "peak": peak, "fp64_frac": b64 / (sp[False] * 1e-3) / 1e9 / peak,
+                    "fp32_frac": b32 / (sp[True] * 1e-3) / 1e9 / peak},
+           "generation_s": gen_s}
+    print(json.dumps(out))
+
+
+def run_colored(args):
+    """The reference's own array API (colored LU-SGS step) on the 32^3 box,
+    FP64, args.iters steps: host numpy arrays (staged by the library) and
+    device tensors, against the oracle's CPU step."""
+    import torch
+
+    from oracle import oracle as orc
+    from ucfd_sparse_gb300 import _build, lib
+    from ucfd_sparse_gb300 import coloredlusgs as cl
+    from ucfd_sparse_gb300 import meshgen as mg
+    _build.build()
+    lib.load()
+    m = args.mesh
+    c = mg.lusgs_case(m)
+    icolor = cl.make_coloring(m, m, m)
+    ranges = [(m ** 3 + 1) // 2, m ** 3]
+    c["lcolor"] = mg.colors_from_icolor(icolor, ranges)
+    N = c["neles"]
+    out = {"workload": "colored", "unit": UNIT, "config": {"workload": f"colored LU-SGS array API, {m}^3 box, "
+                                                                       f"checkerboard, FP64, {args.iters} steps",
+                                                           "cells": N}}
+    for where in ("host", "device"):
+        if where == "device":
+            cc = dict(c, **{k: torch.from_numpy(np.ascontiguousarray(c[k])).cuda() for k in
+                            ("nei_ele", "fnorm_vol", "vec_fnorm", "fspr", "dt", "upts", "rhs", "lcolor")})
+            ic = torch.from_numpy(icolor).cuda()
+            diag = torch.zeros(N, dtype=torch.float64, device="cuda")
+            dub = torch.zeros_like(cc["rhs"])
+        else:
+            cc = dict(c, upts=c["upts"].copy(), rhs=c["rhs"].copy())
+            ic, diag, dub = icolor, np.zeros(N), np.zeros_like(c["rhs"])
+        cl.colored_step(cc, ic, ranges, diag, dub)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(args.iters):
+            cl.colored_step(cc, ic, ranges, diag, dub)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t
+        out[where] = {"s_per_step": el / args.iters, "cell_updates_per_s": N * args.iters / el}
+    p = orc.Port(fast=True)
+    t = time.perf_counter()
+    p.legacy_step(c, icolor, ranges, c["lcolor"], nsteps=args.iters)
+    el = time.perf_counter() - t
+    out["cpu_port"] = {"s_per_step": el / args.iters, "cell_updates_per_s": N * args.iters / el,
+                       "threads": os.cpu_count()}
+    print(json.dumps(out))
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -399,11 +651,20 @@ def main(argv=None):
     ap.add_argument("--check", type=int, default=4, help="FP64 solve: pairs between residual checks")
     ap.add_argument("--max-pairs", type=int, default=400)
     ap.add_argument("--ref-pairs", type=int, default=1)
+    ap.add_argument("--workload", default="blusgs", choices=["blusgs", "lusgs", "gmres", "colored"],
+                    help="blusgs: the headline line; the others measure the remaining configurations")
+    ap.add_argument("--iters", type=int, default=200, help="iterations of the lusgs/colored workloads")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "lusgs":
+        run_lusgs(args)
+    elif args.workload == "gmres":
+        run_gmres(args)
+    elif args.workload == "colored":
+        run_colored(args)
     else:
         run_gpu(args)
 

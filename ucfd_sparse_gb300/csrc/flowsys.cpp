@@ -79,6 +79,9 @@ struct _FlowSys {
     int run_rans = -1;
     double run_kappa = 0;
     bool run_state = false;  // set by UCFDLUSGS_Run, cleared by Pack
+    // persistent sweeps: level offsets on the device, barrier {count, gen}, timeout flag
+    DevBuf<int> d_lev_off, d_err;
+    DevBuf<unsigned> d_bar;
 
     cudaStream_t stream() const { return user ? user : own; }
 };
@@ -214,8 +217,12 @@ void need_mode(FlowSys s, int m) {
 }
 
 // ---- scalar LU-SGS --------------------------------------------------------
+// Polls of the persistent kernel's grid barrier before it gives up (each
+// poll sleeps ~64 ns): about a second, far beyond any legitimate wait.
+constexpr long long kBarrierMaxSpin = 1ll << 24;
+
 template <typename S, bool EX>
-void lusgs_sweep(FlowSys s, bool rans, bool upper, double kappa) {
+void lusgs_sweep(FlowSys s, bool rans, bool upper, double kappa, bool persistent = false) {
     Work<S> &w = work<S>(s);
     const long long N = s->N;
     ScalarSweepArgs<S> a{};
@@ -239,6 +246,13 @@ void lusgs_sweep(FlowSys s, bool rans, bool upper, double kappa) {
     a.pmin = (S)constants().pmin;
     a.upper = upper ? 1 : 0;
     const int L = s->sch.nlev;
+    if (persistent) {
+        // one cooperative launch per sweep, bounded grid barrier between levels
+        a.t0 = a.t1 = a.lo = a.hi = 0;
+        KCALL(EX, scalar_sweep_persistent<S>, a, s->nvars, s->nfvars, s->ndims, rans ? 1 : 0, s->d_lev_off.p, L,
+              s->d_bar.p, s->d_err.p, kBarrierMaxSpin, s->stream());
+        return;
+    }
     for (int q = 0; q < L; ++q) {
         const int l = upper ? L - 1 - q : q;
         a.t0 = s->sch.lev_off[l];
@@ -345,18 +359,18 @@ void blusgs_residual(FlowSys s, const Sx *x, R *r_out, double *rnorm, double *bn
 namespace {
 // One pseudo-time iteration on device-resident state (see UCFDLUSGS_Run).
 template <typename S, bool EX>
-void lusgs_iteration(FlowSys s, bool rans, double kappa, double *resid_slot) {
+void lusgs_iteration(FlowSys s, bool rans, double kappa, double *resid_slot, bool persistent) {
     Work<S> &w = work<S>(s);
     cudaStream_t st = s->stream();
     const size_t n = (size_t)s->nvars * s->N;
     UCFD_CUDA(cudaMemcpyAsync(w.du.p, w.rhs0.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
     lusgs_prepare<S, EX>(s, false, kappa, w.base.p);
-    lusgs_sweep<S, EX>(s, false, false, kappa);
-    lusgs_sweep<S, EX>(s, false, true, kappa);
+    lusgs_sweep<S, EX>(s, false, false, kappa, persistent);
+    lusgs_sweep<S, EX>(s, false, true, kappa, persistent);
     if (rans) {
         lusgs_prepare<S, EX>(s, true, kappa, w.base.p);
-        lusgs_sweep<S, EX>(s, true, false, kappa);
-        lusgs_sweep<S, EX>(s, true, true, kappa);
+        lusgs_sweep<S, EX>(s, true, false, kappa, persistent);
+        lusgs_sweep<S, EX>(s, true, true, kappa, persistent);
     }
     // u += du over the swept variables, ||du|| in FP64
     const int v1 = rans ? s->nvars : s->nfvars;
@@ -645,7 +659,7 @@ ucfd_status_t UCFDLUSGS_Run(FlowSys s, UCFDInt niter, UCFDReal kappa, int rans, 
                 cudaGraph_t g;
                 UCFD_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
                 try {
-                    lusgs_iteration<S, EX>(s, rans, kappa, s->red.p);
+                    lusgs_iteration<S, EX>(s, rans, kappa, s->red.p, false);
                 } catch (...) {
                     cudaStreamEndCapture(st, &g);
                     throw;
@@ -661,11 +675,21 @@ ucfd_status_t UCFDLUSGS_Run(FlowSys s, UCFDInt niter, UCFDReal kappa, int rans, 
                 UCFD_CUDA(cudaMemcpyAsync(s->resid.p + it, s->red.p, sizeof(double), cudaMemcpyDeviceToDevice, st));
             }
         } else {
-            for (int it = 0; it < niter; ++it) lusgs_iteration<S, EX>(s, rans, kappa, s->resid.p + it);
+            // persistent sweeps: barrier state and timeout flag start cleared
+            if (!s->d_lev_off.p) s->d_lev_off.upload(s->sch.lev_off.data(), s->sch.lev_off.size(), st);
+            s->d_bar.zero(2, st);
+            s->d_err.zero(1, st);
+            for (int it = 0; it < niter; ++it) lusgs_iteration<S, EX>(s, rans, kappa, s->resid.p + it, true);
         }
     });
     if (resid && niter > 0)
         UCFD_CUDA(cudaMemcpyAsync(resid, s->resid.p, niter * sizeof(double), cudaMemcpyDefault, st));
+    if (mode == 1) {
+        int err = 0;
+        UCFD_CUDA(cudaMemcpyAsync(&err, s->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+        UCFD_CUDA(cudaStreamSynchronize(st));
+        if (err) fail(UCFD_ERR_TIMEOUT, "persistent sweep: a grid barrier wait timed out");
+    }
     s->run_state = true;
     finish(s, resid != nullptr);
     UCFD_API_END

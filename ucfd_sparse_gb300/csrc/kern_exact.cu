@@ -6,6 +6,8 @@
 
 namespace kexact {
 template void scalar_sweep<double>(const ::ucfd::ScalarSweepArgs<double> &, int, int, int, int, int, cudaStream_t);
+template void scalar_sweep_persistent<double>(const ::ucfd::ScalarSweepArgs<double> &, int, int, int, int,
+                                              const int *, int, unsigned *, int *, long long, cudaStream_t);
 template void legacy_pre<double>(int, int, double, const double *, const double *, double *, const double *, cudaStream_t);
 template void legacy_update<double>(int, int, int, double *, const double *, cudaStream_t);
 template void fs_lusgs_pack<double>(int, int, int, long long, double, double, const int *, const int *, const double *,

@@ -6,6 +6,8 @@
 namespace kfast {
 #define UCFD_INST_T(T)                                                                                          \
     template void scalar_sweep<T>(const ::ucfd::ScalarSweepArgs<T> &, int, int, int, int, int, cudaStream_t);  \
+    template void scalar_sweep_persistent<T>(const ::ucfd::ScalarSweepArgs<T> &, int, int, int, int,           \
+                                             const int *, int, unsigned *, int *, long long, cudaStream_t);    \
     template void legacy_pre<T>(int, int, T, const T *, const T *, T *, const T *, cudaStream_t);              \
     template void legacy_update<T>(int, int, int, T *, const T *, cudaStream_t);                               \
     template void fs_lusgs_pack<T>(int, int, int, long long, double, double, const int *, const int *,         \

@@ -57,12 +57,79 @@ using ScalarSweepArgs = ::ucfd::ScalarSweepArgs<T>;
 
 // lower_sweep / upper_sweep of lusgs.c:157-257 for one level (or colour):
 // every cell of the range is independent of the others.
+template <typename T, int NV, int NFV, int NDIMS, bool RANS, bool COHERENT = false>
+__device__ __forceinline__ void scalar_sweep_cell(const ScalarSweepArgs<T> &a, int t);
+
 template <typename T, int NV, int NFV, int NDIMS, bool RANS>
 __global__ void __launch_bounds__(256) scalar_sweep_kernel(ScalarSweepArgs<T> a) {
-    constexpr int NV0 = RANS ? NFV : 0;
-    constexpr int DNV = RANS ? NV - NFV : NFV;
     const int t = a.t0 + blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.t1) return;
+    scalar_sweep_cell<T, NV, NFV, NDIMS, RANS>(a, t);
+}
+
+// Grid-wide barrier for a cooperative launch (all blocks co-resident).
+// Every wait is bounded: after max_spin polls the block records a timeout
+// in *err and leaves the barrier; the kernel then stops at once.  Returns
+// false after a timeout (also when another block reported one).
+__device__ inline bool grid_barrier_bounded(unsigned *count, unsigned *gen, int *err, long long max_spin) {
+    __shared__ int ok_sh;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        volatile unsigned *vgen = gen;
+        const unsigned g = *vgen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(count, 1u);
+        if (arrived == gridDim.x - 1) {
+            *count = 0u;
+            __threadfence();
+            atomicAdd(gen, 1u);
+        } else {
+            long long spins = 0;
+            while (*vgen == g) {
+                if (*(volatile int *)err) {
+                    ok = 0;
+                    break;
+                }
+                if (++spins > max_spin) {
+                    atomicExch(err, 1);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        ok_sh = ok;
+    }
+    __syncthreads();
+    return ok_sh != 0;
+}
+
+// One whole sweep (every level, ascending or descending) in one
+// cooperative launch: the blocks stride over the cells of a level, then
+// meet at the bounded grid barrier before the next level.
+template <typename T, int NV, int NFV, int NDIMS, bool RANS>
+__global__ void __launch_bounds__(256) scalar_sweep_persistent_kernel(ScalarSweepArgs<T> a, const int *lev_off,
+                                                                      int nlev, unsigned *bar, int *err,
+                                                                      long long max_spin) {
+    for (int q = 0; q < nlev; ++q) {
+        const int l = a.upper ? nlev - 1 - q : q;
+        ScalarSweepArgs<T> b = a;
+        b.t0 = lev_off[l];
+        b.t1 = lev_off[l + 1];
+        b.lo = b.t0;
+        b.hi = b.t1;
+        for (int t = b.t0 + blockIdx.x * blockDim.x + threadIdx.x; t < b.t1; t += gridDim.x * blockDim.x)
+            scalar_sweep_cell<T, NV, NFV, NDIMS, RANS, true>(b, t);
+        if (q + 1 < nlev && !grid_barrier_bounded(bar, bar + 1, err, max_spin)) return;
+    }
+}
+
+template <typename T, int NV, int NFV, int NDIMS, bool RANS, bool COHERENT>
+__device__ __forceinline__ void scalar_sweep_cell(const ScalarSweepArgs<T> &a, int t) {
+    constexpr int NV0 = RANS ? NFV : 0;
+    constexpr int DNV = RANS ? NV - NFV : NFV;
     const long long ld = a.ld;
     const int i = a.cells ? __ldg(a.cells + t) : t;
     const int ci = a.lcolor ? __ldg(a.lcolor + i) : 0;
@@ -102,7 +169,8 @@ __global__ void __launch_bounds__(256) scalar_sweep_kernel(ScalarSweepArgs<T> a)
                 uu[q][v] = need ? __ldg(a.u + v * ld + g) : T(0);
             }
 #pragma unroll
-            for (int k = 0; k < DNV; ++k) dn[q][k] = a.nbsrc[(k + NV0) * ld + g];
+            for (int k = 0; k < DNV; ++k)
+                dn[q][k] = COHERENT ? __ldcg(a.nbsrc + (k + NV0) * ld + g) : a.nbsrc[(k + NV0) * ld + g];
             const int f = act[q] ? f0 + q : 0;
 #pragma unroll
             for (int d = 0; d < NDIMS; ++d) nf[q][d] = __ldg(a.nrm + (f * NDIMS + d) * ld + i);

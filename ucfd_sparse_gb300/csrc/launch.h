@@ -19,6 +19,10 @@
     void scalar_sweep(const ::ucfd::ScalarSweepArgs<T> &a, int nv, int nfv, int ndims, int rans,   \
                       int block, cudaStream_t s);                                                  \
     template <typename T>                                                                          \
+    void scalar_sweep_persistent(const ::ucfd::ScalarSweepArgs<T> &a, int nv, int nfv, int ndims,  \
+                                 int rans, const int *lev_off, int nlev, unsigned *bar, int *err,  \
+                                 long long max_spin, cudaStream_t s);                              \
+    template <typename T>                                                                          \
     void legacy_pre(int neles, int nface, T factor, const T *fnorm_vol, const T *dt, T *diag,      \
                     const T *fspr, cudaStream_t s);                                                \
     template <typename T>                                                                          \

@@ -77,6 +77,50 @@ void scalar_sweep(const ::ucfd::ScalarSweepArgs<T> &a, int nv, int nfv, int ndim
                  nv, nfv, ndims, rans ? "RANS" : "NS");
 }
 
+template <typename T, int NV, int NFV, int NDIMS, bool RANS>
+static void persistent_go(const ::ucfd::ScalarSweepArgs<T> &a, const int *lev_off, int nlev, unsigned *bar,
+                          int *err, long long max_spin, cudaStream_t s) {
+    auto kern = scalar_sweep_persistent_kernel<T, NV, NFV, NDIMS, RANS>;
+    static int grid = 0;  // per instantiation: blocks that fit co-resident
+    if (!grid) {
+        int per_sm = 0, dev = 0, sms = 0;
+        UCFD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kBlock, 0));
+        UCFD_CUDA(cudaGetDevice(&dev));
+        UCFD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        grid = per_sm * sms;
+        if (grid <= 0) ::ucfd::fail(UCFD_ERR_UNSUPPORTED, "persistent sweep kernel does not fit on the device");
+    }
+    ::ucfd::ScalarSweepArgs<T> aa = a;
+    void *args[] = {(void *)&aa, (void *)&lev_off, (void *)&nlev, (void *)&bar, (void *)&err, (void *)&max_spin};
+    UCFD_CUDA(cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(kBlock), args, 0, s));
+}
+
+// Whole sweep (all nlev levels) as one cooperative launch with a bounded
+// grid barrier between levels; lev_off is a device array.
+template <typename T>
+void scalar_sweep_persistent(const ::ucfd::ScalarSweepArgs<T> &a, int nv, int nfv, int ndims, int rans,
+                             const int *lev_off, int nlev, unsigned *bar, int *err, long long max_spin,
+                             cudaStream_t s) {
+#define UCFD_PSW(NV, NFV, ND)                                                                              \
+    if (nv == NV && nfv == NFV && ndims == ND) {                                                           \
+        if (rans) {                                                                                        \
+            if constexpr (NV > NFV) return persistent_go<T, NV, NFV, ND, true>(a, lev_off, nlev, bar, err, \
+                                                                                max_spin, s);              \
+        } else {                                                                                           \
+            return persistent_go<T, NV, NFV, ND, false>(a, lev_off, nlev, bar, err, max_spin, s);          \
+        }                                                                                                  \
+    }
+    UCFD_PSW(5, 5, 3)
+    UCFD_PSW(6, 5, 3)
+    UCFD_PSW(7, 5, 3)
+    UCFD_PSW(4, 4, 2)
+    UCFD_PSW(5, 4, 2)
+    UCFD_PSW(6, 4, 2)
+#undef UCFD_PSW
+    ::ucfd::fail(UCFD_ERR_UNSUPPORTED, "persistent sweep for nvars=%d nfvars=%d ndims=%d is not built", nv, nfv,
+                 ndims);
+}
+
 template <typename T>
 void legacy_pre(int neles, int nface, T factor, const T *fnorm_vol, const T *dt, T *diag,
                 const T *fspr, cudaStream_t s) {
