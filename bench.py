@@ -427,7 +427,7 @@ def run_lusgs(args):
     lib.load()
     m = args.mesh
     t0 = time.perf_counter()
-    c = mg.lusgs_flowsys_case(m, nvars=6, seed=args.seed)
+    c = mg.lusgs_flowsys_case(m, nvars=6, seed=args.seed, rhs_scale=1e-3)
     gen_s = time.perf_counter() - t0
     N = c["nlocal"]
     ic, rg, lc = cl.greedy_coloring_csr(c["rowptr"], c["colidx"])

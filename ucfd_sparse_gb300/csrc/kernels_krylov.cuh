@@ -12,33 +12,75 @@
 
 namespace UCFD_KNS {
 
+// acc[r] += SGN * sum over the ELL row k of (block_p x_{col_p})[r], entries in
+// stored order, each block product summed over its columns first (the
+// reference's order, sparsemat.c:82-97, blusgs.c:113-124).  PW > 0: the
+// row width is at most PW and the loop is unrolled so that every column
+// index, then every gathered x and block value, is requested up front;
+// PW == 0: runtime-width loop.  Padding entries (column < 0) end the row.
+template <typename Tv, typename Tx, typename Ta, int B, int PW, int SGN>
+__device__ __forceinline__ void ell_row_products(long long k, int bn, int P, const int *col, const Tv *val,
+                                                 const Tx *x, Ta *acc) {
+    constexpr int B2 = B * B;
+    if constexpr (PW > 0) {
+        int c[PW];
+#pragma unroll
+        for (int p = 0; p < PW; ++p) c[p] = p < P ? __ldg(col + (long long)p * bn + k) : -1;
+        Ta xv[PW][B];
+#pragma unroll
+        for (int p = 0; p < PW; ++p) {
+            const long long g = c[p] >= 0 ? c[p] : 0;  // padding: any valid address
+#pragma unroll
+            for (int cc = 0; cc < B; ++cc) xv[p][cc] = (Ta)x[g * B + cc];
+        }
+        bool live = true;
+#pragma unroll
+        for (int p = 0; p < PW; ++p) {
+            live = live && c[p] >= 0;
+            if (live) {
+                const Tv *vp = val + (long long)p * B2 * bn + k;
+#pragma unroll
+                for (int r = 0; r < B; ++r) {
+                    Ta v = Ta(0);
+#pragma unroll
+                    for (int cc = 0; cc < B; ++cc) v += (Ta)__ldg(vp + (long long)(r * B + cc) * bn) * xv[p][cc];
+                    if (SGN > 0) acc[r] += v;
+                    else acc[r] -= v;
+                }
+            }
+        }
+    } else {
+        for (int p = 0; p < P; ++p) {
+            const int c = __ldg(col + (long long)p * bn + k);
+            if (c < 0) break;
+            Ta xv[B];
+#pragma unroll
+            for (int cc = 0; cc < B; ++cc) xv[cc] = (Ta)x[(long long)c * B + cc];
+            const Tv *vp = val + (long long)p * B2 * bn + k;
+#pragma unroll
+            for (int r = 0; r < B; ++r) {
+                Ta v = Ta(0);
+#pragma unroll
+                for (int cc = 0; cc < B; ++cc) v += (Ta)__ldg(vp + (long long)(r * B + cc) * bn) * xv[cc];
+                if (SGN > 0) acc[r] += v;
+                else acc[r] -= v;
+            }
+        }
+    }
+}
+
 // SpMV_BSR: sparsemat.c:57-101 -- y = alpha*A*x + beta*y.  Tv is the type
 // of the stored values, Ta the accumulation type.
-template <typename Tv, typename Ta, int B>
+template <typename Tv, typename Ta, int B, int PW>
 __global__ void __launch_bounds__(256) bsr_spmv_kernel(int bn, int P, const int *col, const Tv *val,
                                                        double alpha, const double *x, double beta,
                                                        double *y) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= bn) return;
-    constexpr int B2 = B * B;
     Ta acc[B];
 #pragma unroll
     for (int r = 0; r < B; ++r) acc[r] = Ta(0);
-    for (int p = 0; p < P; ++p) {
-        const int c = __ldg(col + (long long)p * bn + i);
-        if (c < 0) break;
-        Ta xv[B];
-#pragma unroll
-        for (int cc = 0; cc < B; ++cc) xv[cc] = (Ta)__ldg(x + (long long)c * B + cc);
-        const Tv *vp = val + (long long)p * B2 * bn + i;
-#pragma unroll
-        for (int r = 0; r < B; ++r) {
-            Ta v = Ta(0);
-#pragma unroll
-            for (int cc = 0; cc < B; ++cc) v += (Ta)__ldg(vp + (long long)(r * B + cc) * bn) * xv[cc];
-            acc[r] += v;
-        }
-    }
+    ell_row_products<Tv, double, Ta, B, PW, +1>(i, bn, P, col, val, x, acc);
 #pragma unroll
     for (int r = 0; r < B; ++r) {
         const long long o = (long long)i * B + r;
@@ -68,7 +110,7 @@ __global__ void pc_prepare_kernel(int bn, const int *perm, const long long *dslo
 
 // Forward (lower) step of the block SGS apply for rows [t0, t1) of one
 // level: precon/blusgs.c:104-130 (b -> x' in place).
-template <typename T, int B>
+template <typename T, int B, int PW>
 __global__ void __launch_bounds__(256) pc_lower_kernel(int t0, int t1, int bn, int PL, const int *Lcol,
                                                        const T *Lval, const T *LU, T *b) {
     const int k = t0 + blockIdx.x * blockDim.x + threadIdx.x;
@@ -77,21 +119,7 @@ __global__ void __launch_bounds__(256) pc_lower_kernel(int t0, int t1, int bn, i
     T arr[B];
 #pragma unroll
     for (int r = 0; r < B; ++r) arr[r] = b[(long long)k * B + r];
-    for (int p = 0; p < PL; ++p) {
-        const int c = __ldg(Lcol + (long long)p * bn + k);
-        if (c < 0) break;
-        T xv[B];
-#pragma unroll
-        for (int cc = 0; cc < B; ++cc) xv[cc] = b[(long long)c * B + cc];
-        const T *vp = Lval + (long long)p * B2 * bn + k;
-#pragma unroll
-        for (int r = 0; r < B; ++r) {
-            T v = T(0);
-#pragma unroll
-            for (int cc = 0; cc < B; ++cc) v += __ldg(vp + (long long)(r * B + cc) * bn) * xv[cc];
-            arr[r] -= v;
-        }
-    }
+    ell_row_products<T, T, T, B, PW, -1>(k, bn, PL, Lcol, Lval, b, arr);
     T lu[B2];
 #pragma unroll
     for (int e = 0; e < B2; ++e) lu[e] = __ldg(LU + (long long)e * bn + k);
@@ -101,7 +129,7 @@ __global__ void __launch_bounds__(256) pc_lower_kernel(int t0, int t1, int bn, i
 }
 
 // Backward (upper) step: precon/blusgs.c:132-161 (x = x' - inv(D) U x).
-template <typename T, int B>
+template <typename T, int B, int PW>
 __global__ void __launch_bounds__(256) pc_upper_kernel(int t0, int t1, int bn, int PU, const int *Ucol,
                                                        const T *Uval, const T *LU, T *b) {
     const int k = t0 + blockIdx.x * blockDim.x + threadIdx.x;
@@ -110,21 +138,7 @@ __global__ void __launch_bounds__(256) pc_upper_kernel(int t0, int t1, int bn, i
     T arr[B];
 #pragma unroll
     for (int r = 0; r < B; ++r) arr[r] = T(0);
-    for (int p = 0; p < PU; ++p) {
-        const int c = __ldg(Ucol + (long long)p * bn + k);
-        if (c < 0) break;
-        T xv[B];
-#pragma unroll
-        for (int cc = 0; cc < B; ++cc) xv[cc] = b[(long long)c * B + cc];
-        const T *vp = Uval + (long long)p * B2 * bn + k;
-#pragma unroll
-        for (int r = 0; r < B; ++r) {
-            T v = T(0);
-#pragma unroll
-            for (int cc = 0; cc < B; ++cc) v += __ldg(vp + (long long)(r * B + cc) * bn) * xv[cc];
-            arr[r] += v;
-        }
-    }
+    ell_row_products<T, T, T, B, PW, +1>(k, bn, PU, Ucol, Uval, b, arr);
     T lu[B2];
 #pragma unroll
     for (int e = 0; e < B2; ++e) lu[e] = __ldg(LU + (long long)e * bn + k);
@@ -157,75 +171,14 @@ __global__ void scatter_rows_kernel(int bn, int B, const int *perm, const Ts *sr
 constexpr int kMaxK = 32;  // restart length + 1 <= kMaxK
 
 // Per-block partial dots h[k] = sum_i V[k][i] * w[i], k < K.
-__global__ void __launch_bounds__(256) gm_dots_kernel(long long n, int K, const double *V, long long ldv,
-                                                      const double *w, double *part) {
-    double acc[kMaxK];
-#pragma unroll
-    for (int k = 0; k < kMaxK; ++k) acc[k] = 0.0;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x) {
-        const double wi = w[i];
-#pragma unroll
-        for (int k = 0; k < kMaxK; ++k)
-            if (k < K) acc[k] += V[k * ldv + i] * wi;
-    }
-    __shared__ double sm[kMaxK][9];
+// Block partials of KM accumulators (only the first KK meaningful) into
+// part[block][k].
+template <int KM>
+__device__ __forceinline__ void gm_block_partials(const double *acc, int KK, double *part) {
+    __shared__ double sm[KM][9];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-    for (int k = 0; k < kMaxK; ++k) {
-        if (k < K) {
-            double v = acc[k];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-            if (lane == 0) sm[k][wid] = v;
-        }
-    }
-    __syncthreads();
-    if (threadIdx.x < K) {
-        double s = 0.0;
-        const int nw = blockDim.x >> 5;
-        for (int q = 0; q < nw; ++q) s += sm[threadIdx.x][q];
-        part[(long long)blockIdx.x * kMaxK + threadIdx.x] = s;
-    }
-}
-
-// w_out = w - V h (gemvcol with alpha -1, beta 1), then either the partial
-// dots V^T w_out (mode 0) or the partial sum of w_out^2 (mode 1).
-__global__ void __launch_bounds__(256) gm_update_kernel(long long n, int K, const double *V, long long ldv,
-                                                        const double *h, double *w, int mode,
-                                                        double *part) {
-    double acc[kMaxK];
-#pragma unroll
-    for (int k = 0; k < kMaxK; ++k) acc[k] = 0.0;
-    __shared__ double hs[kMaxK];
-    if (threadIdx.x < kMaxK) hs[threadIdx.x] = threadIdx.x < K ? h[threadIdx.x] : 0.0;
-    __syncthreads();
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x) {
-        double v[kMaxK];
-        double s = 0.0;
-#pragma unroll
-        for (int k = 0; k < kMaxK; ++k) {
-            if (k < K) {
-                v[k] = V[k * ldv + i];
-                s += v[k] * hs[k];
-            }
-        }
-        const double wn = -1.0 * s + 1.0 * w[i];
-        w[i] = wn;
-        if (mode == 0) {
-#pragma unroll
-            for (int k = 0; k < kMaxK; ++k)
-                if (k < K) acc[k] += v[k] * wn;
-        } else {
-            acc[0] += wn * wn;
-        }
-    }
-    const int KK = mode == 0 ? K : 1;
-    __shared__ double sm[kMaxK][9];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int k = 0; k < kMaxK; ++k) {
+    for (int k = 0; k < KM; ++k) {
         if (k < KK) {
             double v = acc[k];
 #pragma unroll
@@ -240,6 +193,55 @@ __global__ void __launch_bounds__(256) gm_update_kernel(long long n, int K, cons
         for (int q = 0; q < nw; ++q) s += sm[threadIdx.x][q];
         part[(long long)blockIdx.x * kMaxK + threadIdx.x] = s;
     }
+}
+
+// Per-block partial dots h[k] = sum_i V[k][i] * w[i], k < K <= KM.
+template <int KM>
+__global__ void __launch_bounds__(256, (KM > 8 ? 3 : 4)) gm_dots_kernel(long long n, int K, const double *V, long long ldv,
+                                                      const double *w, double *part) {
+    double acc[KM];
+#pragma unroll
+    for (int k = 0; k < KM; ++k) acc[k] = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double wi = w[i];
+#pragma unroll
+        for (int k = 0; k < KM; ++k)
+            if (k < K) acc[k] += V[k * ldv + i] * wi;
+    }
+    gm_block_partials<KM>(acc, K, part);
+}
+
+// w_out = w - V h (gemvcol with alpha -1, beta 1), then either the partial
+// dots V^T w_out (mode 0) or the partial sum of w_out^2 (mode 1).  The
+// second pass over V re-reads the values this thread just loaded (L1).
+template <int KM>
+__global__ void __launch_bounds__(256, (KM > 8 ? 2 : 4)) gm_update_kernel(long long n, int K, const double *V, long long ldv,
+                                                        const double *h, double *w, int mode,
+                                                        double *part) {
+    double acc[KM];
+#pragma unroll
+    for (int k = 0; k < KM; ++k) acc[k] = 0.0;
+    __shared__ double hs[KM];
+    if (threadIdx.x < KM) hs[threadIdx.x] = threadIdx.x < K ? h[threadIdx.x] : 0.0;
+    __syncthreads();
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        double s = 0.0;
+#pragma unroll
+        for (int k = 0; k < KM; ++k)
+            if (k < K) s += V[k * ldv + i] * hs[k];
+        const double wn = -1.0 * s + 1.0 * w[i];
+        w[i] = wn;
+        if (mode == 0) {
+#pragma unroll
+            for (int k = 0; k < KM; ++k)
+                if (k < K) acc[k] += V[k * ldv + i] * wn;
+        } else {
+            acc[0] += wn * wn;
+        }
+    }
+    gm_block_partials<KM>(acc, mode == 0 ? K : 1, part);
 }
 
 // Sum the per-block partials: out[k] = sum_b part[b][k] (one block, fixed order).
@@ -299,9 +301,13 @@ __global__ void gm_scale_kernel(long long n, const GmState *st, const double *sr
 // Arnoldi step j tail: H[:,j] = h1 + h2, H[j+1,j] = ||w||, previous
 // rotations, new rotation, y update and happy-breakdown test
 // (gmres.c:81-107 and 86-103).
+// rel_floor > 0 (mixed precision only): the cycle also ends (stop = 2) once
+// the Givens residual estimate |y[j+1]| falls below rel_floor * beta, the
+// accuracy an FP32 operator can deliver; the FP64 restart then refreshes the
+// true residual.
 __global__ void gm_givens_kernel(int j, int ld, int nblocks, const double *part_norm, double *H,
                                  const double *h2, double *cs, double *sn, double *y, double haptol,
-                                 GmState *st) {
+                                 double rel_floor, GmState *st) {
     if (st->stop) return;
     double s = 0.0;
     for (int b = 0; b < nblocks; ++b) s += part_norm[(long long)b * kMaxK];
@@ -327,6 +333,7 @@ __global__ void gm_givens_kernel(int j, int ld, int nblocks, const double *part_
     st->k = j + 1;
     st->total += 1;
     if (hsub < haptol * st->beta) st->stop = 1;
+    else if (rel_floor > 0.0 && fabs(y[j + 1]) <= rel_floor * st->beta) st->stop = 2;
 }
 
 // Back substitution of the k x k triangle (gmres.c:111-117).

@@ -266,6 +266,9 @@ struct _Solver {
     std::vector<double> hist;
     int n = 0, m = 0;
     int prec = UCFD_PREC_FP64;
+    // mixed precision: a cycle ends when its residual estimate drops below
+    // this fraction of the cycle's start (FP32 operator accuracy)
+    double mixed_floor = 1e-6;
     long long arnoldi = 0;
     long long ldv = 0;
     DevBuf<double> V, w, r, H, cs, sn, y, h2, part, abeta;
@@ -330,8 +333,16 @@ struct _Solver {
                 kfast::gm_update(n, K, V.p, ldv, Hc, w.p, 0, part.p, s);
                 kfast::gm_reduce(nb, K, part.p, h2.p, 0, s);
                 kfast::gm_update(n, K, V.p, ldv, h2.p, w.p, 1, part.p, s);
-                kfast::gm_givens(j, ld, nb, part.p, H.p, h2.p, cs.p, sn.p, y.p, haptol, st.p, s);
+                kfast::gm_givens(j, ld, nb, part.p, H.p, h2.p, cs.p, sn.p, y.p, haptol, mixed ? mixed_floor : 0.0,
+                                 st.p, s);
                 kfast::gm_scale(n, st.p, w.p, V.p + (size_t)(j + 1) * ldv, s);
+                if (mixed) {
+                    // an FP32 operator cannot resolve the cycle below its floor: stop
+                    // launching once the device reports it (one host read per step)
+                    UCFD_CUDA(cudaMemcpyAsync(h_st.p, st.p, kfast::gm_state_bytes(), cudaMemcpyDeviceToHost, s));
+                    UCFD_CUDA(cudaStreamSynchronize(s));
+                    if (((const int *)h_st.p)[1]) break;
+                }
             }
             kfast::gm_backsub(ld, H.p, y.p, st.p, s);
             kfast::gm_solution(n, V.p, ldv, y.p, st.p, x, s);
@@ -339,7 +350,7 @@ struct _Solver {
             UCFD_CUDA(cudaMemcpyAsync(h_st.p, st.p, kfast::gm_state_bytes(), cudaMemcpyDeviceToHost, s));
             UCFD_CUDA(cudaStreamSynchronize(s));
             const int *sti = (const int *)h_st.p;  // {k, stop, total}
-            if (sti[1]) breakdown = true;
+            if (sti[1] == 1) breakdown = true;
             arnoldi = sti[2];
             iter++;
         }

@@ -118,8 +118,8 @@
                         cudaStream_t s);                                                           \
     void gm_scale(long long n, const void *st, const double *src, double *dst, cudaStream_t s);    \
     void gm_givens(int j, int ld, int nblocks, const double *part_norm, double *H,                 \
-                   const double *h2, double *cs, double *sn, double *y, double haptol, void *st,   \
-                   cudaStream_t s);                                                                \
+                   const double *h2, double *cs, double *sn, double *y, double haptol,             \
+                   double rel_floor, void *st, cudaStream_t s);                                    \
     void gm_backsub(int ld, const double *H, double *y, const void *st, cudaStream_t s);           \
     void gm_solution(long long n, const double *V, long long ldv, const double *y,                 \
                      const void *st, double *x, cudaStream_t s);                                   \

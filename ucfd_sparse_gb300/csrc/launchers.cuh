@@ -285,8 +285,17 @@ void bsr_spmv(int B, int bn, int P, const int *col, const Tv *val, double alpha,
               double beta, double *y, int block, cudaStream_t s) {
     if (bn <= 0) return;
     if (block <= 0) block = kBlock;
-    UCFD_KSW(B, (bsr_spmv_kernel<Tv, Ta, BB><<<grid_for(bn, block), block, 0, s>>>(bn, P, col, val, alpha, x,
-                                                                                   beta, y)));
+    const unsigned g = grid_for(bn, block);
+    // unrolled rows for the 5x5 systems (tets: diag + 4 faces; hexes: + 6)
+    if (B == 5 && P <= 5) {
+        bsr_spmv_kernel<Tv, Ta, 5, 5><<<g, block, 0, s>>>(bn, P, col, val, alpha, x, beta, y);
+        return;
+    }
+    if (B == 5 && P <= 7) {
+        bsr_spmv_kernel<Tv, Ta, 5, 7><<<g, block, 0, s>>>(bn, P, col, val, alpha, x, beta, y);
+        return;
+    }
+    UCFD_KSW(B, (bsr_spmv_kernel<Tv, Ta, BB, 0><<<g, block, 0, s>>>(bn, P, col, val, alpha, x, beta, y)));
 }
 
 template <typename Tl>
@@ -302,8 +311,16 @@ void pc_lower(int B, int t0, int t1, int bn, int PL, const int *Lcol, const T *L
               int block, cudaStream_t s) {
     if (t1 <= t0) return;
     if (block <= 0) block = kBlock;
-    UCFD_KSW(B, (pc_lower_kernel<T, BB><<<grid_for(t1 - t0, block), block, 0, s>>>(t0, t1, bn, PL, Lcol, Lval,
-                                                                                   LU, b)));
+    const unsigned g = grid_for(t1 - t0, block);
+    if (B == 5 && PL <= 4) {
+        pc_lower_kernel<T, 5, 4><<<g, block, 0, s>>>(t0, t1, bn, PL, Lcol, Lval, LU, b);
+        return;
+    }
+    if (B == 5 && PL <= 6) {
+        pc_lower_kernel<T, 5, 6><<<g, block, 0, s>>>(t0, t1, bn, PL, Lcol, Lval, LU, b);
+        return;
+    }
+    UCFD_KSW(B, (pc_lower_kernel<T, BB, 0><<<g, block, 0, s>>>(t0, t1, bn, PL, Lcol, Lval, LU, b)));
 }
 
 template <typename T>
@@ -311,8 +328,16 @@ void pc_upper(int B, int t0, int t1, int bn, int PU, const int *Ucol, const T *U
               int block, cudaStream_t s) {
     if (t1 <= t0) return;
     if (block <= 0) block = kBlock;
-    UCFD_KSW(B, (pc_upper_kernel<T, BB><<<grid_for(t1 - t0, block), block, 0, s>>>(t0, t1, bn, PU, Ucol, Uval,
-                                                                                   LU, b)));
+    const unsigned g = grid_for(t1 - t0, block);
+    if (B == 5 && PU <= 4) {
+        pc_upper_kernel<T, 5, 4><<<g, block, 0, s>>>(t0, t1, bn, PU, Ucol, Uval, LU, b);
+        return;
+    }
+    if (B == 5 && PU <= 6) {
+        pc_upper_kernel<T, 5, 6><<<g, block, 0, s>>>(t0, t1, bn, PU, Ucol, Uval, LU, b);
+        return;
+    }
+    UCFD_KSW(B, (pc_upper_kernel<T, BB, 0><<<g, block, 0, s>>>(t0, t1, bn, PU, Ucol, Uval, LU, b)));
 }
 
 template <typename Ts, typename Td>
@@ -382,14 +407,23 @@ int gm_blocks(long long n) {
     return (int)(g < kRedBlocks ? (g > 0 ? g : 1) : kRedBlocks);
 }
 
+// the vector count K picks the smallest compiled bound (register footprint)
 void gm_dots(long long n, int K, const double *V, long long ldv, const double *w, double *part,
              cudaStream_t s) {
-    gm_dots_kernel<<<gm_blocks(n), kBlock, 0, s>>>(n, K, V, ldv, w, part);
+    const int g = gm_blocks(n);
+    if (K <= 4) gm_dots_kernel<4><<<g, kBlock, 0, s>>>(n, K, V, ldv, w, part);
+    else if (K <= 8) gm_dots_kernel<8><<<g, kBlock, 0, s>>>(n, K, V, ldv, w, part);
+    else if (K <= 16) gm_dots_kernel<16><<<g, kBlock, 0, s>>>(n, K, V, ldv, w, part);
+    else gm_dots_kernel<32><<<g, kBlock, 0, s>>>(n, K, V, ldv, w, part);
 }
 
 void gm_update(long long n, int K, const double *V, long long ldv, const double *h, double *w, int mode,
                double *part, cudaStream_t s) {
-    gm_update_kernel<<<gm_blocks(n), kBlock, 0, s>>>(n, K, V, ldv, h, w, mode, part);
+    const int g = gm_blocks(n);
+    if (K <= 4) gm_update_kernel<4><<<g, kBlock, 0, s>>>(n, K, V, ldv, h, w, mode, part);
+    else if (K <= 8) gm_update_kernel<8><<<g, kBlock, 0, s>>>(n, K, V, ldv, h, w, mode, part);
+    else if (K <= 16) gm_update_kernel<16><<<g, kBlock, 0, s>>>(n, K, V, ldv, h, w, mode, part);
+    else gm_update_kernel<32><<<g, kBlock, 0, s>>>(n, K, V, ldv, h, w, mode, part);
 }
 
 void gm_reduce(int nblocks, int K, const double *part, double *out, int accumulate, cudaStream_t s) {
@@ -409,8 +443,9 @@ void gm_scale(long long n, const void *st, const double *src, double *dst, cudaS
 }
 
 void gm_givens(int j, int ld, int nblocks, const double *part_norm, double *H, const double *h2, double *cs,
-               double *sn, double *y, double haptol, void *st, cudaStream_t s) {
-    gm_givens_kernel<<<1, 1, 0, s>>>(j, ld, nblocks, part_norm, H, h2, cs, sn, y, haptol, (GmState *)st);
+               double *sn, double *y, double haptol, double rel_floor, void *st, cudaStream_t s) {
+    gm_givens_kernel<<<1, 1, 0, s>>>(j, ld, nblocks, part_norm, H, h2, cs, sn, y, haptol, rel_floor,
+                                     (GmState *)st);
 }
 
 void gm_backsub(int ld, const double *H, double *y, const void *st, cudaStream_t s) {

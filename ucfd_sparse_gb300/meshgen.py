@@ -318,10 +318,14 @@ def blusgs_case(m: int, nvars: int = 5, jitter: float = 0.2, permute: bool = Tru
     return fs
 
 
-def lusgs_flowsys_case(m: int, nvars: int = 6, jitter: float = 0.2, permute: bool = True, seed: int = 0):
+def lusgs_flowsys_case(m: int, nvars: int = 6, jitter: float = 0.2, permute: bool = True, seed: int = 0,
+                       rhs_scale: float = 1.0):
     """Scalar LU-SGS FlowSys workload: jittered, permuted hex mesh with
     per-face spectral radii fspr, tfspr ~ U[0.5, 2], dt ~ U[1e-3, 1e-2],
-    rhs ~ N(0, 1) and the free stream (turbulence variables ~ U[0.1, 1])."""
+    rhs ~ N(0, 1) * rhs_scale and the free stream (turbulence variables
+    ~ U[0.1, 1]).  A pseudo-time loop that re-applies the same rhs drifts
+    the state by ~rhs/diag per iteration; rhs_scale = 1e-3 keeps it physical
+    for thousands of iterations."""
     mesh = HexMesh(m, jitter=jitter, seed=seed)
     N = mesh.ncells
     perm = random_perm(N, seed + 1) if permute else np.arange(N)
@@ -333,7 +337,7 @@ def lusgs_flowsys_case(m: int, nvars: int = 6, jitter: float = 0.2, permute: boo
         upts[5:] = rng.uniform(0.1, 1.0, size=(nvars - 5, N))
     fs.update(dict(nvars=nvars, nfvars=min(nvars, 5), ndims=3, neles=N, cell_ids=perm.astype(np.int32),
                    fspr=rng.uniform(0.5, 2.0, nF), tfspr=rng.uniform(0.5, 2.0, nF),
-                   dt=rng.uniform(1e-3, 1e-2, N), rhs=rng.standard_normal((nvars, N)), upts=upts,
+                   dt=rng.uniform(1e-3, 1e-2, N), rhs=rng.standard_normal((nvars, N)) * rhs_scale, upts=upts,
                    vol=mesh.vol.copy()))
     return fs
 
