@@ -97,6 +97,28 @@ UCFD_EXTERN ucfd_status_t UCFDFlowSysGetLevels(FlowSys sys, UCFDInt *nlevels);
 UCFD_EXTERN ucfd_status_t UCFDFlowSysSetPrecision(FlowSys sys, int precision);
 /* Launch shape of the sweep kernels (0 = autotuned default). */
 UCFD_EXTERN ucfd_status_t UCFDFlowSysSetLaunch(FlowSys sys, int threads_per_block);
+
+/* Launch choices of the sweeps.  None of them changes any result: every
+ * choice applies the same operations to each cell in the same order.
+ * No counterpart in the reference (its launch shape is the compile-time
+ * TPB/BLOCK macro of Makefile.inc). */
+typedef struct {
+    int threads_per_block; /* sweep kernels: 0 (default 256) or 32..256 step 32 */
+    int sweep_variant;     /* block sweep: 0 faces unrolled to the ELL width, 1 face loop */
+    int run_mode;          /* UCFDLUSGS_Run with mode -1: 0 CUDA graph, 1 persistent kernel */
+    double ms;             /* Autotune: time of the best candidate (one sweep pair, or one
+                              Run iteration for scalar LU-SGS); 0 when set by hand */
+} UCFDLaunchConfig;
+
+/* Times every launch candidate on the current system and keeps the fastest.
+ * Block LU-SGS (after Pack + NSPrepare): threads_per_block x sweep_variant
+ * on lower+upper sweep pairs into a scratch correction.  Scalar LU-SGS
+ * (after Pack; fspr set): threads_per_block x run_mode on the iteration of
+ * UCFDLUSGS_Run, the state saved before and restored after.  reps >= 1
+ * timed repetitions per candidate after one untimed one.  Synchronises. */
+UCFD_EXTERN ucfd_status_t UCFDFlowSysAutotune(FlowSys sys, int reps, UCFDLaunchConfig *best);
+UCFD_EXTERN ucfd_status_t UCFDFlowSysGetLaunchConfig(FlowSys sys, UCFDLaunchConfig *cfg);
+UCFD_EXTERN ucfd_status_t UCFDFlowSysSetLaunchConfig(FlowSys sys, const UCFDLaunchConfig *cfg);
 /* Run all kernels of a call on the caller's CUDA stream and return without
  * synchronising (stream == NULL restores the private stream and synchronous
  * calls).  Host-pointer arguments still synchronise. */
@@ -105,7 +127,8 @@ UCFD_EXTERN ucfd_status_t UCFDFlowSysSetStream(FlowSys sys, void *cuda_stream, i
 /* Scalar LU-SGS pseudo-time loop on device-resident state: niter times
  * { du = rhs; NS prepare; NS lower; NS upper; [RANS prepare/lower/upper];
  *   u += du }, launched as one CUDA graph (mode 0) or as one persistent
- * grid-synchronised kernel per sweep (mode 1).  Requires a prior Pack of
+ * grid-synchronised kernel per sweep (mode 1); mode -1 takes the run_mode
+ * of the launch configuration (UCFDFlowSysAutotune).  Requires a prior Pack of
  * every element.  resid (optional, [niter]) receives sqrt(sum du^2)
  * accumulated in FP64 after each iteration.  Update() afterwards writes
  * the final state back to the element arrays. */

@@ -1,0 +1,82 @@
+"""Launch autotuner (UCFDFlowSysAutotune): every candidate gives the same
+results, tuning leaves the system's state untouched, and the JSON cache
+round-trips."""
+import numpy as np
+import pytest
+
+from tests.golden import cases
+from tests.test_gpu_blusgs import host, make, run_sweeps
+from tests.test_gpu_lusgs import make_flowsys
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("prec", [0, 2])
+def test_blusgs_launch_choices_bit_identical(prec, ucfd):
+    """Block sizes 64/256 and both sweep variants give bit-identical
+    solutions (same operations in the same order per cell)."""
+    b = cases.blusgs_case(m=10, seed=2)
+    outs = []
+    for tpb in (64, 256):
+        for var in (0, 1):
+            S, e = make(b, prec=prec, on_device=True)
+            S.set_launch_config(threads_per_block=tpb, sweep_variant=var)
+            run_sweeps(S, 3)
+            outs.append(host(e["upts"]))
+    for o in outs[1:]:
+        np.testing.assert_array_equal(o, outs[0])
+
+
+def test_blusgs_autotune_keeps_golden(golden, ucfd):
+    """Autotune runs after Pack + NSPrepare; the sweeps that follow still
+    reproduce the golden FP64 result bit for bit."""
+    meta, arr = golden
+    kw = cases.BLUSGS["blu10"]
+    b = cases.blusgs_case(**kw)
+    S, e = make(b, on_device=True)
+    S.blusgs_pack(0, 0.0)
+    S.blusgs_ns_prepare()
+    cfg = S.autotune(reps=2)
+    assert cfg["threads_per_block"] in (64, 128, 192, 256)
+    assert cfg["sweep_variant"] in (0, 1) and cfg["ms"] > 0
+    assert S.launch_config()["threads_per_block"] == cfg["threads_per_block"]
+    run_sweeps(S, kw["nsweeps"])
+    np.testing.assert_array_equal(host(e["upts"]), arr["blu10_upts"])
+    np.testing.assert_array_equal(host(e["res"]), arr["blu10_resid"])
+
+
+def test_lusgs_autotune_restores_state(ucfd):
+    """Scalar autotune times the Run loop on the packed state and restores
+    it: Run(mode=-1) afterwards equals Run on an untuned system."""
+    fs, inp = cases.flowsys_case(**cases.FLOWSYS["fs9"])
+    S, e = make_flowsys(fs, inp, prec=2, on_device=True)
+    S.lusgs_pack(0, 1.0, 0.0)
+    cfg = S.autotune(reps=2)
+    assert cfg["run_mode"] in (0, 1) and cfg["ms"] > 0
+    r1 = np.zeros(4)
+    S.lusgs_run(4, 1.0, rans=False, mode=-1, resid=r1)
+    S.lusgs_update(0)
+    S2, e2 = make_flowsys(fs, inp, prec=2, on_device=True)
+    S2.lusgs_pack(0, 1.0, 0.0)
+    r2 = np.zeros(4)
+    S2.lusgs_run(4, 1.0, rans=False, mode=0, resid=r2)
+    S2.lusgs_update(0)
+    np.testing.assert_array_equal(e["upts"].cpu().numpy(), e2["upts"].cpu().numpy())
+    np.testing.assert_array_equal(r1, r2)
+
+
+def test_autotune_cache_round_trip(tmp_path, ucfd):
+    path = str(tmp_path / "tune.json")
+    b = cases.blusgs_case(m=8, seed=3)
+    S, e = make(b, prec=2, on_device=True)
+    S.blusgs_pack(0, 0.0)
+    S.blusgs_ns_prepare()
+    first = S.autotune(reps=1, cache=path)
+    assert first["source"] == "measured"
+    S2, e2 = make(b, prec=2, on_device=True)
+    S2.blusgs_pack(0, 0.0)
+    S2.blusgs_ns_prepare()
+    second = S2.autotune(reps=1, cache=path)
+    assert second["source"] == "cache"
+    for k in ("threads_per_block", "sweep_variant", "run_mode"):
+        assert second[k] == first[k]

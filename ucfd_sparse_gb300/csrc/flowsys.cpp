@@ -51,7 +51,10 @@ struct _FlowSys {
     std::vector<Elem> eles;
 
     int prec = UCFD_PREC_FP64;
-    int block = 0;
+    int block = 0;     // sweep threads per block (0: launcher default)
+    int variant = 0;   // block sweep: 0 unrolled faces, 1 face loop
+    int run_mode = 0;  // UCFDLUSGS_Run with mode -1
+    double tuned_ms = 0;
     cudaStream_t own = nullptr, user = nullptr;
     bool async = false;
 
@@ -327,7 +330,7 @@ void blusgs_sweep_into(FlowSys s, bool turb, bool upper, const S *rhs, S *du) {
         const int l = upper ? L - 1 - q : q;
         KCALL(EX, fs_blusgs_sweep<S>, B, s->sch.lev_off[l], s->sch.lev_off[l + 1], s->N, s->P, var0,
               s->d_nei.p, geo_fa<S>(s), geo_rv<S>(s), turb ? w.tJ.p : w.J.p, blu_LU<S>(s, turb), rhs, du,
-              s->block, s->stream());
+              s->block, s->variant, s->stream());
     }
 }
 
@@ -376,6 +379,98 @@ void lusgs_iteration(FlowSys s, bool rans, double kappa, double *resid_slot, boo
     const int v1 = rans ? s->nvars : s->nfvars;
     kfast::axpy_norm<S>((long long)v1 * s->N, w.du.p, w.u.p, s->part.p, resid_slot, st);
 }
+
+void run_graph_drop(FlowSys s) {
+    if (s->run_exec) cudaGraphExecDestroy(s->run_exec);
+    s->run_exec = nullptr;
+}
+
+// Spectral radii of the loop, gathered from the face arrays (fspr / tfspr)
+// into the ELL layout, and the scratch of the loop's norms.
+template <typename S>
+void run_gather_lambda(FlowSys s, bool rans, int niter) {
+    static thread_local DevBuf<double> stage;
+    cudaStream_t st = s->stream();
+    Work<S> &w = work<S>(s);
+    s->part.ensure(4096);
+    s->red.ensure(4);
+    s->resid.ensure((size_t)std::max(niter, 1));
+    w.lamN.ensure((size_t)s->P * s->N);
+    kfast::gather_idx<S>((long long)s->P * s->N, s->d_slot.p, device_view<double>(s->fspr, s->nfaces, stage, st),
+                         w.lamN.p, st);
+    if (rans) {
+        w.lamT.ensure((size_t)s->P * s->N);
+        kfast::gather_idx<S>((long long)s->P * s->N, s->d_slot.p, device_view<double>(s->tfspr, s->nfaces, stage, st),
+                             w.lamT.p, st);
+    }
+}
+
+// One iteration captured once per (rans, kappa, launch shape) and replayed.
+template <typename S, bool EX>
+void run_graph_build(FlowSys s, bool rans, double kappa) {
+    if (s->run_exec && s->run_rans == (int)rans && s->run_kappa == kappa) return;
+    run_graph_drop(s);
+    cudaStream_t st = s->stream();
+    UCFD_CUDA(cudaStreamSynchronize(st));
+    cudaGraph_t g;
+    UCFD_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    try {
+        lusgs_iteration<S, EX>(s, rans, kappa, s->red.p, false);
+    } catch (...) {
+        cudaStreamEndCapture(st, &g);
+        throw;
+    }
+    UCFD_CUDA(cudaStreamEndCapture(st, &g));
+    UCFD_CUDA(cudaGraphInstantiate(&s->run_exec, g, 0));
+    cudaGraphDestroy(g);
+    s->run_rans = rans;
+    s->run_kappa = kappa;
+}
+
+// Persistent sweeps: barrier state and timeout flag start cleared ...
+void run_persistent_begin(FlowSys s) {
+    cudaStream_t st = s->stream();
+    if (!s->d_lev_off.p) s->d_lev_off.upload(s->sch.lev_off.data(), s->sch.lev_off.size(), st);
+    s->d_bar.zero(2, st);
+    s->d_err.zero(1, st);
+}
+
+// ... and a barrier wait that gave up is reported after the launches.
+void run_persistent_check(FlowSys s) {
+    int err = 0;
+    UCFD_CUDA(cudaMemcpyAsync(&err, s->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, s->stream()));
+    UCFD_CUDA(cudaStreamSynchronize(s->stream()));
+    if (err) fail(UCFD_ERR_TIMEOUT, "persistent sweep: a grid barrier wait timed out");
+}
+
+// Mean device time (ms) of fn over reps calls after one untimed call.
+struct EventPair {
+    cudaEvent_t a = nullptr, b = nullptr;
+    EventPair() {
+        UCFD_CUDA(cudaEventCreate(&a));
+        UCFD_CUDA(cudaEventCreate(&b));
+    }
+    ~EventPair() {
+        if (a) cudaEventDestroy(a);
+        if (b) cudaEventDestroy(b);
+    }
+};
+
+template <typename F>
+double time_ms(cudaStream_t st, int reps, F &&fn) {
+    fn();
+    EventPair ev;
+    UCFD_CUDA(cudaEventRecord(ev.a, st));
+    for (int r = 0; r < reps; ++r) fn();
+    UCFD_CUDA(cudaEventRecord(ev.b, st));
+    UCFD_CUDA(cudaEventSynchronize(ev.b));
+    UCFD_CHECK_LAUNCH();
+    float ms = 0.f;
+    UCFD_CUDA(cudaEventElapsedTime(&ms, ev.a, ev.b));
+    return (double)ms / reps;
+}
+
+constexpr int kTuneBlocks[] = {64, 128, 192, 256};
 
 }  // namespace
 
@@ -503,9 +598,140 @@ ucfd_status_t UCFDFlowSysSetLaunch(FlowSys s, int threads_per_block) {
     UCFD_REQUIRE(threads_per_block == 0 || (threads_per_block % 32 == 0 && threads_per_block <= 256),
                  "threads_per_block must be 0 or a multiple of 32 up to 256");
     s->block = threads_per_block;
-    if (s->run_exec) {
-        cudaGraphExecDestroy(s->run_exec);
-        s->run_exec = nullptr;
+    run_graph_drop(s);
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDFlowSysGetLaunchConfig(FlowSys s, UCFDLaunchConfig *cfg) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(s && cfg, "null argument");
+    cfg->threads_per_block = s->block;
+    cfg->sweep_variant = s->variant;
+    cfg->run_mode = s->run_mode;
+    cfg->ms = s->tuned_ms;
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDFlowSysSetLaunchConfig(FlowSys s, const UCFDLaunchConfig *cfg) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(s && cfg, "null argument");
+    const int b = cfg->threads_per_block;
+    UCFD_REQUIRE(b == 0 || (b % 32 == 0 && b >= 32 && b <= 256),
+                 "threads_per_block must be 0 or a multiple of 32 up to 256 (got %d)", b);
+    UCFD_REQUIRE(cfg->sweep_variant == 0 || cfg->sweep_variant == 1, "sweep_variant must be 0 or 1");
+    UCFD_REQUIRE(cfg->run_mode == 0 || cfg->run_mode == 1, "run_mode must be 0 or 1");
+    if (b != s->block) run_graph_drop(s);
+    s->block = b;
+    s->variant = cfg->sweep_variant;
+    s->run_mode = cfg->run_mode;
+    s->tuned_ms = 0;
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDFlowSysAutotune(FlowSys s, int reps, UCFDLaunchConfig *best) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(s, "null FlowSys handle");
+    UCFD_REQUIRE(reps >= 1 && reps <= 1000, "reps must be in [1, 1000]");
+    UCFD_REQUIRE(s->mode == MODE_LUSGS || s->mode == MODE_BLUSGS, "Autotune needs SetLUSGS or SetBLUSGS first");
+    build_topology(s);
+    cudaStream_t st = s->stream();
+    UCFD_CUDA(cudaStreamSynchronize(st));
+    double best_ms = -1;
+    int best_block = s->block, best_var = s->variant, best_mode = s->run_mode;
+    // a failed candidate leaves the launch configuration as it was
+    struct Keep {
+        FlowSys s;
+        int b, v;
+        bool done = false;
+        ~Keep() {
+            if (!done) {
+                s->block = b;
+                s->variant = v;
+                run_graph_drop(s);
+            }
+        }
+    } keep{s, s->block, s->variant};
+    auto consider = [&](double ms, int b, int v, int m) {
+        if (best_ms < 0 || ms < best_ms) {
+            best_ms = ms;
+            best_block = b;
+            best_var = v;
+            best_mode = m;
+        }
+    };
+    const size_t n = (size_t)s->nvars * s->N;
+    if (s->mode == MODE_BLUSGS) {
+        dispatch(s, [&]<typename S, bool EX>() {
+            Work<S> &w = work<S>(s);
+            UCFD_REQUIRE(w.rhs.p && w.J.p && blu_LU<S>(s, false), "Autotune before Pack and NSPrepare");
+            DevBuf<S> scratch;
+            scratch.zero(n, st);
+            // the unrolled kernel exists for ELL widths 6 and 4 only
+            const int nvar = (s->P == 6 || s->P == 4) ? 2 : 1;
+            for (int v = 0; v < nvar; ++v)
+                for (int b : kTuneBlocks) {
+                    s->block = b;
+                    s->variant = v;
+                    const double ms = time_ms(st, reps, [&] {
+                        blusgs_sweep_into<S, EX>(s, false, false, w.rhs.p, scratch.p);
+                        blusgs_sweep_into<S, EX>(s, false, true, w.rhs.p, scratch.p);
+                    });
+                    consider(ms, b, v, s->run_mode);
+                }
+        });
+    } else {
+        UCFD_REQUIRE(s->fspr, "fspr is not set");
+        dispatch(s, [&]<typename S, bool EX>() {
+            Work<S> &w = work<S>(s);
+            UCFD_REQUIRE(w.u.p, "Autotune before Pack");
+            // the loop writes u, du, diag and the spectral radii: keep them
+            DevBuf<S> su, sdu, sdiag, slam;
+            const size_t nl = (size_t)s->P * s->N;
+            const bool had_lam = w.lamN.p != nullptr;
+            su.ensure(n);
+            sdu.ensure(n);
+            sdiag.ensure(n);
+            UCFD_CUDA(cudaMemcpyAsync(su.p, w.u.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
+            UCFD_CUDA(cudaMemcpyAsync(sdu.p, w.du.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
+            UCFD_CUDA(cudaMemcpyAsync(sdiag.p, w.diag.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
+            if (had_lam) {
+                slam.ensure(nl);
+                UCFD_CUDA(cudaMemcpyAsync(slam.p, w.lamN.p, nl * sizeof(S), cudaMemcpyDeviceToDevice, st));
+            }
+            run_gather_lambda<S>(s, false, 1);
+            for (int b : kTuneBlocks) {
+                s->block = b;
+                run_graph_drop(s);
+                run_graph_build<S, EX>(s, false, 1.0);
+                const double ms = time_ms(st, reps, [&] { UCFD_CUDA(cudaGraphLaunch(s->run_exec, st)); });
+                consider(ms, b, s->variant, 0);
+            }
+            run_graph_drop(s);
+            // the persistent kernel has its own fixed launch shape
+            run_persistent_begin(s);
+            const double pms =
+                time_ms(st, reps, [&] { lusgs_iteration<S, EX>(s, false, 1.0, s->red.p, true); });
+            run_persistent_check(s);
+            consider(pms, best_block, s->variant, 1);
+            UCFD_CUDA(cudaMemcpyAsync(w.u.p, su.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
+            UCFD_CUDA(cudaMemcpyAsync(w.du.p, sdu.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
+            UCFD_CUDA(cudaMemcpyAsync(w.diag.p, sdiag.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
+            if (had_lam) UCFD_CUDA(cudaMemcpyAsync(w.lamN.p, slam.p, nl * sizeof(S), cudaMemcpyDeviceToDevice, st));
+            UCFD_CUDA(cudaStreamSynchronize(st));
+            if (!had_lam) w.lamN.release();
+        });
+    }
+    keep.done = true;
+    s->block = best_block;
+    s->variant = best_var;
+    s->run_mode = best_mode;
+    s->tuned_ms = best_ms;
+    run_graph_drop(s);
+    if (best) {
+        best->threads_per_block = best_block;
+        best->sweep_variant = best_var;
+        best->run_mode = best_mode;
+        best->ms = best_ms;
     }
     UCFD_API_END
 }
@@ -631,65 +857,29 @@ ucfd_status_t UCFDLUSGS_Run(FlowSys s, UCFDInt niter, UCFDReal kappa, int rans, 
     need_mode(s, MODE_LUSGS);
     build_topology(s);
     UCFD_REQUIRE(niter >= 0, "niter must be >= 0");
-    UCFD_REQUIRE(mode == 0 || mode == 1, "mode must be 0 (graph) or 1 (persistent)");
+    UCFD_REQUIRE(mode == -1 || mode == 0 || mode == 1,
+                 "mode must be 0 (graph), 1 (persistent) or -1 (launch configuration)");
+    if (mode == -1) mode = s->run_mode;
     if (rans) UCFD_REQUIRE(s->ntvars > 0 && s->tfspr, "RANS loop needs turbulence variables and tfspr");
     cudaStream_t st = s->stream();
-    // spectral radii for the loop
-    static thread_local DevBuf<double> stage;
-    s->part.ensure(4096);
-    s->red.ensure(4);
-    s->resid.ensure((size_t)std::max(niter, 1));
     dispatch(s, [&]<typename S, bool EX>() {
         Work<S> &w = work<S>(s);
         UCFD_REQUIRE(w.u.p, "Run before Pack");
-        w.lamN.ensure((size_t)s->P * s->N);
-        kfast::gather_idx<S>((long long)s->P * s->N, s->d_slot.p, device_view<double>(s->fspr, s->nfaces, stage, st),
-                             w.lamN.p, st);
-        if (rans) {
-            w.lamT.ensure((size_t)s->P * s->N);
-            kfast::gather_idx<S>((long long)s->P * s->N, s->d_slot.p,
-                                 device_view<double>(s->tfspr, s->nfaces, stage, st), w.lamT.p, st);
-        }
+        run_gather_lambda<S>(s, rans, niter);
         if (mode == 0) {
-            // one iteration captured once per (rans, kappa) and replayed
-            if (!s->run_exec || s->run_rans != rans || s->run_kappa != kappa) {
-                if (s->run_exec) cudaGraphExecDestroy(s->run_exec);
-                s->run_exec = nullptr;
-                UCFD_CUDA(cudaStreamSynchronize(st));
-                cudaGraph_t g;
-                UCFD_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-                try {
-                    lusgs_iteration<S, EX>(s, rans, kappa, s->red.p, false);
-                } catch (...) {
-                    cudaStreamEndCapture(st, &g);
-                    throw;
-                }
-                UCFD_CUDA(cudaStreamEndCapture(st, &g));
-                UCFD_CUDA(cudaGraphInstantiate(&s->run_exec, g, 0));
-                cudaGraphDestroy(g);
-                s->run_rans = rans;
-                s->run_kappa = kappa;
-            }
+            run_graph_build<S, EX>(s, rans, kappa);
             for (int it = 0; it < niter; ++it) {
                 UCFD_CUDA(cudaGraphLaunch(s->run_exec, st));
                 UCFD_CUDA(cudaMemcpyAsync(s->resid.p + it, s->red.p, sizeof(double), cudaMemcpyDeviceToDevice, st));
             }
         } else {
-            // persistent sweeps: barrier state and timeout flag start cleared
-            if (!s->d_lev_off.p) s->d_lev_off.upload(s->sch.lev_off.data(), s->sch.lev_off.size(), st);
-            s->d_bar.zero(2, st);
-            s->d_err.zero(1, st);
+            run_persistent_begin(s);
             for (int it = 0; it < niter; ++it) lusgs_iteration<S, EX>(s, rans, kappa, s->resid.p + it, true);
         }
     });
     if (resid && niter > 0)
         UCFD_CUDA(cudaMemcpyAsync(resid, s->resid.p, niter * sizeof(double), cudaMemcpyDefault, st));
-    if (mode == 1) {
-        int err = 0;
-        UCFD_CUDA(cudaMemcpyAsync(&err, s->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, st));
-        UCFD_CUDA(cudaStreamSynchronize(st));
-        if (err) fail(UCFD_ERR_TIMEOUT, "persistent sweep: a grid barrier wait timed out");
-    }
+    if (mode == 1) run_persistent_check(s);
     s->run_state = true;
     finish(s, resid != nullptr);
     UCFD_API_END

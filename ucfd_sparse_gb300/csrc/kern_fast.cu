@@ -24,7 +24,7 @@ namespace kfast {
                                        const int8_t *, const double *, const double *, const double *,         \
                                        const double *, double *, double *, T *, T *, double *, cudaStream_t);  \
     template void fs_blusgs_sweep<T>(int, int, int, long long, int, int, const int *, const T *, const T *,    \
-                                     const T *, const T *, const T *, T *, int, cudaStream_t);                 \
+                                     const T *, const T *, const T *, T *, int, int, cudaStream_t);            \
     template void fs_blusgs_residual<T, T>(int, long long, int, int, int, const int *, const double *,         \
                                            const double *, const double *, const double *, const double *,     \
                                            const T *, T *, double *, int, int *, cudaStream_t);                \

@@ -224,11 +224,17 @@ void fs_blusgs_prepare(int B, long long N, int P, long long nF, const int *nei, 
 template <typename S>
 void fs_blusgs_sweep(int B, int t0, int t1, long long N, int P, int var0, const int *nei, const S *fa,
                      const S *rv, const S *J, const S *LU, const S *rhs, S *du, int block,
-                     cudaStream_t s) {
+                     int variant, cudaStream_t s) {
     if (t1 <= t0) return;
     if (block <= 0) block = kBlock;
     const unsigned g = grid_for(t1 - t0, block);
-    if (P == 6) {
+    // variant 0: faces unrolled to the ELL width (6 or 4) when it matches;
+    // variant 1: the face loop that stops at the first padding slot.
+    // Both apply the faces in the same order with the same operations.
+    if (variant == 1) {
+        UCFD_BSW(B, (fs_blusgs_sweep_kernel<S, BB, 0><<<g, block, 0, s>>>(t0, t1, N, P, var0, nei, fa, rv, J, LU,
+                                                                          rhs, du)));
+    } else if (P == 6) {
         UCFD_BSW(B, (fs_blusgs_sweep_kernel<S, BB, 6><<<g, block, 0, s>>>(t0, t1, N, P, var0, nei, fa, rv, J, LU,
                                                                           rhs, du)));
     } else if (P == 4) {

@@ -10,7 +10,7 @@ from __future__ import annotations
 
 from ctypes import byref, c_double, c_int, c_void_p
 
-from .lib import PREC_FP32, PREC_FP64, PREC_FP64_FMA, call, load, ptr
+from .lib import PREC_FP32, PREC_FP64, PREC_FP64_FMA, LaunchConfig, call, load, ptr
 
 __all__ = ["FlowSys", "PREC_FP64", "PREC_FP64_FMA", "PREC_FP32"]
 
@@ -24,6 +24,9 @@ class FlowSys:
         call("UCFDFlowSysCreate", byref(self._h), nlocal, nvars, nfvars, ndims, nfaces, nelem, ptr(rowptr),
              ptr(colidx), ptr(slots), ptr(sides), ptr(face_area), ptr(face_normal), ptr(rcp_vol))
         self.nlocal, self.nvars, self.nfvars, self.ndims = nlocal, nvars, nfvars, ndims
+        self.nfaces = nfaces
+        self.precision = PREC_FP64
+        self.kind = None
 
     @classmethod
     def from_dict(cls, fs: dict, nelem: int = 1):
@@ -64,15 +67,33 @@ class FlowSys:
 
     def set_precision(self, prec: int):
         call("UCFDFlowSysSetPrecision", self._h, prec)
+        self.precision = prec
 
     def set_launch(self, threads: int):
         call("UCFDFlowSysSetLaunch", self._h, threads)
+
+    def launch_config(self) -> dict:
+        cfg = LaunchConfig()
+        call("UCFDFlowSysGetLaunchConfig", self._h, byref(cfg))
+        return cfg.as_dict()
+
+    def set_launch_config(self, threads_per_block=0, sweep_variant=0, run_mode=0, **_ignored):
+        cfg = LaunchConfig(threads_per_block, sweep_variant, run_mode, 0.0)
+        call("UCFDFlowSysSetLaunchConfig", self._h, byref(cfg))
+
+    def autotune(self, reps: int = 5, cache: str | bool | None = None) -> dict:
+        """Times the launch candidates (``UCFDFlowSysAutotune``) and keeps the
+        fastest.  With ``cache`` (a path, or True for the default file) the
+        choice is looked up in / stored to the JSON cache of ``autotune.py``."""
+        from . import autotune as _at
+        return _at.tune(self, reps=reps, cache=cache)
 
     def set_stream(self, stream_ptr: int | None, asynchronous: bool = False):
         call("UCFDFlowSysSetStream", self._h, stream_ptr, 1 if asynchronous else 0)
 
     # ---- scalar LU-SGS -------------------------------------------------------
     def set_lusgs(self, fspr, tfspr=None):
+        self.kind = "lusgs"
         self._keep += [fspr, tfspr]
         call("UCFDFlowSysSetLUSGS", byref(self._h), ptr(fspr), ptr(tfspr))
 
@@ -105,6 +126,7 @@ class FlowSys:
 
     # ---- block LU-SGS -------------------------------------------------------
     def set_blusgs(self, jmat, tjmat=None):
+        self.kind = "blusgs"
         self._keep += [jmat, tjmat]
         call("UCFDFlowSysSetBLUSGS", byref(self._h), ptr(jmat), ptr(tjmat))
 

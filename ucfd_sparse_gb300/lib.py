@@ -20,6 +20,17 @@ LIB_PATH = os.path.join(HERE, "lib", "libucfd_gb300.so")
 
 _I, _D, _P = c_int, c_double, c_void_p
 
+
+class LaunchConfig(ctypes.Structure):
+    """``UCFDLaunchConfig`` of ucfdlusgs.h."""
+
+    _fields_ = [("threads_per_block", c_int), ("sweep_variant", c_int), ("run_mode", c_int), ("ms", c_double)]
+
+    def as_dict(self) -> dict:
+        return {"threads_per_block": self.threads_per_block, "sweep_variant": self.sweep_variant,
+                "run_mode": self.run_mode, "ms": self.ms}
+
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     # ucfd_gb300.h
@@ -63,6 +74,9 @@ SIGNATURES = {
     "UCFDFlowSysGetLevels": (_I, [_P, POINTER(c_int)]),
     "UCFDFlowSysSetPrecision": (_I, [_P, _I]),
     "UCFDFlowSysSetLaunch": (_I, [_P, _I]),
+    "UCFDFlowSysAutotune": (_I, [_P, _I, POINTER(LaunchConfig)]),
+    "UCFDFlowSysGetLaunchConfig": (_I, [_P, POINTER(LaunchConfig)]),
+    "UCFDFlowSysSetLaunchConfig": (_I, [_P, POINTER(LaunchConfig)]),
     "UCFDFlowSysSetStream": (_I, [_P, _P, _I]),
     "UCFDLUSGS_Run": (_I, [_P, _I, _D, _I, _I, _P]),
     "UCFDBLUSGS_Solve": (_I, [_P, _D, _I, _I, POINTER(c_int), POINTER(c_double)]),
