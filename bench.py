@@ -653,6 +653,74 @@ def run_colored(args):
     print(json.dumps(out))
 
 
+def run_kernels(args):
+    """The BLU-SGS pieces of one pseudo-time step timed one by one on a
+    single FP32 system (device-resident inputs): Pack + NSPrepare, one
+    lower+upper sweep pair over all colours, and the FP64 true residual.
+    Small meshes of this workload are the ncu capture cases."""
+    import torch
+
+    from ucfd_sparse_gb300 import _build, lib
+    from ucfd_sparse_gb300 import coloredlusgs as cl
+    _build.build()
+    lib.load()
+    case = make_case(args.mesh, seed=args.seed)
+    N = case["nlocal"]
+    ic, rg, lc = cl.greedy_coloring_csr(case["rowptr"], case["colidx"])
+    device = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(device=device)
+    P = Problem(case, lc, 2, stream, device)
+    S = P.S
+    tuned = P.tune() if not args.no_autotune else None
+    S.blusgs_reset()
+
+    def timed(fn, reps):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = _events(stream)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    def prep():
+        S.blusgs_pack(0, 0.0)
+        S.blusgs_ns_prepare()
+
+    def pair():
+        S.blusgs_ns_lower()
+        S.blusgs_ns_upper()
+
+    reps = max(args.steps, 3)
+    prep_ms = timed(prep, reps)
+    pair_ms = timed(pair, 4 * reps)
+    S.blusgs_solve(0.0, 1, 1)                    # one refinement step: x (FP64) != 0 from here on
+    res_ms = timed(S.blusgs_residual, reps)      # includes its host read-back
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    nnz = int(case["rowptr"][-1])
+    nF = int(case["nfaces"])
+    sw = 2 * sweep_bytes(case["rowptr"], 4, 5, 4)
+    # Prepare: jmat read twice (transpose in, face records out) + written once,
+    # face records read per cell-face, J32/J64/D/LU32 written, ELL index arrays
+    prep_b = nF * 400 * 3 + nnz * (400 + 100 + 200 + 4 + 4 + 1 + 8) + N * (200 + 100 + 8 + 8)
+    res_b = nnz * (4 + 8 + 200) + N * (8 + 200 + 40 + 40 + 20)
+    out = {"workload": "kernels", "unit": "ms", "config": {
+        "workload": f"BLU-SGS 5x5 FP32 pieces, {args.mesh}^3 jittered permuted hex ({N} cells, {nF} faces), "
+                    f"{len(rg)} colours", "cells": N, "colors": len(rg)},
+        "launch": tuned,
+        "prepare": {"ms": prep_ms, "GBps": prep_b / (prep_ms * 1e-3) / 1e9, "bytes": prep_b},
+        "sweep_pair": {"ms": pair_ms, "GBps": sw / (pair_ms * 1e-3) / 1e9, "frac": sw / (pair_ms * 1e-3) / 1e9 / peak,
+                       "bytes": sw},
+        "residual_fp64": {"ms": res_ms, "GBps": res_b / (res_ms * 1e-3) / 1e9, "bytes": res_b},
+        "peak": peak}
+    print(json.dumps(out))
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -667,7 +735,7 @@ def main(argv=None):
     ap.add_argument("--max-pairs", type=int, default=400)
     ap.add_argument("--ref-pairs", type=int, default=1)
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")
-    ap.add_argument("--workload", default="blusgs", choices=["blusgs", "lusgs", "gmres", "colored"],
+    ap.add_argument("--workload", default="blusgs", choices=["blusgs", "lusgs", "gmres", "colored", "kernels"],
                     help="blusgs: the headline line; the others measure the remaining configurations")
     ap.add_argument("--iters", type=int, default=200, help="iterations of the lusgs/colored workloads")
     args = ap.parse_args(argv)
@@ -681,6 +749,8 @@ def main(argv=None):
         run_gmres(args)
     elif args.workload == "colored":
         run_colored(args)
+    elif args.workload == "kernels":
+        run_kernels(args)
     else:
         run_gpu(args)
 

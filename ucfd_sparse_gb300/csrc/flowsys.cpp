@@ -73,7 +73,9 @@ struct _FlowSys {
     Work<double> w64;
     Work<float> w32;
     DevBuf<double> D, dd, LU64, tD, tLU64, J64, rhs64, x64;  // FP64 block arrays
+    DevBuf<double> jt;  // Prepare scratch: face Jacobians, one record per face
     bool du64_valid = false;
+    bool x_zero = false;  // the correction du is all zeros (Reset, no sweep since)
     DevBuf<double> part, red, resid;
     PinnedBuf<double> h_red;
 
@@ -973,8 +975,9 @@ static ucfd_status_t blusgs_prepare_api(FlowSys s, bool turb) {
             LU64 = nullptr;
             if (!turb) J64 = s->J64.ensure((size_t)s->P * B * B * s->N);
         }
+        double *jt = s->jt.ensure((size_t)2 * B * B * s->nfaces);
         KCALL(EX, fs_blusgs_prepare<S>, B, s->N, s->P, (long long)s->nfaces, s->d_nei.p, s->d_slot.p, s->d_side.p,
-              s->fa64.p, s->rv64.p, jd, dd, D, LU64, LU_s, turb ? w.tJ.p : w.J.p, J64, st);
+              s->fa64.p, s->rv64.p, jd, dd, D, LU64, LU_s, turb ? w.tJ.p : w.J.p, J64, jt, st);
     });
     finish(s, !is_device_ptr(jm));
     UCFD_API_END
@@ -994,6 +997,7 @@ static ucfd_status_t blusgs_sweep_api(FlowSys s, bool turb, bool upper) {
         blusgs_sweep_into<S, EX>(s, turb, upper, w.rhs.p, w.bdu.p);
     });
     s->du64_valid = false;
+    s->x_zero = false;
     finish(s);
     UCFD_API_END
 }
@@ -1017,6 +1021,7 @@ ucfd_status_t UCFDBLUSGS_Reset(FlowSys s) {
         if (std::is_same<S, float>::value) s->x64.zero(n, st);
     });
     s->du64_valid = false;
+    s->x_zero = true;
     finish(s);
     UCFD_API_END
 }
@@ -1077,12 +1082,12 @@ ucfd_status_t UCFDBLUSGS_Residual(FlowSys s, UCFDReal *relres) {
     if (s->prec == UCFD_PREC_FP32) {
         UCFD_REQUIRE(s->J64.p, "Residual before NSPrepare");
         if (s->du64_valid)
-            blusgs_residual<double, double, false>(s, s->x64.p, (double *)nullptr, &rn, &bn);
+            blusgs_residual<double, double, false>(s, s->x_zero ? nullptr : s->x64.p, (double *)nullptr, &rn, &bn);
         else
-            blusgs_residual<float, float, false>(s, s->w32.bdu.p, (float *)nullptr, &rn, &bn);
+            blusgs_residual<float, float, false>(s, s->x_zero ? nullptr : s->w32.bdu.p, (float *)nullptr, &rn, &bn);
     } else {
         UCFD_REQUIRE(s->w64.J.p, "Residual before NSPrepare");
-        blusgs_residual<double, double, false>(s, s->w64.bdu.p, (double *)nullptr, &rn, &bn);
+        blusgs_residual<double, double, false>(s, s->x_zero ? nullptr : s->w64.bdu.p, (double *)nullptr, &rn, &bn);
     }
     *relres = bn > 0 ? rn / bn : rn;
     UCFD_API_END
@@ -1104,7 +1109,7 @@ ucfd_status_t UCFDBLUSGS_Solve(FlowSys s, UCFDReal rtol, UCFDInt max_sweeps, UCF
         w.r.ensure(n);
         w.delta.ensure(n);
         if (!s->du64_valid) kfast::convert<float, double>((long long)n, w.bdu.p, s->x64.p, st);
-        blusgs_residual<double, float, false>(s, s->x64.p, w.r.p, &rn, &bn);
+        blusgs_residual<double, float, false>(s, s->x_zero ? nullptr : s->x64.p, w.r.p, &rn, &bn);
         rel = bn > 0 ? rn / bn : rn;
         while (rel > rtol && pairs < max_sweeps) {
             w.delta.zero(n, st);
@@ -1125,7 +1130,7 @@ ucfd_status_t UCFDBLUSGS_Solve(FlowSys s, UCFDReal rtol, UCFDInt max_sweeps, UCF
         Work<double> &w = s->w64;
         UCFD_REQUIRE(w.J.p, "Solve before NSPrepare");
         const bool ex = s->prec == UCFD_PREC_FP64;
-        blusgs_residual<double, double, false>(s, w.bdu.p, (double *)nullptr, &rn, &bn);
+        blusgs_residual<double, double, false>(s, s->x_zero ? nullptr : w.bdu.p, (double *)nullptr, &rn, &bn);
         rel = bn > 0 ? rn / bn : rn;
         while (rel > rtol && pairs < max_sweeps) {
             const int m = std::min(inner_sweeps, max_sweeps - pairs);
@@ -1144,6 +1149,7 @@ ucfd_status_t UCFDBLUSGS_Solve(FlowSys s, UCFDReal rtol, UCFDInt max_sweeps, UCF
             UCFD_CHECK_LAUNCH();
         }
     }
+    if (pairs > 0) s->x_zero = false;
     if (nsweeps) *nsweeps = pairs;
     if (relres) *relres = rel;
     finish(s, true);

@@ -20,7 +20,7 @@ template void fs_blusgs_pack<double>(int, int, int, long long, double, const int
                                      const double *, double *, double *, double *, cudaStream_t);
 template void fs_blusgs_prepare<double>(int, long long, int, long long, const int *, const int *, const int8_t *,
                                         const double *, const double *, const double *, const double *, double *,
-                                        double *, double *, double *, double *, cudaStream_t);
+                                        double *, double *, double *, double *, double *, cudaStream_t);
 template void fs_blusgs_sweep<double>(int, int, int, long long, int, int, const int *, const double *, const double *,
                                       const double *, const double *, const double *, double *, int, int,
                                       cudaStream_t);

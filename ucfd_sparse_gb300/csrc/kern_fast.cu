@@ -22,7 +22,8 @@ namespace kfast {
                                     const double *, const double *, T *, double *, double *, cudaStream_t);    \
     template void fs_blusgs_prepare<T>(int, long long, int, long long, const int *, const int *,               \
                                        const int8_t *, const double *, const double *, const double *,         \
-                                       const double *, double *, double *, T *, T *, double *, cudaStream_t);  \
+                                       const double *, double *, double *, T *, T *, double *, double *,       \
+                                       cudaStream_t);                                                          \
     template void fs_blusgs_sweep<T>(int, int, int, long long, int, int, const int *, const T *, const T *,    \
                                      const T *, const T *, const T *, T *, int, int, cudaStream_t);            \
     template void fs_blusgs_residual<T, T>(int, long long, int, int, int, const int *, const double *,         \

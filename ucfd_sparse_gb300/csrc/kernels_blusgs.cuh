@@ -107,17 +107,42 @@ __global__ void fs_tblusgs_pack_kernel(int model, int neles, int nvars, int nt, 
     for (int e = 0; e < nt * nt; ++e) D[e * N + k] = A[e];
 }
 
+// Face Jacobians from the caller's layout jmat[2][B][B][nF] (face index
+// fastest) to one contiguous record per face, jt[f][2*B*B], through a
+// shared-memory tile: both the reads and the writes are coalesced.  The
+// prepare kernel then reads a cell-face's two blocks as 2*B*B*8 contiguous
+// bytes instead of 2*B*B separate 8-byte words nF apart.
+template <int B>
+__global__ void __launch_bounds__(256) jmat_face_major_kernel(long long nF, const double *__restrict__ jmat,
+                                                              double *__restrict__ jt) {
+    constexpr int R = 2 * B * B;
+    constexpr int FT = 32;         // faces per tile
+    constexpr int LD = R + 1;      // padded row: fewer shared-memory bank conflicts
+    __shared__ double tile[FT * LD];
+    const long long f0 = (long long)blockIdx.x * FT;
+    const int nf = (int)(nF - f0 < FT ? nF - f0 : FT);
+    for (int q = threadIdx.x; q < R * FT; q += blockDim.x) {
+        const int e = q / FT, j = q % FT;
+        if (j < nf) tile[j * LD + e] = __ldg(jmat + (long long)e * nF + f0 + j);
+    }
+    __syncthreads();
+    double *out = jt + f0 * R;
+    for (int q = threadIdx.x; q < nf * R; q += blockDim.x) out[q] = tile[(q / R) * LD + q % R];
+}
+
 // pre_blusgs: blusgs.c:200-246, plus the gather of each cell-face's
 // off-diagonal block (the half the sweeps use) into the ELL layout.
 // The block starts from dd[k] I when dd is given (NS pack), else from D.
+// jt holds the face-major records written by jmat_face_major_kernel.
 template <typename S, int B>
-__global__ void fs_blusgs_prepare_kernel(long long N, int P, long long nF, const int *nei,
-                                         const int *slot, const int8_t *side, const double *fa,
-                                         const double *rv, const double *jmat, const double *dd,
-                                         double *D, double *LU64, S *LU_s, S *J_s, double *J64) {
+__global__ void fs_blusgs_prepare_kernel(long long N, int P, const int *nei, const int *slot,
+                                         const int8_t *side, const double *fa, const double *rv,
+                                         const double *jt, const double *dd, double *D, double *LU64,
+                                         S *LU_s, S *J_s, double *J64) {
     const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (k >= N) return;
     constexpr int B2 = B * B;
+    constexpr int R = 2 * B2;  // even: a record is a whole number of 16-byte pairs
     double dm[B2];
     if (dd) {
         const double d = dd[k];
@@ -132,12 +157,19 @@ __global__ void fs_blusgs_prepare_kernel(long long N, int P, long long nF, const
         const long long s = slot[p * N + k];
         const int sd = side[p * N + k];
         const double fv = fa[p * N + k] * rv[k];
+        double h[R];
+        const double2 *rec = reinterpret_cast<const double2 *>(jt + s * R);
+#pragma unroll
+        for (int q = 0; q < R / 2; ++q) {
+            const double2 v = __ldg(rec + q);
+            h[2 * q] = v.x;
+            h[2 * q + 1] = v.y;
+        }
 #pragma unroll
         for (int r = 0; r < B; ++r) {
 #pragma unroll
             for (int c = 0; c < B; ++c) {
-                const long long o = s + c * nF + (long long)r * nF * B;
-                const double h0 = jmat[o], h1 = jmat[o + B2 * nF];
+                const double h0 = h[r * B + c], h1 = h[B2 + r * B + c];
                 const double val = (sd == 1) ? h0 : -h1;
                 dm[c + r * B] += val * fv;
                 const double jv = (sd == 1) ? h1 : -h0;
@@ -249,20 +281,23 @@ __global__ void fs_blusgs_residual_kernel(long long N, int P, int var0, int nvar
         constexpr int B2 = B * B;
         double res[B];
         double xk[B];
+        // x == nullptr: x is known to be zero, r = rhs (no matrix reads)
 #pragma unroll
-        for (int c = 0; c < B; ++c) xk[c] = (double)x[(var0 + c) * N + k];
+        for (int c = 0; c < B; ++c) xk[c] = x ? (double)x[(var0 + c) * N + k] : 0.0;
 #pragma unroll
         for (int r = 0; r < B; ++r) {
             double v = rhs64[(var0 + r) * N + k];
             bb += v * v;
+            if (x) {
 #pragma unroll
-            for (int c = 0; c < B; ++c) v -= D[(r * B + c) * N + k] * xk[c];
+                for (int c = 0; c < B; ++c) v -= D[(r * B + c) * N + k] * xk[c];
+            }
             res[r] = v;
         }
         // fixed trip count (6 = hex ELL width) so all gathers are issued
         // up front; padding entries contribute nothing
         constexpr int PU = 6;
-        for (int p0 = 0; p0 < P; p0 += PU) {
+        for (int p0 = 0; x && p0 < P; p0 += PU) {
             int nbv[PU];
             double xn[PU][B];
 #pragma unroll

@@ -55,7 +55,8 @@
     void fs_blusgs_prepare(int B, long long N, int P, long long nF, const int *nei,               \
                            const int *slot, const int8_t *side, const double *fa,                  \
                            const double *rv, const double *jmat, const double *dd, double *D,      \
-                           double *LU64, S *LU_s, S *J_s, double *J64, cudaStream_t s);            \
+                           double *LU64, S *LU_s, S *J_s, double *J64, double *jt,                 \
+                           cudaStream_t s);                                                        \
     template <typename S>                                                                          \
     void fs_blusgs_sweep(int B, int t0, int t1, long long N, int P, int var0, const int *nei,      \
                          const S *fa, const S *rv, const S *J, const S *LU, const S *rhs, S *du,   \

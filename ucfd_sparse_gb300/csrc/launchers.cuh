@@ -215,10 +215,12 @@ template <typename S>
 void fs_blusgs_prepare(int B, long long N, int P, long long nF, const int *nei, const int *slot,
                        const int8_t *side, const double *fa, const double *rv, const double *jmat,
                        const double *dd, double *D, double *LU64, S *LU_s, S *J_s, double *J64,
-                       cudaStream_t s) {
+                       double *jt, cudaStream_t s) {
     if (N <= 0) return;
+    const unsigned gt = (unsigned)((nF + 31) / 32);
+    UCFD_BSW(B, (jmat_face_major_kernel<BB><<<gt, 256, 0, s>>>(nF, jmat, jt)));
     UCFD_BSW(B, (fs_blusgs_prepare_kernel<S, BB><<<grid_for(N, 128), 128, 0, s>>>(
-                    N, P, nF, nei, slot, side, fa, rv, jmat, dd, D, LU64, LU_s, J_s, J64)));
+                    N, P, nei, slot, side, fa, rv, jt, dd, D, LU64, LU_s, J_s, J64)));
 }
 
 template <typename S>
