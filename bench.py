@@ -696,6 +696,13 @@ def run_kernels(args):
 
     reps = max(args.steps, 3)
     prep_ms = timed(prep, reps)
+    # every launch candidate of the sweep, then the tuned one
+    candidates = {}
+    for tpb, var in ((64, 0), (128, 0), (256, 0), (64, 1), (256, 1), (0, 2), (0, 3), (64, 4), (128, 4), (256, 4)):
+        S.set_launch_config(threads_per_block=tpb, sweep_variant=var)
+        candidates[f"v{var}/b{tpb}"] = timed(pair, 2 * reps)
+    if tuned:
+        S.set_launch_config(**tuned)
     pair_ms = timed(pair, 4 * reps)
     S.blusgs_solve(0.0, 1, 1)                    # one refinement step: x (FP64) != 0 from here on
     res_ms = timed(S.blusgs_residual, reps)      # includes its host read-back
@@ -717,6 +724,7 @@ def run_kernels(args):
         "sweep_pair": {"ms": pair_ms, "GBps": sw / (pair_ms * 1e-3) / 1e9, "frac": sw / (pair_ms * 1e-3) / 1e9 / peak,
                        "bytes": sw},
         "residual_fp64": {"ms": res_ms, "GBps": res_b / (res_ms * 1e-3) / 1e9, "bytes": res_b},
+        "sweep_pair_candidates_ms": candidates,
         "peak": peak}
     print(json.dumps(out))
 

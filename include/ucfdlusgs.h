@@ -104,7 +104,11 @@ UCFD_EXTERN ucfd_status_t UCFDFlowSysSetLaunch(FlowSys sys, int threads_per_bloc
  * TPB/BLOCK macro of Makefile.inc). */
 typedef struct {
     int threads_per_block; /* sweep kernels: 0 (default 256) or 32..256 step 32 */
-    int sweep_variant;     /* block sweep: 0 faces unrolled to the ELL width, 1 face loop */
+    int sweep_variant;     /* block sweep: 0 faces unrolled to the ELL width, 1 face loop,
+                              2 / 3 FP32 5x5 with J and LU tiles staged in shared memory
+                              by bulk copies (2 / 1 buffers per warp; ELL width 6 or 4),
+                              4 = 0 launched as a programmatic dependent of the previous
+                              colour (its start overlaps the previous colour's tail) */
     int run_mode;          /* UCFDLUSGS_Run with mode -1: 0 CUDA graph, 1 persistent kernel */
     double ms;             /* Autotune: time of the best candidate (one sweep pair, or one
                               Run iteration for scalar LU-SGS); 0 when set by hand */

@@ -24,7 +24,9 @@ def test_key_and_validation(monkeypatch):
     assert at.cache_key(FakeSys()) == "GPU|152 SMs|blusgs|N=2097152|nface=6340608|nvars=5|prec=fp32"
     assert at.valid_entry(dict(threads_per_block=128, sweep_variant=1, run_mode=0))
     assert not at.valid_entry(dict(threads_per_block=100, sweep_variant=1, run_mode=0))
-    assert not at.valid_entry(dict(threads_per_block=128, sweep_variant=2, run_mode=0))
+    assert at.valid_entry(dict(threads_per_block=0, sweep_variant=3, run_mode=1))
+    assert not at.valid_entry(dict(threads_per_block=128, sweep_variant=5, run_mode=0))
+    assert not at.valid_entry(dict(threads_per_block=128, sweep_variant=1, run_mode=2))
     assert not at.valid_entry(None)
 
 

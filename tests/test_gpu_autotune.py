@@ -17,14 +17,34 @@ def test_blusgs_launch_choices_bit_identical(prec, ucfd):
     solutions (same operations in the same order per cell)."""
     b = cases.blusgs_case(m=10, seed=2)
     outs = []
-    for tpb in (64, 256):
-        for var in (0, 1):
-            S, e = make(b, prec=prec, on_device=True)
-            S.set_launch_config(threads_per_block=tpb, sweep_variant=var)
-            run_sweeps(S, 3)
-            outs.append(host(e["upts"]))
+    # variants 2 and 3 (bulk copies into shared memory) are FP32-only; the
+    # FP64 systems run the register kernel for them
+    for tpb, var in ((64, 0), (256, 0), (64, 1), (256, 1), (0, 2), (0, 3), (64, 4), (256, 4)):
+        S, e = make(b, prec=prec, on_device=True)
+        S.set_launch_config(threads_per_block=tpb, sweep_variant=var)
+        run_sweeps(S, 3)
+        outs.append(host(e["upts"]))
     for o in outs[1:]:
         np.testing.assert_array_equal(o, outs[0])
+
+
+def test_bulk_sweep_partial_tiles_and_levels(port, ucfd):
+    """Natural-order schedule: many levels whose cell ranges start and end
+    inside 32-cell tiles; the bulk-copy sweep (FP32) equals the register
+    sweep bit for bit and both stay close to the FP64 oracle."""
+    b = cases.blusgs_case(m=7, seed=4)
+    outs = []
+    for var in (0, 2, 3, 4):
+        S, e = make(b, prec=2, on_device=True)
+        assert S.levels() > 5
+        S.set_launch_config(threads_per_block=64, sweep_variant=var)
+        run_sweeps(S, 2)
+        outs.append(host(e["upts"]))
+    for o in outs[1:]:
+        np.testing.assert_array_equal(o, outs[0])
+    up = port.flowsys_blusgs(b, b["rhs"], b["dt"], b["jmat"], b["vol"], b["upts"], nsweeps=2)[0]
+    dq = up - b["upts"]
+    assert np.abs(outs[0] - up).max() <= 1e-4 * np.abs(dq).max()
 
 
 def test_blusgs_autotune_keeps_golden(golden, ucfd):
@@ -38,7 +58,7 @@ def test_blusgs_autotune_keeps_golden(golden, ucfd):
     S.blusgs_ns_prepare()
     cfg = S.autotune(reps=2)
     assert cfg["threads_per_block"] in (64, 128, 192, 256)
-    assert cfg["sweep_variant"] in (0, 1) and cfg["ms"] > 0
+    assert cfg["sweep_variant"] in (0, 1, 4) and cfg["ms"] > 0  # FP64: no bulk-copy variants
     assert S.launch_config()["threads_per_block"] == cfg["threads_per_block"]
     run_sweeps(S, kw["nsweeps"])
     np.testing.assert_array_equal(host(e["upts"]), arr["blu10_upts"])

@@ -73,7 +73,7 @@ def store_cache(path: str, data: dict) -> None:
 
 def valid_entry(e) -> bool:
     return (isinstance(e, dict) and e.get("threads_per_block") in (0, 32, 64, 96, 128, 160, 192, 224, 256)
-            and e.get("sweep_variant") in (0, 1) and e.get("run_mode") in (0, 1))
+            and e.get("sweep_variant") in (0, 1, 2, 3, 4) and e.get("run_mode") in (0, 1))
 
 
 def tune(sys, reps: int = 5, cache: str | bool | None = None, force: bool = False) -> dict:

@@ -74,6 +74,7 @@ struct _FlowSys {
     Work<float> w32;
     DevBuf<double> D, dd, LU64, tD, tLU64, J64, rhs64, x64;  // FP64 block arrays
     DevBuf<double> jt;  // Prepare scratch: face Jacobians, one record per face
+    DevBuf<int> d_sweep_err;  // set by a bulk-copy block sweep whose copy wait gave up
     bool du64_valid = false;
     bool x_zero = false;  // the correction du is all zeros (Reset, no sweep since)
     DevBuf<double> part, red, resid;
@@ -225,6 +226,9 @@ void need_mode(FlowSys s, int m) {
 // Polls of the persistent kernel's grid barrier before it gives up (each
 // poll sleeps ~64 ns): about a second, far beyond any legitimate wait.
 constexpr long long kBarrierMaxSpin = 1ll << 24;
+// Polls of a bulk copy's mbarrier before a block sweep gives up (each
+// poll may suspend for a while): far beyond a copy's microseconds.
+constexpr long long kBulkMaxSpin = 1ll << 20;
 
 template <typename S, bool EX>
 void lusgs_sweep(FlowSys s, bool rans, bool upper, double kappa, bool persistent = false) {
@@ -294,22 +298,37 @@ void blusgs_alloc(FlowSys s) {
     w.rhs.ensure(nv * N);
     w.bdu.ensure(nv * N);
     w.dup.ensure(nv * N);
+    // block arrays in the cell-tiled layout (whole tiles of 32 cells)
     const long long b2 = (long long)s->nfvars * s->nfvars;
-    s->D.ensure(b2 * N);
+    s->D.ensure(tiled_size(N, b2));
     s->dd.ensure(N);
-    s->LU64.ensure(b2 * N);
-    w.J.ensure((long long)s->P * b2 * N);
+    s->LU64.ensure(tiled_size(N, b2));
+    w.J.ensure(tiled_size(N, (long long)s->P * b2));
     if (std::is_same<S, float>::value) {
-        w.LU.ensure(b2 * N);
+        w.LU.ensure(tiled_size(N, b2));
         s->rhs64.ensure(nv * N);
         s->x64.ensure(nv * N);
     }
     if (s->ntvars > 0) {
         const long long t2 = (long long)s->ntvars * s->ntvars;
-        s->tD.ensure(t2 * N);
-        s->tLU64.ensure(t2 * N);
-        w.tJ.ensure((long long)s->P * t2 * N);
-        if (std::is_same<S, float>::value) w.tLU.ensure(t2 * N);
+        s->tD.ensure(tiled_size(N, t2));
+        s->tLU64.ensure(tiled_size(N, t2));
+        w.tJ.ensure(tiled_size(N, (long long)s->P * t2));
+        if (std::is_same<S, float>::value) w.tLU.ensure(tiled_size(N, t2));
+    }
+    if (!s->d_sweep_err.p) s->d_sweep_err.zero(1, s->stream());
+}
+
+// Bulk-copy sweeps report a copy wait that gave up through d_sweep_err;
+// read (and clear) it at the points where the host synchronises anyway.
+void check_sweep_err(FlowSys s) {
+    if (!s->d_sweep_err.p) return;
+    int err = 0;
+    UCFD_CUDA(cudaMemcpyAsync(&err, s->d_sweep_err.p, sizeof(int), cudaMemcpyDeviceToHost, s->stream()));
+    UCFD_CUDA(cudaStreamSynchronize(s->stream()));
+    if (err) {
+        s->d_sweep_err.zero(1, s->stream());
+        fail(UCFD_ERR_TIMEOUT, "block sweep: a bulk copy into shared memory did not complete in time");
     }
 }
 
@@ -332,7 +351,7 @@ void blusgs_sweep_into(FlowSys s, bool turb, bool upper, const S *rhs, S *du) {
         const int l = upper ? L - 1 - q : q;
         KCALL(EX, fs_blusgs_sweep<S>, B, s->sch.lev_off[l], s->sch.lev_off[l + 1], s->N, s->P, var0,
               s->d_nei.p, geo_fa<S>(s), geo_rv<S>(s), turb ? w.tJ.p : w.J.p, blu_LU<S>(s, turb), rhs, du,
-              s->block, s->variant, s->stream());
+              s->block, s->variant, s->d_sweep_err.p, kBulkMaxSpin, s->stream());
     }
 }
 
@@ -355,6 +374,7 @@ void blusgs_residual(FlowSys s, const Sx *x, R *r_out, double *rnorm, double *bn
     double *h = s->h_red.ensure(2);
     UCFD_CUDA(cudaMemcpyAsync(h, s->red.p, 2 * sizeof(double), cudaMemcpyDeviceToHost, s->stream()));
     UCFD_CUDA(cudaStreamSynchronize(s->stream()));
+    check_sweep_err(s);
     *rnorm = std::sqrt(h[0]);
     *bnorm = std::sqrt(h[1]);
 }
@@ -620,7 +640,7 @@ ucfd_status_t UCFDFlowSysSetLaunchConfig(FlowSys s, const UCFDLaunchConfig *cfg)
     const int b = cfg->threads_per_block;
     UCFD_REQUIRE(b == 0 || (b % 32 == 0 && b >= 32 && b <= 256),
                  "threads_per_block must be 0 or a multiple of 32 up to 256 (got %d)", b);
-    UCFD_REQUIRE(cfg->sweep_variant == 0 || cfg->sweep_variant == 1, "sweep_variant must be 0 or 1");
+    UCFD_REQUIRE(cfg->sweep_variant >= 0 && cfg->sweep_variant <= 4, "sweep_variant must be 0..4");
     UCFD_REQUIRE(cfg->run_mode == 0 || cfg->run_mode == 1, "run_mode must be 0 or 1");
     if (b != s->block) run_graph_drop(s);
     s->block = b;
@@ -668,18 +688,31 @@ ucfd_status_t UCFDFlowSysAutotune(FlowSys s, int reps, UCFDLaunchConfig *best) {
             UCFD_REQUIRE(w.rhs.p && w.J.p && blu_LU<S>(s, false), "Autotune before Pack and NSPrepare");
             DevBuf<S> scratch;
             scratch.zero(n, st);
-            // the unrolled kernel exists for ELL widths 6 and 4 only
-            const int nvar = (s->P == 6 || s->P == 4) ? 2 : 1;
-            for (int v = 0; v < nvar; ++v)
+            auto pair_ms = [&] {
+                return time_ms(st, reps, [&] {
+                    blusgs_sweep_into<S, EX>(s, false, false, w.rhs.p, scratch.p);
+                    blusgs_sweep_into<S, EX>(s, false, true, w.rhs.p, scratch.p);
+                });
+            };
+            // the unrolled kernels exist for ELL widths 6 and 4 only
+            const bool unrolled = s->P == 6 || s->P == 4;
+            for (int v : {0, 1, 4}) {
+                if (v != 0 && !unrolled) continue;
                 for (int b : kTuneBlocks) {
                     s->block = b;
                     s->variant = v;
-                    const double ms = time_ms(st, reps, [&] {
-                        blusgs_sweep_into<S, EX>(s, false, false, w.rhs.p, scratch.p);
-                        blusgs_sweep_into<S, EX>(s, false, true, w.rhs.p, scratch.p);
-                    });
-                    consider(ms, b, v, s->run_mode);
+                    consider(pair_ms(), b, v, s->run_mode);
                 }
+            }
+            // bulk-copy kernels (FP32, 5x5 blocks): fixed launch shape
+            if (std::is_same<S, float>::value && unrolled && s->nfvars == 5) {
+                for (int v = 2; v <= 3; ++v) {
+                    s->block = 0;
+                    s->variant = v;
+                    consider(pair_ms(), 0, v, s->run_mode);
+                }
+                check_sweep_err(s);
+            }
         });
     } else {
         UCFD_REQUIRE(s->fspr, "fspr is not set");
@@ -973,7 +1006,7 @@ static ucfd_status_t blusgs_prepare_api(FlowSys s, bool turb) {
             // FP32 sweeps read the rounded factors only
             LU_s = turb ? w.tLU.p : w.LU.p;
             LU64 = nullptr;
-            if (!turb) J64 = s->J64.ensure((size_t)s->P * B * B * s->N);
+            if (!turb) J64 = s->J64.ensure(tiled_size(s->N, (long long)s->P * B * B));
         }
         double *jt = s->jt.ensure((size_t)2 * B * B * s->nfaces);
         KCALL(EX, fs_blusgs_prepare<S>, B, s->N, s->P, (long long)s->nfaces, s->d_nei.p, s->d_slot.p, s->d_side.p,
@@ -999,6 +1032,7 @@ static ucfd_status_t blusgs_sweep_api(FlowSys s, bool turb, bool upper) {
     s->du64_valid = false;
     s->x_zero = false;
     finish(s);
+    if (!s->async) check_sweep_err(s);
     UCFD_API_END
 }
 

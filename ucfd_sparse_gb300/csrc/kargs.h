@@ -1,7 +1,24 @@
 // kargs.h -- plain argument structs shared by host code and kernels.
 #pragma once
 
+#ifdef __CUDACC__
+#define UCFD_HD __host__ __device__
+#else
+#define UCFD_HD
+#endif
+
 namespace ucfd {
+
+// Cell-tiled layout of the per-cell block arrays (J, LU, D of block
+// LU-SGS): internal cells are grouped in tiles of 32 consecutive cells and
+// element j (of m per cell) of cell k sits at ((k / 32) * m + j) * 32 + k % 32.
+// A warp on one tile reads each element as one 128-byte (FP32) line, and
+// all m elements of a tile are one contiguous block (a single bulk copy).
+constexpr int kCellTile = 32;
+UCFD_HD inline long long tile_index(long long k, long long j, long long m) {
+    return (((k >> 5) * m + j) << 5) + (k & 31);
+}
+UCFD_HD inline long long tiled_size(long long N, long long m) { return ((N + 31) >> 5) * m * 32; }
 
 // One launch of the scalar LU-SGS sweep over a range of cells that are
 // independent of each other (one colour or one level).

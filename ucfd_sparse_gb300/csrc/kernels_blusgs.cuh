@@ -2,12 +2,14 @@
 //
 // Internal arrays (N = internal cells, P = ELL width, B = block size):
 //   nei [P][N] (-1 padding), fa [P][N], rv [N]
-//   J   [P][B*B][N]  the off-diagonal block each cell-face multiplies its
-//                    neighbour increment with (jmat half 1 when side == 1,
-//                    minus half 0 otherwise, blusgs.c:307-310)
-//   D   [B*B][N]     unfactored diagonal block (FP64)
-//   LU  [B*B][N]     its in-place LU factors (ludcmp, inverse.h:13-45)
+//   J   tiled, m = P*B*B (element p*B*B + r*B + c): the off-diagonal block
+//                    each cell-face multiplies its neighbour increment with
+//                    (jmat half 1 when side == 1, minus half 0 otherwise,
+//                    blusgs.c:307-310)
+//   D   tiled, m = B*B   unfactored diagonal block (FP64)
+//   LU  tiled, m = B*B   its in-place LU factors (ludcmp, inverse.h:13-45)
 //   rhs, du [nvars][N]
+// "tiled" is the cell-tile layout of kargs.h (tile_index).
 #pragma once
 
 #include "kernels_common.cuh"
@@ -104,7 +106,7 @@ __global__ void fs_tblusgs_pack_kernel(int model, int neles, int nvars, int nt, 
         A[0] += dsrc[idx + (long long)(nvars - 1) * neles];
     }
     for (int row = 0; row < nt; ++row) A[row + row * nt] += 1 / (dt[idx] * factor) + a0;
-    for (int e = 0; e < nt * nt; ++e) D[e * N + k] = A[e];
+    for (int e = 0; e < nt * nt; ++e) D[::ucfd::tile_index(k, e, nt * nt)] = A[e];
 }
 
 // Face Jacobians from the caller's layout jmat[2][B][B][nF] (face index
@@ -150,8 +152,9 @@ __global__ void fs_blusgs_prepare_kernel(long long N, int P, const int *nei, con
         for (int e = 0; e < B2; ++e) dm[e] = (e % (B + 1) == 0) ? d : 0.0;
     } else {
 #pragma unroll
-        for (int e = 0; e < B2; ++e) dm[e] = D[e * N + k];
+        for (int e = 0; e < B2; ++e) dm[e] = D[::ucfd::tile_index(k, e, B2)];
     }
+    const long long jbase = ::ucfd::tile_index(k, 0, (long long)P * B2);
     for (int p = 0; p < P; ++p) {
         if (nei[p * N + k] < 0) break;
         const long long s = slot[p * N + k];
@@ -173,18 +176,20 @@ __global__ void fs_blusgs_prepare_kernel(long long N, int P, const int *nei, con
                 const double val = (sd == 1) ? h0 : -h1;
                 dm[c + r * B] += val * fv;
                 const double jv = (sd == 1) ? h1 : -h0;
-                J_s[((long long)p * B2 + r * B + c) * N + k] = (S)jv;
-                if (J64) J64[((long long)p * B2 + r * B + c) * N + k] = jv;
+                const long long o = jbase + ((long long)(p * B2 + r * B + c) << 5);
+                J_s[o] = (S)jv;
+                if (J64) J64[o] = jv;
             }
         }
     }
+    const long long dbase = ::ucfd::tile_index(k, 0, B2);
 #pragma unroll
-    for (int e = 0; e < B2; ++e) D[e * N + k] = dm[e];
+    for (int e = 0; e < B2; ++e) D[dbase + (e << 5)] = dm[e];
     ludcmp_dev<double, B>(dm);
 #pragma unroll
     for (int e = 0; e < B2; ++e) {
-        if (LU64) LU64[e * N + k] = dm[e];
-        if (LU_s) LU_s[e * N + k] = (S)dm[e];
+        if (LU64) LU64[dbase + (e << 5)] = dm[e];
+        if (LU_s) LU_s[dbase + (e << 5)] = (S)dm[e];
     }
 }
 
@@ -198,14 +203,30 @@ __global__ void fs_blusgs_prepare_kernel(long long N, int P, const int *nei, con
 // keeps all of its memory traffic in flight (the reference's per-face
 // order of the products and subtractions is kept; padding entries only
 // skip their contribution).  PW == 0 is the generic runtime-width loop.
-template <typename S, int B, int PW>
+//
+// DEP (PW > 0 only): launched as a programmatic dependent of the previous
+// sweep launch (one colour after the other).  The grid lets its own
+// dependent start at once, then loads every input the previous launch
+// does not write (rhs, rv, nei, fa) before it waits for that launch to
+// complete (griddepcontrol.wait); the neighbour increments du are read
+// after the wait.  This overlaps a launch's start with the previous
+// launch's tail, which pays where levels are small.  Results are those of
+// DEP == false.  (An L2 bulk prefetch of each warp's J and LU tiles in
+// front of the wait measured slower at 2.1M cells: the early grids'
+// prefetches evict the running grid's data.)
+template <typename S, int B, int PW, bool DEP = false>
 __global__ void __launch_bounds__(256) fs_blusgs_sweep_kernel(int t0, int t1, long long N, int P,
                                                               int var0, const int *nei, const S *fa,
                                                               const S *rv, const S *J, const S *LU,
                                                               const S *rhs, S *du) {
-    const int k = t0 + blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= t1) return;
+    static_assert(!DEP || PW > 0, "the dependent-launch form is the unrolled one");
+    if constexpr (DEP) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    // threads start at the tile boundary below t0, so every warp reads
+    // whole tiles; the cells of the tile outside [t0, t1) do nothing
+    const int k = (t0 & ~31) + blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < t0 || k >= t1) return;
     constexpr int B2 = B * B;
+    const S *Jk = J + ::ucfd::tile_index(k, 0, (long long)P * B2);
     S b[B];
 #pragma unroll
     for (int r = 0; r < B; ++r) b[r] = rhs[(var0 + r) * N + k];
@@ -218,6 +239,7 @@ __global__ void __launch_bounds__(256) fs_blusgs_sweep_kernel(int t0, int t1, lo
             nb[p] = __ldg(nei + p * N + k);
             fv[p] = __ldg(fa + p * N + k) * rvk;
         }
+        if constexpr (DEP) asm volatile("griddepcontrol.wait;" ::: "memory");
         S x[PW][B];
 #pragma unroll
         for (int p = 0; p < PW; ++p) {
@@ -227,10 +249,10 @@ __global__ void __launch_bounds__(256) fs_blusgs_sweep_kernel(int t0, int t1, lo
         }
 #pragma unroll
         for (int p = 0; p < PW; ++p) {
-            const S *Jp = J + (long long)p * B2 * N + k;
+            const S *Jp = Jk + ((long long)p * B2 << 5);
             S jv[B2];
 #pragma unroll
-            for (int e = 0; e < B2; ++e) jv[e] = __ldg(Jp + e * N);
+            for (int e = 0; e < B2; ++e) jv[e] = __ldg(Jp + (e << 5));
             if (nb[p] >= 0) {
 #pragma unroll
                 for (int r = 0; r < B; ++r) {
@@ -249,22 +271,132 @@ __global__ void __launch_bounds__(256) fs_blusgs_sweep_kernel(int t0, int t1, lo
             S x[B];
 #pragma unroll
             for (int c = 0; c < B; ++c) x[c] = du[(var0 + c) * N + nb];
-            const S *Jp = J + (long long)p * B2 * N + k;
+            const S *Jp = Jk + ((long long)p * B2 << 5);
 #pragma unroll
             for (int r = 0; r < B; ++r) {
                 S val = S(0);
 #pragma unroll
-                for (int c = 0; c < B; ++c) val += __ldg(Jp + (r * B + c) * N) * x[c];
+                for (int c = 0; c < B; ++c) val += __ldg(Jp + ((r * B + c) << 5)) * x[c];
                 b[r] -= val * fv;
             }
         }
     }
     S lu[B2];
+    const S *LUk = LU + ::ucfd::tile_index(k, 0, B2);
 #pragma unroll
-    for (int e = 0; e < B2; ++e) lu[e] = __ldg(LU + e * N + k);
+    for (int e = 0; e < B2; ++e) lu[e] = __ldg(LUk + (e << 5));
     lusub_dev<S, B>(lu, b);
 #pragma unroll
     for (int r = 0; r < B; ++r) du[(var0 + r) * N + k] = b[r];
+}
+
+// FP32 block sweep with each tile's J and LU staged in shared memory by
+// bulk asynchronous copies (cp.async.bulk, completed on an mbarrier).
+// Every warp owns a ring of NST tile buffers and walks the level's tiles
+// with a grid stride; one tile's J and LU (PW*B*B + B*B values for each of
+// its 32 cells) are two contiguous blocks of the tiled layout, so each is
+// one copy.  With NST == 2 the copy of the warp's next tile is in flight
+// while it gathers the neighbour increments of the current tile and
+// computes it; with NST == 1 twice as many warps fit, each with one
+// buffer.  Per cell the arithmetic is that of fs_blusgs_sweep_kernel
+// (same products and subtractions, same order).  A copy that has not
+// landed after max_spin polls sets *err; the warp then waits (bounded)
+// for its other copy and returns.
+template <int B, int PW, int NST>
+__global__ void __launch_bounds__(NST == 2 ? 128 : 256)
+    fs_blusgs_sweep_bulk_kernel(int t0, int t1, long long N, int var0, const int *__restrict__ nei,
+                                const float *__restrict__ fa, const float *__restrict__ rv,
+                                const float *__restrict__ J, const float *__restrict__ LU,
+                                const float *__restrict__ rhs, float *du, int *err, long long max_spin) {
+    constexpr int B2 = B * B;
+    constexpr int JT = PW * B2 * 32;  // floats of J in one tile
+    constexpr int LT = B2 * 32;       // floats of LU in one tile
+    constexpr int ST = JT + LT;       // floats per buffer
+    constexpr unsigned JBYTES = JT * 4, LBYTES = LT * 4;
+    static_assert(JBYTES % 16 == 0 && LBYTES % 16 == 0, "bulk copies move multiples of 16 bytes");
+    static_assert(JBYTES + LBYTES < (1u << 20), "mbarrier transaction count");
+    extern __shared__ __align__(16) float smem_f[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nwarps = blockDim.x >> 5;
+    float *buf = smem_f + (size_t)warp * NST * ST;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_f + (size_t)nwarps * NST * ST) + NST * warp;
+    const long long tile1 = ((long long)t1 + 31) >> 5;
+    const long long step = (long long)gridDim.x * nwarps;
+    long long t = (t0 >> 5) + (long long)blockIdx.x * nwarps + warp;
+    if (lane == 0) {
+#pragma unroll
+        for (int q = 0; q < NST; ++q) ::ucfd::dev::mbar_init(&bar[q], 1);
+        ::ucfd::dev::fence_mbar_init();
+    }
+    __syncwarp();
+    // lane 0 starts the copies of tile tt into buffer q
+    auto issue = [&](long long tt, int q) {
+        if (lane == 0) {
+            ::ucfd::dev::fence_proxy_async_smem();
+            ::ucfd::dev::mbar_arrive_expect_tx(&bar[q], JBYTES + LBYTES);
+            ::ucfd::dev::bulk_copy_g2s(buf + q * ST, J + tt * JT, JBYTES, &bar[q]);
+            ::ucfd::dev::bulk_copy_g2s(buf + q * ST + JT, LU + tt * LT, LBYTES, &bar[q]);
+        }
+    };
+    if (t < tile1) issue(t, 0);
+    for (unsigned it = 0; t < tile1; t += step, ++it) {
+        const int q = NST == 2 ? (int)(it & 1) : 0;
+        const unsigned parity = (NST == 2 ? (it >> 1) : it) & 1;
+        const long long tn = t + step;
+        if (NST == 2 && tn < tile1) issue(tn, q ^ 1);
+        const long long k = (t << 5) + lane;
+        const bool act = k >= t0 && k < t1;
+        const long long kk = act ? k : t0;  // any valid cell for the idle lanes
+        float b[B];
+#pragma unroll
+        for (int r = 0; r < B; ++r) b[r] = rhs[(var0 + r) * N + kk];
+        const float rvk = rv[kk];
+        int nb[PW];
+        float fv[PW];
+#pragma unroll
+        for (int p = 0; p < PW; ++p) {
+            nb[p] = act ? __ldg(nei + p * N + kk) : -1;
+            fv[p] = __ldg(fa + p * N + kk) * rvk;
+        }
+        float x[PW][B];
+#pragma unroll
+        for (int p = 0; p < PW; ++p) {
+            const long long g = nb[p] >= 0 ? nb[p] : kk;
+#pragma unroll
+            for (int c = 0; c < B; ++c) x[p][c] = nb[p] >= 0 ? du[(var0 + c) * N + g] : 0.f;
+        }
+        const bool ok = __all_sync(0xffffffffu, ::ucfd::dev::mbar_wait_bounded(&bar[q], parity, max_spin));
+        if (!ok) {
+            if (lane == 0) atomicExch(err, 1);
+            if (NST == 2 && tn < tile1)
+                (void)::ucfd::dev::mbar_wait_bounded(&bar[q ^ 1], ((it + 1) >> 1) & 1, max_spin);
+            (void)::ucfd::dev::mbar_wait_bounded(&bar[q], parity, max_spin);
+            return;
+        }
+        const float *sJ = buf + q * ST + lane;
+#pragma unroll
+        for (int p = 0; p < PW; ++p) {
+            if (nb[p] >= 0) {
+#pragma unroll
+                for (int r = 0; r < B; ++r) {
+                    float val = 0.f;
+#pragma unroll
+                    for (int c = 0; c < B; ++c) val += sJ[(p * B2 + r * B + c) << 5] * x[p][c];
+                    b[r] -= val * fv[p];
+                }
+            }
+        }
+        float lu[B2];
+#pragma unroll
+        for (int e = 0; e < B2; ++e) lu[e] = sJ[JT + (e << 5)];
+        lusub_dev<float, B>(lu, b);
+        if (act) {
+#pragma unroll
+            for (int r = 0; r < B; ++r) du[(var0 + r) * N + k] = b[r];
+        }
+        __syncwarp();
+        if (NST == 1 && tn < tile1) issue(tn, 0);
+    }
 }
 
 // FP64 residual of the packed system: r = rhs - D x - sum_f J x_nb fv.
@@ -290,7 +422,7 @@ __global__ void fs_blusgs_residual_kernel(long long N, int P, int var0, int nvar
             bb += v * v;
             if (x) {
 #pragma unroll
-                for (int c = 0; c < B; ++c) v -= D[(r * B + c) * N + k] * xk[c];
+                for (int c = 0; c < B; ++c) v -= D[::ucfd::tile_index(k, r * B + c, B2)] * xk[c];
             }
             res[r] = v;
         }
@@ -320,7 +452,8 @@ __global__ void fs_blusgs_residual_kernel(long long N, int P, int var0, int nvar
                 for (int r = 0; r < B; ++r) {
                     double val = 0.0;
 #pragma unroll
-                    for (int c = 0; c < B; ++c) val += J64[((long long)p * B2 + r * B + c) * N + k] * xn[q][c];
+                    for (int c = 0; c < B; ++c)
+                        val += J64[::ucfd::tile_index(k, (long long)p * B2 + r * B + c, (long long)P * B2)] * xn[q][c];
                     res[r] -= val * fv;
                 }
             }

@@ -4,6 +4,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "bulk_copy.cuh"
+#include "kargs.h"
+
 #ifndef UCFD_KNS
 #error "UCFD_KNS (kernel namespace) must be defined by the including translation unit"
 #endif

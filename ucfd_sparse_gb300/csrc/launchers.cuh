@@ -223,16 +223,86 @@ void fs_blusgs_prepare(int B, long long N, int P, long long nF, const int *nei, 
                     N, P, nei, slot, side, fa, rv, jt, dd, D, LU64, LU_s, J_s, J64)));
 }
 
+// Bulk-copy sweep: NST buffers per warp, 4 (NST 2) or 8 (NST 1) warps per
+// block; grid capped at the blocks that fit on the device at once.
+template <int B, int PW, int NST>
+static void sweep_bulk_go(int t0, int t1, long long N, int var0, const int *nei, const float *fa,
+                          const float *rv, const float *J, const float *LU, const float *rhs, float *du,
+                          int *err, long long max_spin, cudaStream_t s) {
+    auto kern = fs_blusgs_sweep_bulk_kernel<B, PW, NST>;
+    constexpr int threads = NST == 2 ? 128 : 256;
+    constexpr size_t smem = (size_t)(threads / 32) * NST * ((PW + 1) * B * B * 32 * sizeof(float) + 8);
+    static int cap = 0;  // per instantiation: co-resident blocks on the device
+    if (!cap) {
+        UCFD_CUDA(cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        int per_sm = 0, dev = 0, sms = 0;
+        UCFD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
+        UCFD_CUDA(cudaGetDevice(&dev));
+        UCFD_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        if (per_sm <= 0) ::ucfd::fail(UCFD_ERR_UNSUPPORTED, "bulk-copy sweep kernel does not fit on the device");
+        cap = per_sm * sms;
+    }
+    const long long tiles = (((long long)t1 + 31) >> 5) - (t0 >> 5);
+    const long long want = (tiles + threads / 32 - 1) / (threads / 32);
+    const unsigned g = (unsigned)(want < cap ? want : cap);
+    kern<<<g, threads, smem, s>>>(t0, t1, N, var0, nei, fa, rv, J, LU, rhs, du, err, max_spin);
+}
+
+// Unrolled sweep launched as a programmatic dependent of the previous
+// launch on the stream (cudaLaunchAttributeProgrammaticStreamSerialization).
+template <typename S, int B, int PW>
+static void sweep_dep_go(unsigned g, int block, cudaStream_t s, int t0, int t1, long long N, int P, int var0,
+                         const int *nei, const S *fa, const S *rv, const S *J, const S *LU, const S *rhs, S *du) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(g);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    UCFD_CUDA(cudaLaunchKernelEx(&cfg, fs_blusgs_sweep_kernel<S, B, PW, true>, t0, t1, N, P, var0, nei, fa, rv, J,
+                                 LU, rhs, du));
+}
+
 template <typename S>
 void fs_blusgs_sweep(int B, int t0, int t1, long long N, int P, int var0, const int *nei, const S *fa,
                      const S *rv, const S *J, const S *LU, const S *rhs, S *du, int block,
-                     int variant, cudaStream_t s) {
+                     int variant, int *err, long long max_spin, cudaStream_t s) {
     if (t1 <= t0) return;
     if (block <= 0) block = kBlock;
-    const unsigned g = grid_for(t1 - t0, block);
+    // threads start at the tile boundary below t0 (see the kernel)
+    const unsigned g = grid_for(t1 - (t0 & ~31), block);
     // variant 0: faces unrolled to the ELL width (6 or 4) when it matches;
-    // variant 1: the face loop that stops at the first padding slot.
-    // Both apply the faces in the same order with the same operations.
+    // variant 1: the face loop that stops at the first padding slot;
+    // variants 2 / 3: FP32, ELL width 6 or 4, block 5: J and LU tiles staged
+    // in shared memory by bulk copies, 2 / 1 buffers per warp;
+    // variant 4: variant 0 launched as a programmatic dependent of the
+    // previous launch (its start overlaps the previous colour's tail).
+    // All apply the faces in the same order with the same operations.
+    if (variant == 4 && (P == 6 || P == 4)) {
+        if (P == 6) {
+            UCFD_BSW(B, (sweep_dep_go<S, BB, 6>(g, block, s, t0, t1, N, P, var0, nei, fa, rv, J, LU, rhs, du)));
+        } else {
+            UCFD_BSW(B, (sweep_dep_go<S, BB, 4>(g, block, s, t0, t1, N, P, var0, nei, fa, rv, J, LU, rhs, du)));
+        }
+        return;
+    }
+    if constexpr (std::is_same<S, float>::value) {
+        if ((variant == 2 || variant == 3) && B == 5 && (P == 6 || P == 4)) {
+            if (!err) ::ucfd::fail(UCFD_ERR_ARGUMENT, "bulk-copy sweep needs an error flag");
+            if (P == 6) {
+                if (variant == 2) sweep_bulk_go<5, 6, 2>(t0, t1, N, var0, nei, fa, rv, J, LU, rhs, du, err, max_spin, s);
+                else sweep_bulk_go<5, 6, 1>(t0, t1, N, var0, nei, fa, rv, J, LU, rhs, du, err, max_spin, s);
+            } else {
+                if (variant == 2) sweep_bulk_go<5, 4, 2>(t0, t1, N, var0, nei, fa, rv, J, LU, rhs, du, err, max_spin, s);
+                else sweep_bulk_go<5, 4, 1>(t0, t1, N, var0, nei, fa, rv, J, LU, rhs, du, err, max_spin, s);
+            }
+            return;
+        }
+    }
     if (variant == 1) {
         UCFD_BSW(B, (fs_blusgs_sweep_kernel<S, BB, 0><<<g, block, 0, s>>>(t0, t1, N, P, var0, nei, fa, rv, J, LU,
                                                                           rhs, du)));

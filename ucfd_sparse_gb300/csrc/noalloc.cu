@@ -28,6 +28,7 @@
 #include <cmath>
 
 #include "../../include/ucfdlusgs.h"
+#include "kargs.h"
 #include "flowsys_view.h"
 #include "ucfd_internal.h"
 
@@ -81,7 +82,7 @@ __global__ void __launch_bounds__(kThreads) residual_noalloc_kernel(long long N,
             double v = rhs64[r * N + k];
             bb += v * v;
 #pragma unroll
-            for (int c = 0; c < B; ++c) v -= D[(r * B + c) * N + k] * xk[c];
+            for (int c = 0; c < B; ++c) v -= D[::ucfd::tile_index(k, r * B + c, B2)] * xk[c];
             res[r] = v;
         }
         for (int p = 0; p < P; ++p) {
@@ -95,7 +96,8 @@ __global__ void __launch_bounds__(kThreads) residual_noalloc_kernel(long long N,
             for (int r = 0; r < B; ++r) {
                 double val = 0.0;
 #pragma unroll
-                for (int c = 0; c < B; ++c) val += J64[((long long)p * B2 + r * B + c) * N + k] * xn[c];
+                for (int c = 0; c < B; ++c)
+                    val += J64[::ucfd::tile_index(k, (long long)p * B2 + r * B + c, (long long)P * B2)] * xn[c];
                 res[r] -= val * fv;
             }
         }
