@@ -33,6 +33,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "LU-SGS cell-updates/s & HBM GB/s @2.1M cells; FP32+refine vs FP64 @1e-10"
 UNIT = "cell-updates/s"
+# DRAM bytes per cell update of the unrolled FP32 block sweep measured by
+# ncu on the 64^3 mesh (profiles/fs_blusgs_sweep_float5_64cubed.md)
+SWEEP_TRAFFIC_PER_CELL = 866.0
 
 
 # ---------------------------------------------------------------------------
@@ -286,7 +289,7 @@ def run_gpu(args):
 
     case = make_case(args.mesh, seed=args.seed + rank)
     N = case["nlocal"]
-    ic, rg, lc = cl.greedy_coloring_csr(case["rowptr"], case["colidx"])
+    ic, rg, lc = cl.greedy_coloring_csr(case["rowptr"], case["colidx"], order=args.coloring)
     stream = torch.cuda.Stream(device=device)
     P32 = Problem(case, lc, 2, stream, device)
     P64 = Problem(case, lc, 1, stream, device)
@@ -345,15 +348,17 @@ def run_gpu(args):
     bytes_sweep = sweep_bytes(case["rowptr"], 4, 5, 4)
     achieved = bytes_sweep / (sweep_ms * 1e-3) / 1e9
     launch_bytes = bytes_sweep / nlev
-    traffic = None
-    tf = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tf):
-        t = json.load(open(tf)).get("fs_blusgs_sweep_kernel<float,5>")
-        if t:
-            traffic = t["bytes_per_cell"] * N / nlev
+    cfg32 = P32.S.launch_config()
+    kname = {0: "fs_blusgs_sweep_kernel<float,5,6>", 1: "fs_blusgs_sweep_kernel<float,5,0>",
+             2: "fs_blusgs_sweep_bulk_kernel<5,6,2>", 3: "fs_blusgs_sweep_bulk_kernel<5,6,1>",
+             4: "fs_blusgs_sweep_kernel<float,5,6,true>"}.get(cfg32["sweep_variant"], "fs_blusgs_sweep_kernel")
+    # DRAM bytes per cell update from ncu (dram__bytes_read.sum + write) of
+    # the unrolled FP32 sweep on the 64^3 case, scaled to this launch's cells
+    traffic = SWEEP_TRAFFIC_PER_CELL * N / nlev if cfg32["sweep_variant"] in (0, 4) else None
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": traffic, "kernel": "fs_blusgs_sweep_kernel<float,5>",
+                "traffic": traffic, "kernel": kname, "threads_per_block": cfg32["threads_per_block"],
                 "algorithmic_bytes_per_launch": launch_bytes, "launch_ms": sweep_ms / nlev,
+                "traffic_source": "ncu 64^3 capture, 866 B per cell update, scaled by cells per launch",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s"}
 
     # ---- end to end through the C-ABI with pinned host buffers -------------
@@ -380,8 +385,9 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 sweeps + f64 refinement/LU/residual", "data": "synthetic",
             "config": {"workload": f"BLU-SGS 5x5 face Jacobians, {args.mesh}^3 jittered (+-0.2h) randomly permuted "
-                                   f"hex ({N} cells), greedy colouring ({len(rg)} colours), solve to rtol "
-                                   f"{args.rtol:g} per pseudo-time step", "cells": N, "colors": len(rg),
+                                   f"hex ({N} cells), greedy colouring in {args.coloring} order ({len(rg)} colours), "
+                                   f"solve to rtol {args.rtol:g} per pseudo-time step", "cells": N, "colors": len(rg),
+                       "coloring": args.coloring,
                        "inner_sweeps": args.inner, "fp64_check_every": args.check, "l2": "inputs larger than L2 (no flush needed)",
                        "parallelism": f"replicas x{ws}"},
             "pairs_per_step": pairs_mean, "relres": max(rel32),
@@ -666,7 +672,7 @@ def run_kernels(args):
     lib.load()
     case = make_case(args.mesh, seed=args.seed)
     N = case["nlocal"]
-    ic, rg, lc = cl.greedy_coloring_csr(case["rowptr"], case["colidx"])
+    ic, rg, lc = cl.greedy_coloring_csr(case["rowptr"], case["colidx"], order=args.coloring)
     device = torch.device("cuda", 0)
     stream = torch.cuda.Stream(device=device)
     P = Problem(case, lc, 2, stream, device)
@@ -700,10 +706,10 @@ def run_kernels(args):
     candidates = {}
     for tpb, var in ((64, 0), (128, 0), (256, 0), (64, 1), (256, 1), (0, 2), (0, 3), (64, 4), (128, 4), (256, 4)):
         S.set_launch_config(threads_per_block=tpb, sweep_variant=var)
-        candidates[f"v{var}/b{tpb}"] = timed(pair, 2 * reps)
+        candidates[f"v{var}/b{tpb}"] = timed(pair, max(10, 2 * reps))
     if tuned:
         S.set_launch_config(**tuned)
-    pair_ms = timed(pair, 4 * reps)
+    pair_ms = timed(pair, max(20, 4 * reps))
     S.blusgs_solve(0.0, 1, 1)                    # one refinement step: x (FP64) != 0 from here on
     res_ms = timed(S.blusgs_residual, reps)      # includes its host read-back
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
@@ -743,6 +749,8 @@ def main(argv=None):
     ap.add_argument("--max-pairs", type=int, default=400)
     ap.add_argument("--ref-pairs", type=int, default=1)
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")
+    ap.add_argument("--coloring", default="index", choices=["index", "bfs"],
+                    help="greedy colouring visiting cells by index or in breadth-first order")
     ap.add_argument("--workload", default="blusgs", choices=["blusgs", "lusgs", "gmres", "colored", "kernels"],
                     help="blusgs: the headline line; the others measure the remaining configurations")
     ap.add_argument("--iters", type=int, default=200, help="iterations of the lusgs/colored workloads")

@@ -77,6 +77,13 @@ UCFD_EXTERN ucfd_status_t UCFDSetConstants(UCFDReal gamma, UCFDReal pmin, UCFDRe
 UCFD_EXTERN const char *UCFDVersion(void);
 UCFD_EXTERN ucfd_status_t UCFDDeviceInfo(char *name, size_t len, int *sm_count);
 
+/* Diagnostics: runs the two bounded device waits of the sweeps (the grid
+ * barrier of the persistent scalar sweep, the mbarrier wait of the
+ * bulk-copy block sweep) on states that never complete and reports
+ * whether each gave up as designed (1) -- instead of hanging -- leaving the
+ * context usable.  No counterpart in the reference. */
+UCFD_EXTERN ucfd_status_t UCFDSelfTestTimeouts(int *barrier_timed_out, int *mbarrier_timed_out);
+
 #if defined(__cplusplus)
 }
 #endif

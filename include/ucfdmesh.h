@@ -35,6 +35,13 @@ UCFD_EXTERN ucfd_status_t UCFDGreedyColoring(int neles, int nface, const int *ne
 UCFD_EXTERN ucfd_status_t UCFDGreedyColoringCSR(int n, const int *rowptr, const int *colidx,
                                                 int *lcolor, int *icolor, int *ranges,
                                                 int *ncolors);
+/* First-fit greedy colouring of a CSR graph visiting the cells in
+ * breadth-first order from a pseudo-peripheral cell (fewer colours than
+ * index order: two on a bipartite hexahedral mesh); same outputs as
+ * UCFDGreedyColoringCSR.  No counterpart in the reference (its colourings
+ * come from the caller or examples/utils/pbutils). */
+UCFD_EXTERN ucfd_status_t UCFDBFSColoringCSR(int n, const int *rowptr, const int *colidx,
+                                             int *lcolor, int *icolor, int *ranges, int *ncolors);
 
 #if defined(__cplusplus)
 }

@@ -120,6 +120,27 @@ def test_greedy_colouring_csr(ucfd):
     _check_colouring(tab, ic, rg, lc)
 
 
+def test_bfs_colouring_csr(ucfd):
+    """Breadth-first greedy colouring: valid, and two colours on a permuted
+    hexahedral mesh (a bipartite graph) where index order needs more."""
+    from ucfd_sparse_gb300 import coloredlusgs as cl
+    from ucfd_sparse_gb300 import meshgen as mg
+    b = mg.blusgs_case(8)
+    ic, rg, lc = cl.greedy_coloring_csr(b["rowptr"], b["colidx"], order="bfs")
+    tab = mg.csr_neighbors_to_table(b["rowptr"], b["colidx"])
+    _check_colouring(tab, ic, rg, lc)
+    assert len(rg) == 2
+    assert len(cl.greedy_coloring_csr(b["rowptr"], b["colidx"])[1]) > 2
+    # tets: valid, not bipartite
+    nei = mg.kuhn_tet_adjacency(4)
+    n = nei.shape[1]
+    rp = np.arange(0, 4 * n + 1, 4, dtype=np.int32)
+    ci = np.where(nei >= 0, nei, np.arange(n)[None, :]).T.reshape(-1).astype(np.int32)
+    ic, rg, lc = cl.greedy_coloring_csr(rp, ci, order="bfs")
+    tab = np.where(nei >= 0, nei, np.arange(n)[None, :]).astype(np.int32)
+    _check_colouring(tab, ic, rg, lc)
+
+
 def test_meshgen_geometry_is_closed():
     from ucfd_sparse_gb300 import meshgen as mg
     m = mg.HexMesh(6, jitter=0.2, seed=3)

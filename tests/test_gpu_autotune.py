@@ -47,6 +47,24 @@ def test_bulk_sweep_partial_tiles_and_levels(port, ucfd):
     assert np.abs(outs[0] - up).max() <= 1e-4 * np.abs(dq).max()
 
 
+def test_dependent_launch_large_and_small_levels(ucfd):
+    """Greedy colours of a 40^3 mesh: the big colours (> 16384 cells) take the
+    dependent-launch register kernel, the small ones the register-hoisted
+    kernel; both equal the plain unrolled kernel bit for bit."""
+    from ucfd_sparse_gb300 import coloredlusgs as cl
+    b = cases.blusgs_case(m=40, seed=6)
+    ic, rg, lc = cl.greedy_coloring_csr(b["rowptr"], b["colidx"])
+    sizes = np.diff([0] + rg)
+    assert sizes.max() > 16384 and sizes.min() < 16384
+    outs = []
+    for var in (0, 4):
+        S, e = make(b, prec=2, on_device=True, colored=lc)
+        S.set_launch_config(threads_per_block=128, sweep_variant=var)
+        run_sweeps(S, 3)
+        outs.append(host(e["upts"]))
+    np.testing.assert_array_equal(outs[1], outs[0])
+
+
 def test_blusgs_autotune_keeps_golden(golden, ucfd):
     """Autotune runs after Pack + NSPrepare; the sweeps that follow still
     reproduce the golden FP64 result bit for bit."""

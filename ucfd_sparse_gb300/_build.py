@@ -36,6 +36,7 @@ UNITS = [
     ("legacy.cpp", []),
     ("krylov.cpp", []),
     ("noalloc.cu", []),
+    ("selftest.cu", []),
     ("adjoint.cpp", []),
 ]
 

@@ -121,7 +121,11 @@ def greedy_coloring(nei_ele: np.ndarray):
     return icolor, [int(x) for x in ranges[:nc.value]], lcolor
 
 
-def greedy_coloring_csr(rowptr: np.ndarray, colidx: np.ndarray):
+def greedy_coloring_csr(rowptr: np.ndarray, colidx: np.ndarray, order: str = "index"):
+    """First-fit greedy colouring of a CSR graph -> (icolor, ranges, lcolor).
+
+    order "index" visits cells by index (UCFDGreedyColoringCSR); "bfs" in
+    breadth-first order (UCFDBFSColoringCSR), which needs fewer colours."""
     from ctypes import byref, c_int
     n = rowptr.shape[0] - 1
     rp = np.ascontiguousarray(rowptr, dtype=np.int32)
@@ -130,5 +134,6 @@ def greedy_coloring_csr(rowptr: np.ndarray, colidx: np.ndarray):
     icolor = np.empty(n, dtype=np.int32)
     ranges = np.empty(64, dtype=np.int32)
     nc = c_int()
-    call("UCFDGreedyColoringCSR", n, ptr(rp), ptr(ci), ptr(lcolor), ptr(icolor), ptr(ranges), byref(nc))
+    fn = {"index": "UCFDGreedyColoringCSR", "bfs": "UCFDBFSColoringCSR"}[order]
+    call(fn, n, ptr(rp), ptr(ci), ptr(lcolor), ptr(icolor), ptr(ranges), byref(nc))
     return icolor, [int(x) for x in ranges[:nc.value]], lcolor

@@ -169,6 +169,33 @@ std::vector<int> greedy_color_csr(int n, const int *rowptr, const int *colidx, i
     return col;
 }
 
+std::vector<int> greedy_color_bfs(int n, const int *rowptr, const int *colidx, int *ncolors) {
+    std::vector<int> srp, sci;
+    symmetrize(n, rowptr, colidx, srp, sci);
+    const std::vector<int> rank = bfs_rank(n, rowptr, colidx);
+    std::vector<int> order(n);
+    for (int i = 0; i < n; ++i) order[rank[i]] = i;
+    std::vector<int> col(n, -1);
+    std::vector<int> mark;  // mark[c] == step when colour c is taken by a neighbour
+    int nc = 0;
+    for (int step = 0; step < n; ++step) {
+        const int i = order[step];
+        for (int p = srp[i]; p < srp[i + 1]; ++p) {
+            const int c = col[sci[p]];
+            if (c >= 0) {
+                if ((int)mark.size() <= c) mark.resize(c + 1, -1);
+                mark[c] = step;
+            }
+        }
+        int c = 0;
+        while (c < (int)mark.size() && mark[c] == step) ++c;
+        col[i] = c;
+        if (c + 1 > nc) nc = c + 1;
+    }
+    if (ncolors) *ncolors = nc;
+    return col;
+}
+
 }  // namespace ucfd
 
 // ---------------------------------------------------------------------------
@@ -239,6 +266,16 @@ ucfd_status_t UCFDGreedyColoringCSR(int n, const int *rowptr, const int *colidx,
     UCFD_REQUIRE(n >= 0 && rowptr && colidx, "UCFDGreedyColoringCSR: bad arguments");
     int nc = 0;
     std::vector<int> col = ucfd::greedy_color_csr(n, rowptr, colidx, &nc);
+    color_out(n, col, nc, lcolor, icolor, ranges, ncolors);
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDBFSColoringCSR(int n, const int *rowptr, const int *colidx, int *lcolor, int *icolor,
+                                 int *ranges, int *ncolors) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(n >= 0 && rowptr && colidx, "UCFDBFSColoringCSR: bad arguments");
+    int nc = 0;
+    std::vector<int> col = ucfd::greedy_color_bfs(n, rowptr, colidx, &nc);
     color_out(n, col, nc, lcolor, icolor, ranges, ncolors);
     UCFD_API_END
 }

@@ -29,6 +29,9 @@ Schedule schedule_colored(int n, const int *rowptr, const int *colidx, const int
 // Greedy first-fit colouring in index order (neighbours from the
 // symmetrised graph); returns 0-based colours and the colour count.
 std::vector<int> greedy_color_csr(int n, const int *rowptr, const int *colidx, int *ncolors);
+// First-fit greedy colouring visiting the cells in breadth-first order
+// (bfs_rank): two colours on a bipartite graph such as a hexahedral mesh.
+std::vector<int> greedy_color_bfs(int n, const int *rowptr, const int *colidx, int *ncolors);
 
 // Breadth-first order of the symmetrised graph started from a
 // pseudo-peripheral cell (each connected component in turn): rank[i] is

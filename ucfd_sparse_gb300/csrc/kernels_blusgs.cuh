@@ -290,6 +290,64 @@ __global__ void __launch_bounds__(256) fs_blusgs_sweep_kernel(int t0, int t1, lo
     for (int r = 0; r < B; ++r) du[(var0 + r) * N + k] = b[r];
 }
 
+// FP32 sweep of a small level (a colour of a few thousand cells), where a
+// launch costs one thread's chain of dependent memory round trips rather
+// than bandwidth.  Launched like the DEP form of fs_blusgs_sweep_kernel,
+// but every input the previous launch does not write -- rhs, rv, nei, fa,
+// all PW J blocks and the LU block -- is loaded into registers before
+// griddepcontrol.wait, so after the wait only the neighbour increments
+// are fetched.  Same products and subtractions in the same order.
+template <int B, int PW>
+__global__ void __launch_bounds__(128) fs_blusgs_sweep_small_kernel(int t0, int t1, long long N, int var0,
+                                                                    const int *nei, const float *fa,
+                                                                    const float *rv, const float *J,
+                                                                    const float *LU, const float *rhs,
+                                                                    float *du) {
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    const int k = (t0 & ~31) + blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < t0 || k >= t1) return;
+    constexpr int B2 = B * B;
+    const float *Jk = J + ::ucfd::tile_index(k, 0, (long long)PW * B2);
+    const float *LUk = LU + ::ucfd::tile_index(k, 0, B2);
+    float b[B], fv[PW], jv[PW][B2], lu[B2];
+    int nb[PW];
+#pragma unroll
+    for (int r = 0; r < B; ++r) b[r] = rhs[(var0 + r) * N + k];
+    const float rvk = rv[k];
+#pragma unroll
+    for (int p = 0; p < PW; ++p) {
+        nb[p] = __ldg(nei + p * N + k);
+        fv[p] = __ldg(fa + p * N + k) * rvk;
+#pragma unroll
+        for (int e = 0; e < B2; ++e) jv[p][e] = __ldg(Jk + ((p * B2 + e) << 5));
+    }
+#pragma unroll
+    for (int e = 0; e < B2; ++e) lu[e] = __ldg(LUk + (e << 5));
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    float x[PW][B];
+#pragma unroll
+    for (int p = 0; p < PW; ++p) {
+        const int g = nb[p] >= 0 ? nb[p] : k;
+#pragma unroll
+        for (int c = 0; c < B; ++c) x[p][c] = du[(var0 + c) * N + g];
+    }
+#pragma unroll
+    for (int p = 0; p < PW; ++p) {
+        if (nb[p] >= 0) {
+#pragma unroll
+            for (int r = 0; r < B; ++r) {
+                float val = 0.f;
+#pragma unroll
+                for (int c = 0; c < B; ++c) val += jv[p][r * B + c] * x[p][c];
+                b[r] -= val * fv[p];
+            }
+        }
+    }
+    lusub_dev<float, B>(lu, b);
+#pragma unroll
+    for (int r = 0; r < B; ++r) du[(var0 + r) * N + k] = b[r];
+}
+
 // FP32 block sweep with each tile's J and LU staged in shared memory by
 // bulk asynchronous copies (cp.async.bulk, completed on an mbarrier).
 // Every warp owns a ring of NST tile buffers and walks the level's tiles

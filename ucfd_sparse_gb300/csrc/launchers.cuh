@@ -267,6 +267,29 @@ static void sweep_dep_go(unsigned g, int block, cudaStream_t s, int t0, int t1, 
                                  LU, rhs, du));
 }
 
+// Levels with at most this many cells take the register-hoisted kernel in
+// the dependent-launch variant (FP32): they are bound by one thread's
+// memory latency, not by bandwidth.
+constexpr int kSmallLevel = 16384;
+
+template <int B, int PW>
+static void sweep_small_go(cudaStream_t s, int t0, int t1, long long N, int var0, const int *nei, const float *fa,
+                           const float *rv, const float *J, const float *LU, const float *rhs, float *du) {
+    constexpr int threads = 128;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid_for(t1 - (t0 & ~31), threads));
+    cfg.blockDim = dim3(threads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    UCFD_CUDA(cudaLaunchKernelEx(&cfg, fs_blusgs_sweep_small_kernel<B, PW>, t0, t1, N, var0, nei, fa, rv, J, LU,
+                                 rhs, du));
+}
+
 template <typename S>
 void fs_blusgs_sweep(int B, int t0, int t1, long long N, int P, int var0, const int *nei, const S *fa,
                      const S *rv, const S *J, const S *LU, const S *rhs, S *du, int block,
@@ -283,6 +306,13 @@ void fs_blusgs_sweep(int B, int t0, int t1, long long N, int P, int var0, const 
     // previous launch (its start overlaps the previous colour's tail).
     // All apply the faces in the same order with the same operations.
     if (variant == 4 && (P == 6 || P == 4)) {
+        if constexpr (std::is_same<S, float>::value) {
+            if (B == 5 && t1 - t0 <= kSmallLevel) {
+                if (P == 6) sweep_small_go<5, 6>(s, t0, t1, N, var0, nei, fa, rv, J, LU, rhs, du);
+                else sweep_small_go<5, 4>(s, t0, t1, N, var0, nei, fa, rv, J, LU, rhs, du);
+                return;
+            }
+        }
         if (P == 6) {
             UCFD_BSW(B, (sweep_dep_go<S, BB, 6>(g, block, s, t0, t1, N, P, var0, nei, fa, rv, J, LU, rhs, du)));
         } else {

@@ -38,11 +38,13 @@ SIGNATURES = {
     "UCFDSetConstants": (_I, [_D, _D, _D]),
     "UCFDVersion": (c_char_p, []),
     "UCFDDeviceInfo": (_I, [c_char_p, c_size_t, POINTER(c_int)]),
+    "UCFDSelfTestTimeouts": (_I, [POINTER(c_int), POINTER(c_int)]),
     # ucfdmesh.h
     "UCFDMakeNeiEle": (_I, [_I, _I, _I, _P]),
     "UCFDMakeColoring": (_I, [_I, _I, _I, _P]),
     "UCFDGreedyColoring": (_I, [_I, _I, _P, _P, _P, _P, POINTER(c_int)]),
     "UCFDGreedyColoringCSR": (_I, [_I, _P, _P, _P, _P, _P, POINTER(c_int)]),
+    "UCFDBFSColoringCSR": (_I, [_I, _P, _P, _P, _P, _P, POINTER(c_int)]),
     # ucfdlusgs.h
     "UCFDFlowSysCreate": (_I, [POINTER(c_void_p), _I, _I, _I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
     "UCFDFlowSysSetElement": (_I, [POINTER(c_void_p), _I, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
