@@ -470,6 +470,10 @@ def run_lusgs(args):
                       torch.zeros_like(uu))
         S.set_lusgs(g["fspr"], g["tfspr"])
         S.lusgs_pack(0, 1.0, 0.0)
+        if not args.no_autotune:
+            tuned = S.autotune(reps=2)                   # block size x register build (state restored)
+            tuned.pop("source", None)
+            res.setdefault("launch", tuned)
         hist = np.zeros(args.iters)
         S.lusgs_run(3, 1.0, True, mode, None)          # warm-up (graph capture / occupancy query)
         S.lusgs_pack(0, 1.0, 0.0)
@@ -521,7 +525,7 @@ def run_lusgs(args):
                         "sweep_ms": res["sweep_ms"], "algorithmic_bytes_per_sweep": sweep_bytes_},
            "loop_frac_of_peak": bytes_iter * args.iters / (best * 1e-3) / 1e9 / peak,
            "resid_fp64": [res[0]["resid_first"], res[0]["resid_last"]],
-           "clocks": res[0]["clocks"], "generation_s": gen_s}
+           "clocks": res[0]["clocks"], "generation_s": gen_s, "launch": res.get("launch")}
     print(json.dumps(out))
 
 

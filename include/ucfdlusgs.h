@@ -108,7 +108,9 @@ typedef struct {
                               2 / 3 FP32 5x5 with J and LU tiles staged in shared memory
                               by bulk copies (2 / 1 buffers per warp; ELL width 6 or 4),
                               4 = 0 launched as a programmatic dependent of the previous
-                              colour (its start overlaps the previous colour's tail) */
+                              colour (its start overlaps the previous colour's tail);
+                              scalar sweeps: 0 default build, 1 capped at 64 registers
+                              (more resident warps) */
     int run_mode;          /* UCFDLUSGS_Run with mode -1: 0 CUDA graph, 1 persistent kernel */
     double ms;             /* Autotune: time of the best candidate (one sweep pair, or one
                               Run iteration for scalar LU-SGS); 0 when set by hand */

@@ -254,6 +254,7 @@ void lusgs_sweep(FlowSys s, bool rans, bool upper, double kappa, bool persistent
     a.gamma = (S)constants().gamma;
     a.pmin = (S)constants().pmin;
     a.upper = upper ? 1 : 0;
+    a.regcap = s->variant == 1 ? 1 : 0;  // scalar sweeps: variant 1 = 64-register build
     const int L = s->sch.nlev;
     if (persistent) {
         // one cooperative launch per sweep, bounded grid barrier between levels
@@ -734,20 +735,24 @@ ucfd_status_t UCFDFlowSysAutotune(FlowSys s, int reps, UCFDLaunchConfig *best) {
                 UCFD_CUDA(cudaMemcpyAsync(slam.p, w.lamN.p, nl * sizeof(S), cudaMemcpyDeviceToDevice, st));
             }
             run_gather_lambda<S>(s, false, 1);
-            for (int b : kTuneBlocks) {
-                s->block = b;
+            // variant 0: unconstrained registers; 1: 64-register build
+            for (int v = 0; v <= 1; ++v) {
+                s->variant = v;
+                for (int b : kTuneBlocks) {
+                    s->block = b;
+                    run_graph_drop(s);
+                    run_graph_build<S, EX>(s, false, 1.0);
+                    const double ms = time_ms(st, reps, [&] { UCFD_CUDA(cudaGraphLaunch(s->run_exec, st)); });
+                    consider(ms, b, v, 0);
+                }
                 run_graph_drop(s);
-                run_graph_build<S, EX>(s, false, 1.0);
-                const double ms = time_ms(st, reps, [&] { UCFD_CUDA(cudaGraphLaunch(s->run_exec, st)); });
-                consider(ms, b, s->variant, 0);
+                // the persistent kernel has its own fixed launch shape
+                run_persistent_begin(s);
+                const double pms =
+                    time_ms(st, reps, [&] { lusgs_iteration<S, EX>(s, false, 1.0, s->red.p, true); });
+                run_persistent_check(s);
+                consider(pms, 256, v, 1);
             }
-            run_graph_drop(s);
-            // the persistent kernel has its own fixed launch shape
-            run_persistent_begin(s);
-            const double pms =
-                time_ms(st, reps, [&] { lusgs_iteration<S, EX>(s, false, 1.0, s->red.p, true); });
-            run_persistent_check(s);
-            consider(pms, best_block, s->variant, 1);
             UCFD_CUDA(cudaMemcpyAsync(w.u.p, su.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
             UCFD_CUDA(cudaMemcpyAsync(w.du.p, sdu.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
             UCFD_CUDA(cudaMemcpyAsync(w.diag.p, sdiag.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));

@@ -43,6 +43,7 @@ struct ScalarSweepArgs {
     long long diag_vs;
     T kappa, gamma, pmin;
     int upper;
+    int regcap;            // 1: the kernel built for 4 blocks of 256 threads per SM (64 registers)
 };
 
 // One colour of a transposed (adjoint) colored LU-SGS sweep.

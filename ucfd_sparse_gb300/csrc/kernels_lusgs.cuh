@@ -60,8 +60,11 @@ using ScalarSweepArgs = ::ucfd::ScalarSweepArgs<T>;
 template <typename T, int NV, int NFV, int NDIMS, bool RANS, bool COHERENT = false>
 __device__ __forceinline__ void scalar_sweep_cell(const ScalarSweepArgs<T> &a, int t);
 
-template <typename T, int NV, int NFV, int NDIMS, bool RANS>
-__global__ void __launch_bounds__(256) scalar_sweep_kernel(ScalarSweepArgs<T> a) {
+// MINB: minimum resident blocks of 256 threads per SM the compiler must
+// allow (1: no register cap, about 85 registers; 4: 64 registers, twice
+// the warps to cover the gathers' latency, a few spilled bytes).
+template <typename T, int NV, int NFV, int NDIMS, bool RANS, int MINB = 1>
+__global__ void __launch_bounds__(256, MINB) scalar_sweep_kernel(ScalarSweepArgs<T> a) {
     const int t = a.t0 + blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.t1) return;
     scalar_sweep_cell<T, NV, NFV, NDIMS, RANS>(a, t);
@@ -109,8 +112,8 @@ __device__ inline bool grid_barrier_bounded(unsigned *count, unsigned *gen, int 
 // One whole sweep (every level, ascending or descending) in one
 // cooperative launch: the blocks stride over the cells of a level, then
 // meet at the bounded grid barrier before the next level.
-template <typename T, int NV, int NFV, int NDIMS, bool RANS>
-__global__ void __launch_bounds__(256) scalar_sweep_persistent_kernel(ScalarSweepArgs<T> a, const int *lev_off,
+template <typename T, int NV, int NFV, int NDIMS, bool RANS, int MINB = 1>
+__global__ void __launch_bounds__(256, MINB) scalar_sweep_persistent_kernel(ScalarSweepArgs<T> a, const int *lev_off,
                                                                       int nlev, unsigned *bar, int *err,
                                                                       long long max_spin) {
     for (int q = 0; q < nlev; ++q) {
@@ -140,11 +143,16 @@ __device__ __forceinline__ void scalar_sweep_cell(const ScalarSweepArgs<T> &a, i
     const T rvi = a.rv ? __ldg(a.rv + i) : T(1);
 
     // Faces are handled FB at a time: the neighbour indices, then the
-    // colour tests, then every gather of the batch are issued before any
-    // flux is evaluated (latency hiding); the accumulation into df keeps
-    // the reference's face order.
-    constexpr int FB = sizeof(T) == 4 ? 6 : 3;
-    for (int f0 = 0; f0 < a.nface; f0 += FB) {
+    // colour tests, then every gather of an active face of the batch are
+    // issued before any flux is evaluated (latency hiding); inactive faces
+    // load nothing, and the accumulation into df keeps the reference's
+    // face order.  Three faces per batch keep the kernel near 80 registers
+    // (occupancy for the gathers' latency).  In the level-major layout the
+    // first level of a lower sweep and the last of an upper sweep have no
+    // active face at all and skip the loop.
+    constexpr int FB = 3;
+    const bool none = !a.lcolor && (a.upper ? a.hi >= ld : a.lo <= 0);
+    for (int f0 = 0; f0 < (none ? 0 : a.nface); f0 += FB) {
         int nb[FB];
         bool act[FB];
 #pragma unroll
@@ -161,7 +169,8 @@ __device__ __forceinline__ void scalar_sweep_cell(const ScalarSweepArgs<T> &a, i
         T uu[FB][NV], dn[FB][DNV], nf[FB][NDIMS], fv[FB], kl[FB];
 #pragma unroll
         for (int q = 0; q < FB; ++q) {
-            const int g = act[q] ? nb[q] : i;
+            if (!act[q]) continue;
+            const int g = nb[q];
 #pragma unroll
             for (int v = 0; v < NV; ++v) {
                 // only the variables the flux reads are loaded
@@ -171,7 +180,7 @@ __device__ __forceinline__ void scalar_sweep_cell(const ScalarSweepArgs<T> &a, i
 #pragma unroll
             for (int k = 0; k < DNV; ++k)
                 dn[q][k] = COHERENT ? __ldcg(a.nbsrc + (k + NV0) * ld + g) : a.nbsrc[(k + NV0) * ld + g];
-            const int f = act[q] ? f0 + q : 0;
+            const int f = f0 + q;
 #pragma unroll
             for (int d = 0; d < NDIMS; ++d) nf[q][d] = __ldg(a.nrm + (f * NDIMS + d) * ld + i);
             fv[q] = __ldg(a.fa + f * ld + i);

@@ -49,7 +49,10 @@ template <typename T, int NV, int NFV, int NDIMS, bool RANS>
 static void sweep_go(const ::ucfd::ScalarSweepArgs<T> &a, int block, cudaStream_t s) {
     const long long n = a.t1 - a.t0;
     if (n <= 0) return;
-    scalar_sweep_kernel<T, NV, NFV, NDIMS, RANS><<<grid_for(n, block), block, 0, s>>>(a);
+    if (a.regcap)
+        scalar_sweep_kernel<T, NV, NFV, NDIMS, RANS, 4><<<grid_for(n, block), block, 0, s>>>(a);
+    else
+        scalar_sweep_kernel<T, NV, NFV, NDIMS, RANS, 1><<<grid_for(n, block), block, 0, s>>>(a);
 }
 
 template <typename T>
@@ -77,10 +80,10 @@ void scalar_sweep(const ::ucfd::ScalarSweepArgs<T> &a, int nv, int nfv, int ndim
                  nv, nfv, ndims, rans ? "RANS" : "NS");
 }
 
-template <typename T, int NV, int NFV, int NDIMS, bool RANS>
-static void persistent_go(const ::ucfd::ScalarSweepArgs<T> &a, const int *lev_off, int nlev, unsigned *bar,
-                          int *err, long long max_spin, cudaStream_t s) {
-    auto kern = scalar_sweep_persistent_kernel<T, NV, NFV, NDIMS, RANS>;
+template <typename T, int NV, int NFV, int NDIMS, bool RANS, int MINB>
+static void persistent_minb_go(const ::ucfd::ScalarSweepArgs<T> &a, const int *lev_off, int nlev, unsigned *bar,
+                               int *err, long long max_spin, cudaStream_t s) {
+    auto kern = scalar_sweep_persistent_kernel<T, NV, NFV, NDIMS, RANS, MINB>;
     static int grid = 0;  // per instantiation: blocks that fit co-resident
     if (!grid) {
         int per_sm = 0, dev = 0, sms = 0;
@@ -93,6 +96,13 @@ static void persistent_go(const ::ucfd::ScalarSweepArgs<T> &a, const int *lev_of
     ::ucfd::ScalarSweepArgs<T> aa = a;
     void *args[] = {(void *)&aa, (void *)&lev_off, (void *)&nlev, (void *)&bar, (void *)&err, (void *)&max_spin};
     UCFD_CUDA(cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(kBlock), args, 0, s));
+}
+
+template <typename T, int NV, int NFV, int NDIMS, bool RANS>
+static void persistent_go(const ::ucfd::ScalarSweepArgs<T> &a, const int *lev_off, int nlev, unsigned *bar,
+                          int *err, long long max_spin, cudaStream_t s) {
+    if (a.regcap) persistent_minb_go<T, NV, NFV, NDIMS, RANS, 4>(a, lev_off, nlev, bar, err, max_spin, s);
+    else persistent_minb_go<T, NV, NFV, NDIMS, RANS, 1>(a, lev_off, nlev, bar, err, max_spin, s);
 }
 
 // Whole sweep (all nlev levels) as one cooperative launch with a bounded
