@@ -507,8 +507,11 @@ def run_lusgs(args):
     best = min(res[0]["ms"], res[1]["ms"])
     rp = c["rowptr"]
     nnz = int(rp[-1])
-    # NS lower sweep algorithmic bytes: faces' index + active half of the geometry, own/nbr state
-    sweep_bytes_ = nnz * 4 + (nnz // 2) * (5 * 4) + N * (4 + 5 * 4 + 3 * 5 * 4 + 5 * 4)
+    # NS sweep algorithmic bytes, every array element once at storage precision:
+    # per cell-face neighbour index, area, spectral radius, 3 normal components;
+    # per cell rcp_vol and 4 x nvars state values (u and du of neighbours as
+    # other cells' own data, du read and written, diag) -- 228 B/cell on hex
+    sweep_bytes_ = nnz * (4 + (2 + 3) * 4) + N * (4 + 4 * 5 * 4)
     out = {"workload": "lusgs", "metric": METRIC, "unit": UNIT,
            "config": {"workload": f"scalar LU-SGS pseudo-time loop, {m}^3 jittered permuted hex ({N} cells), "
                                   f"nvars 5 + 1 RANS, FP32, greedy colouring ({len(rg)} colours), "

@@ -109,8 +109,8 @@ typedef struct {
                               by bulk copies (2 / 1 buffers per warp; ELL width 6 or 4),
                               4 = 0 launched as a programmatic dependent of the previous
                               colour (its start overlaps the previous colour's tail);
-                              scalar sweeps: 0 default build, 1 capped at 64 registers
-                              (more resident warps) */
+                              scalar sweeps: 0 default build, 1 / 2 capped at 80 / 64
+                              registers (more resident warps) */
     int run_mode;          /* UCFDLUSGS_Run with mode -1: 0 CUDA graph, 1 persistent kernel */
     double ms;             /* Autotune: time of the best candidate (one sweep pair, or one
                               Run iteration for scalar LU-SGS); 0 when set by hand */

@@ -254,7 +254,8 @@ void lusgs_sweep(FlowSys s, bool rans, bool upper, double kappa, bool persistent
     a.gamma = (S)constants().gamma;
     a.pmin = (S)constants().pmin;
     a.upper = upper ? 1 : 0;
-    a.regcap = s->variant == 1 ? 1 : 0;  // scalar sweeps: variant 1 = 64-register build
+    // scalar sweeps: variant 1 / 2 = the builds for 3 / 4 resident blocks of 256 per SM
+    a.regcap = s->variant == 1 ? 3 : s->variant == 2 ? 4 : 0;
     const int L = s->sch.nlev;
     if (persistent) {
         // one cooperative launch per sweep, bounded grid barrier between levels
@@ -735,8 +736,8 @@ ucfd_status_t UCFDFlowSysAutotune(FlowSys s, int reps, UCFDLaunchConfig *best) {
                 UCFD_CUDA(cudaMemcpyAsync(slam.p, w.lamN.p, nl * sizeof(S), cudaMemcpyDeviceToDevice, st));
             }
             run_gather_lambda<S>(s, false, 1);
-            // variant 0: unconstrained registers; 1: 64-register build
-            for (int v = 0; v <= 1; ++v) {
+            // variant 0: unconstrained registers; 1 / 2: at most 80 / 64 registers
+            for (int v = 0; v <= 2; ++v) {
                 s->variant = v;
                 for (int b : kTuneBlocks) {
                     s->block = b;

@@ -43,7 +43,8 @@ struct ScalarSweepArgs {
     long long diag_vs;
     T kappa, gamma, pmin;
     int upper;
-    int regcap;            // 1: the kernel built for 4 blocks of 256 threads per SM (64 registers)
+    int regcap;            // 0, or 3 / 4: the kernel built for that many blocks of 256 threads per SM
+                           // (at most 80 / 64 registers)
 };
 
 // One colour of a transposed (adjoint) colored LU-SGS sweep.

@@ -61,8 +61,9 @@ template <typename T, int NV, int NFV, int NDIMS, bool RANS, bool COHERENT = fal
 __device__ __forceinline__ void scalar_sweep_cell(const ScalarSweepArgs<T> &a, int t);
 
 // MINB: minimum resident blocks of 256 threads per SM the compiler must
-// allow (1: no register cap, about 85 registers; 4: 64 registers, twice
-// the warps to cover the gathers' latency, a few spilled bytes).
+// allow (1: no register cap, about 106 registers; 3 / 4: at most 80 / 64
+// registers, more warps to cover the gathers' latency for a few spilled
+// bytes).  The autotuner picks.
 template <typename T, int NV, int NFV, int NDIMS, bool RANS, int MINB = 1>
 __global__ void __launch_bounds__(256, MINB) scalar_sweep_kernel(ScalarSweepArgs<T> a) {
     const int t = a.t0 + blockIdx.x * blockDim.x + threadIdx.x;
@@ -137,26 +138,28 @@ __device__ __forceinline__ void scalar_sweep_cell(const ScalarSweepArgs<T> &a, i
     const int i = a.cells ? __ldg(a.cells + t) : t;
     const int ci = a.lcolor ? __ldg(a.lcolor + i) : 0;
 
-    T df[DNV];
+    // the cell's own inputs first (independent of every gather)
+    T own[DNV], dg[DNV], df[DNV];
 #pragma unroll
-    for (int k = 0; k < DNV; ++k) df[k] = T(0);
+    for (int k = 0; k < DNV; ++k) {
+        own[k] = a.own_in[(k + NV0) * ld + i];
+        dg[k] = a.diag[(k + NV0) * a.diag_vs + i];
+        df[k] = T(0);
+    }
     const T rvi = a.rv ? __ldg(a.rv + i) : T(1);
 
-    // Faces are handled FB at a time: the neighbour indices, then the
-    // colour tests, then every gather of an active face of the batch are
-    // issued before any flux is evaluated (latency hiding); inactive faces
-    // load nothing, and the accumulation into df keeps the reference's
-    // face order.  Three faces per batch keep the kernel near 80 registers
-    // (occupancy for the gathers' latency).  In the level-major layout the
-    // first level of a lower sweep and the last of an upper sweep have no
-    // active face at all and skip the loop.
+    // Faces are handled FB at a time: the colour tests, then every gather
+    // of an active face of the batch are issued before any flux is
+    // evaluated (latency hiding); inactive faces load nothing, and the
+    // accumulation into df keeps the reference's face order.  Three faces
+    // per batch keep the kernel near 80 registers (occupancy for the
+    // gathers' latency).  In the level-major layout the first level of a
+    // lower sweep and the last of an upper sweep have no active face at all
+    // and skip the faces.
     constexpr int FB = 3;
     const bool none = !a.lcolor && (a.upper ? a.hi >= ld : a.lo <= 0);
-    for (int f0 = 0; f0 < (none ? 0 : a.nface); f0 += FB) {
-        int nb[FB];
+    auto batch = [&](int f0, const int *nb) {
         bool act[FB];
-#pragma unroll
-        for (int q = 0; q < FB; ++q) nb[q] = (f0 + q < a.nface) ? __ldg(a.nei + (f0 + q) * ld + i) : -1;
 #pragma unroll
         for (int q = 0; q < FB; ++q) {
             if (a.lcolor) {
@@ -213,15 +216,30 @@ __device__ __forceinline__ void scalar_sweep_cell(const ScalarSweepArgs<T> &a, i
                 df[k] += (dfj - klq * dn[q][k]) * fvq;
             }
         }
+    };
+    if (none) {
+    } else if (a.nface <= 2 * FB) {
+        // every neighbour index of the cell up front, two unrolled batches
+        int nba[2 * FB];
+#pragma unroll
+        for (int p = 0; p < 2 * FB; ++p) nba[p] = p < a.nface ? __ldg(a.nei + p * ld + i) : -1;
+        batch(0, nba);
+        if (a.nface > FB) batch(FB, nba + FB);
+    } else {
+        for (int f0 = 0; f0 < a.nface; f0 += FB) {
+            int nb[FB];
+#pragma unroll
+            for (int q = 0; q < FB; ++q) nb[q] = (f0 + q < a.nface) ? __ldg(a.nei + (f0 + q) * ld + i) : -1;
+            batch(f0, nb);
+        }
     }
 #pragma unroll
     for (int k = 0; k < DNV; ++k) {
         const long long l = (k + NV0) * ld + i;
-        const T dg = a.diag[(k + NV0) * a.diag_vs + i];
         if (!a.upper)
-            a.own_out[l] = (a.own_in[l] - T(0.5) * df[k]) / dg;
+            a.own_out[l] = (own[k] - T(0.5) * df[k]) / dg[k];
         else
-            a.own_out[l] = a.own_in[l] - (T(0.5) * df[k] / dg);
+            a.own_out[l] = own[k] - (T(0.5) * df[k] / dg[k]);
     }
 }
 

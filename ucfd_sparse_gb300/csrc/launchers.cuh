@@ -49,8 +49,10 @@ template <typename T, int NV, int NFV, int NDIMS, bool RANS>
 static void sweep_go(const ::ucfd::ScalarSweepArgs<T> &a, int block, cudaStream_t s) {
     const long long n = a.t1 - a.t0;
     if (n <= 0) return;
-    if (a.regcap)
+    if (a.regcap == 4)
         scalar_sweep_kernel<T, NV, NFV, NDIMS, RANS, 4><<<grid_for(n, block), block, 0, s>>>(a);
+    else if (a.regcap == 3)
+        scalar_sweep_kernel<T, NV, NFV, NDIMS, RANS, 3><<<grid_for(n, block), block, 0, s>>>(a);
     else
         scalar_sweep_kernel<T, NV, NFV, NDIMS, RANS, 1><<<grid_for(n, block), block, 0, s>>>(a);
 }
@@ -101,7 +103,8 @@ static void persistent_minb_go(const ::ucfd::ScalarSweepArgs<T> &a, const int *l
 template <typename T, int NV, int NFV, int NDIMS, bool RANS>
 static void persistent_go(const ::ucfd::ScalarSweepArgs<T> &a, const int *lev_off, int nlev, unsigned *bar,
                           int *err, long long max_spin, cudaStream_t s) {
-    if (a.regcap) persistent_minb_go<T, NV, NFV, NDIMS, RANS, 4>(a, lev_off, nlev, bar, err, max_spin, s);
+    if (a.regcap == 4) persistent_minb_go<T, NV, NFV, NDIMS, RANS, 4>(a, lev_off, nlev, bar, err, max_spin, s);
+    else if (a.regcap == 3) persistent_minb_go<T, NV, NFV, NDIMS, RANS, 3>(a, lev_off, nlev, bar, err, max_spin, s);
     else persistent_minb_go<T, NV, NFV, NDIMS, RANS, 1>(a, lev_off, nlev, bar, err, max_spin, s);
 }
 
