@@ -83,6 +83,28 @@ def test_blusgs_autotune_keeps_golden(golden, ucfd):
     np.testing.assert_array_equal(host(e["res"]), arr["blu10_resid"])
 
 
+@pytest.mark.parametrize("prec", [0, 2])
+def test_scalar_sweep_variants_identical(prec, golden, ucfd):
+    """The five scalar sweep builds (one thread per cell with 3 register
+    budgets, two threads per cell with 2) give the same result; in FP64 it
+    is the golden oracle result bit for bit."""
+    from tests.test_gpu_lusgs import flowsys_step
+    meta, arr = golden
+    name = "fs9"
+    kw = cases.FLOWSYS[name]
+    fs, inp = cases.flowsys_case(**kw)
+    outs = []
+    for var in range(5):
+        S, e = make_flowsys(fs, inp, prec=prec, on_device=True)
+        S.set_launch_config(threads_per_block=128, sweep_variant=var)
+        flowsys_step(S, kw, kw["nsteps"])
+        outs.append(e["upts"].cpu().numpy())
+    for o in outs[1:]:
+        np.testing.assert_array_equal(o, outs[0])
+    if prec == 0:
+        np.testing.assert_array_equal(outs[0], arr[f"{name}_upts"])
+
+
 def test_lusgs_autotune_restores_state(ucfd):
     """Scalar autotune times the Run loop on the packed state and restores
     it: Run(mode=-1) afterwards equals Run on an untuned system."""

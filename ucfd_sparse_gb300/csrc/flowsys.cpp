@@ -254,8 +254,10 @@ void lusgs_sweep(FlowSys s, bool rans, bool upper, double kappa, bool persistent
     a.gamma = (S)constants().gamma;
     a.pmin = (S)constants().pmin;
     a.upper = upper ? 1 : 0;
-    // scalar sweeps: variant 1 / 2 = the builds for 3 / 4 resident blocks of 256 per SM
-    a.regcap = s->variant == 1 ? 3 : s->variant == 2 ? 4 : 0;
+    // scalar sweeps: variant 1 / 2 = the builds for 3 / 4 resident blocks of
+    // 256 per SM; 3 / 4 = two threads per cell, default / 64-register build
+    a.regcap = (s->variant == 1) ? 3 : (s->variant == 2 || s->variant == 4) ? 4 : 0;
+    a.pair = (s->variant == 3 || s->variant == 4) ? 1 : 0;
     const int L = s->sch.nlev;
     if (persistent) {
         // one cooperative launch per sweep, bounded grid barrier between levels
@@ -736,8 +738,9 @@ ucfd_status_t UCFDFlowSysAutotune(FlowSys s, int reps, UCFDLaunchConfig *best) {
                 UCFD_CUDA(cudaMemcpyAsync(slam.p, w.lamN.p, nl * sizeof(S), cudaMemcpyDeviceToDevice, st));
             }
             run_gather_lambda<S>(s, false, 1);
-            // variant 0: unconstrained registers; 1 / 2: at most 80 / 64 registers
-            for (int v = 0; v <= 2; ++v) {
+            // variant 0: unconstrained registers; 1 / 2: at most 80 / 64 registers;
+            // 3 / 4: two threads per cell (the persistent kernel stays one per cell)
+            for (int v = 0; v <= 4; ++v) {
                 s->variant = v;
                 for (int b : kTuneBlocks) {
                     s->block = b;
@@ -747,6 +750,7 @@ ucfd_status_t UCFDFlowSysAutotune(FlowSys s, int reps, UCFDLaunchConfig *best) {
                     consider(ms, b, v, 0);
                 }
                 run_graph_drop(s);
+                if (v > 2) continue;
                 // the persistent kernel has its own fixed launch shape
                 run_persistent_begin(s);
                 const double pms =

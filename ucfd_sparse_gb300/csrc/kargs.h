@@ -45,6 +45,7 @@ struct ScalarSweepArgs {
     int upper;
     int regcap;            // 0, or 3 / 4: the kernel built for that many blocks of 256 threads per SM
                            // (at most 80 / 64 registers)
+    int pair;              // 1: two threads per cell (faces 0-2 / 3-5; ELL width <= 6, per-level launches)
 };
 
 // One colour of a transposed (adjoint) colored LU-SGS sweep.

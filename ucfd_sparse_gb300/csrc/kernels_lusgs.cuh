@@ -130,6 +130,97 @@ __global__ void __launch_bounds__(256, MINB) scalar_sweep_persistent_kernel(Scal
     }
 }
 
+// x * y rounded on its own (never fused into a following add), so that
+// every sweep kernel forms the same per-face term whatever the compiler
+// contracts; with contraction off this is the plain product.
+__device__ __forceinline__ float mul_rn(float x, float y) { return __fmul_rn(x, y); }
+__device__ __forceinline__ double mul_rn(double x, double y) { return __dmul_rn(x, y); }
+
+// Faces f0 .. f0+FB-1 of cell i (neighbours nb[]): the colour / level test,
+// every gather of an active face before any flux is evaluated (latency
+// hiding; inactive faces load nothing), then each active face's term
+// ((F(u+du) - F(u)) - kappa lam du) * area * rcp_vol of lusgs.c:143-205,
+// added to df in face order (ACC) or stored in c[q][k] for the caller to
+// add in face order.
+template <typename T, int NV, int NFV, int NDIMS, bool RANS, bool COHERENT, int FB, bool ACC>
+__device__ __forceinline__ void face_terms(const ScalarSweepArgs<T> &a, int i, int ci, T rvi, int f0,
+                                           const int *nb, bool *act, T (*c)[RANS ? NV - NFV : NFV], T *df) {
+    constexpr int NV0 = RANS ? NFV : 0;
+    constexpr int DNV = RANS ? NV - NFV : NFV;
+    const long long ld = a.ld;
+#pragma unroll
+    for (int q = 0; q < FB; ++q) {
+        if (a.lcolor) {
+            const int cn = nb[q] >= 0 ? __ldg(a.lcolor + nb[q]) : ci;
+            act[q] = a.upper ? (cn > ci) : (cn < ci);
+        } else {
+            act[q] = nb[q] >= 0 && (a.upper ? (nb[q] >= a.hi) : (nb[q] < a.lo));
+        }
+    }
+    T uu[FB][NV], dn[FB][DNV], nf[FB][NDIMS], fv[FB], kl[FB];
+#pragma unroll
+    for (int q = 0; q < FB; ++q) {
+        if (!act[q]) continue;
+        const int g = nb[q];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            // only the variables the flux reads are loaded
+            const bool need = RANS ? (v <= NDIMS || v >= NFV) : (v < NFV);
+            uu[q][v] = need ? __ldg(a.u + v * ld + g) : T(0);
+        }
+#pragma unroll
+        for (int k = 0; k < DNV; ++k)
+            dn[q][k] = COHERENT ? __ldcg(a.nbsrc + (k + NV0) * ld + g) : a.nbsrc[(k + NV0) * ld + g];
+        const int f = f0 + q;
+#pragma unroll
+        for (int d = 0; d < NDIMS; ++d) nf[q][d] = __ldg(a.nrm + (f * NDIMS + d) * ld + i);
+        fv[q] = __ldg(a.fa + f * ld + i);
+        kl[q] = __ldg(a.lam + f * ld + i);
+    }
+#pragma unroll
+    for (int q = 0; q < FB; ++q) {
+        if (!act[q]) continue;
+        T *u = uu[q];
+        T du[NV], f0v[DNV], f1v[DNV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) du[v] = T(0);
+#pragma unroll
+        for (int k = 0; k < DNV; ++k) du[k + NV0] = dn[q][k];
+        const T fvq = a.rv ? fv[q] * rvi : fv[q];
+        // diff_flux: lusgs.c:143-155 (du += u before either flux)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) du[v] += u[v];
+        if constexpr (RANS) {
+            rans_flux<T, NFV, NDIMS, NV - NFV>(u, nf[q], f0v);
+            rans_flux<T, NFV, NDIMS, NV - NFV>(du, nf[q], f1v);
+        } else {
+            ns_flux<T, NFV, NDIMS>(a.gamma, a.pmin, u, nf[q], f0v);
+            ns_flux<T, NFV, NDIMS>(a.gamma, a.pmin, du, nf[q], f1v);
+        }
+        const T klq = a.kappa * kl[q];
+#pragma unroll
+        for (int k = 0; k < DNV; ++k) {
+            const T dfj = f1v[k] - f0v[k];
+            const T term = mul_rn(dfj - klq * dn[q][k], fvq);
+            if constexpr (ACC) df[k] += term;
+            else c[q][k] = term;
+        }
+    }
+}
+
+// In the level-major layout the first level of a lower sweep and the last
+// of an upper sweep have no active face at all.
+template <typename T>
+__device__ __forceinline__ bool no_active_face(const ScalarSweepArgs<T> &a) {
+    return !a.lcolor && (a.upper ? a.hi >= a.ld : a.lo <= 0);
+}
+
+// The cell's new increment from its own input, diagonal and df.
+template <typename T>
+__device__ __forceinline__ T sweep_result(bool upper, T own, T df, T dg) {
+    return !upper ? (own - T(0.5) * df) / dg : own - (T(0.5) * df / dg);
+}
+
 template <typename T, int NV, int NFV, int NDIMS, bool RANS, bool COHERENT>
 __device__ __forceinline__ void scalar_sweep_cell(const ScalarSweepArgs<T> &a, int t) {
     constexpr int NV0 = RANS ? NFV : 0;
@@ -148,76 +239,14 @@ __device__ __forceinline__ void scalar_sweep_cell(const ScalarSweepArgs<T> &a, i
     }
     const T rvi = a.rv ? __ldg(a.rv + i) : T(1);
 
-    // Faces are handled FB at a time: the colour tests, then every gather
-    // of an active face of the batch are issued before any flux is
-    // evaluated (latency hiding); inactive faces load nothing, and the
-    // accumulation into df keeps the reference's face order.  Three faces
-    // per batch keep the kernel near 80 registers (occupancy for the
-    // gathers' latency).  In the level-major layout the first level of a
-    // lower sweep and the last of an upper sweep have no active face at all
-    // and skip the faces.
+    // Faces three at a time (about 80 registers: occupancy for the gathers'
+    // latency); the terms are added to df in the reference's face order.
     constexpr int FB = 3;
-    const bool none = !a.lcolor && (a.upper ? a.hi >= ld : a.lo <= 0);
     auto batch = [&](int f0, const int *nb) {
         bool act[FB];
-#pragma unroll
-        for (int q = 0; q < FB; ++q) {
-            if (a.lcolor) {
-                const int cn = nb[q] >= 0 ? __ldg(a.lcolor + nb[q]) : ci;
-                act[q] = a.upper ? (cn > ci) : (cn < ci);
-            } else {
-                act[q] = nb[q] >= 0 && (a.upper ? (nb[q] >= a.hi) : (nb[q] < a.lo));
-            }
-        }
-        T uu[FB][NV], dn[FB][DNV], nf[FB][NDIMS], fv[FB], kl[FB];
-#pragma unroll
-        for (int q = 0; q < FB; ++q) {
-            if (!act[q]) continue;
-            const int g = nb[q];
-#pragma unroll
-            for (int v = 0; v < NV; ++v) {
-                // only the variables the flux reads are loaded
-                const bool need = RANS ? (v <= NDIMS || v >= NFV) : (v < NFV);
-                uu[q][v] = need ? __ldg(a.u + v * ld + g) : T(0);
-            }
-#pragma unroll
-            for (int k = 0; k < DNV; ++k)
-                dn[q][k] = COHERENT ? __ldcg(a.nbsrc + (k + NV0) * ld + g) : a.nbsrc[(k + NV0) * ld + g];
-            const int f = f0 + q;
-#pragma unroll
-            for (int d = 0; d < NDIMS; ++d) nf[q][d] = __ldg(a.nrm + (f * NDIMS + d) * ld + i);
-            fv[q] = __ldg(a.fa + f * ld + i);
-            kl[q] = __ldg(a.lam + f * ld + i);
-        }
-#pragma unroll
-        for (int q = 0; q < FB; ++q) {
-            if (!act[q]) continue;
-            T *u = uu[q];
-            T du[NV], f0v[DNV], f1v[DNV];
-#pragma unroll
-            for (int v = 0; v < NV; ++v) du[v] = T(0);
-#pragma unroll
-            for (int k = 0; k < DNV; ++k) du[k + NV0] = dn[q][k];
-            const T fvq = a.rv ? fv[q] * rvi : fv[q];
-            // diff_flux: lusgs.c:143-155 (du += u before either flux)
-#pragma unroll
-            for (int v = 0; v < NV; ++v) du[v] += u[v];
-            if constexpr (RANS) {
-                rans_flux<T, NFV, NDIMS, NV - NFV>(u, nf[q], f0v);
-                rans_flux<T, NFV, NDIMS, NV - NFV>(du, nf[q], f1v);
-            } else {
-                ns_flux<T, NFV, NDIMS>(a.gamma, a.pmin, u, nf[q], f0v);
-                ns_flux<T, NFV, NDIMS>(a.gamma, a.pmin, du, nf[q], f1v);
-            }
-            const T klq = a.kappa * kl[q];
-#pragma unroll
-            for (int k = 0; k < DNV; ++k) {
-                const T dfj = f1v[k] - f0v[k];
-                df[k] += (dfj - klq * dn[q][k]) * fvq;
-            }
-        }
+        face_terms<T, NV, NFV, NDIMS, RANS, COHERENT, FB, true>(a, i, ci, rvi, f0, nb, act, nullptr, df);
     };
-    if (none) {
+    if (no_active_face(a)) {
     } else if (a.nface <= 2 * FB) {
         // every neighbour index of the cell up front, two unrolled batches
         int nba[2 * FB];
@@ -234,13 +263,73 @@ __device__ __forceinline__ void scalar_sweep_cell(const ScalarSweepArgs<T> &a, i
         }
     }
 #pragma unroll
-    for (int k = 0; k < DNV; ++k) {
-        const long long l = (k + NV0) * ld + i;
-        if (!a.upper)
-            a.own_out[l] = (own[k] - T(0.5) * df[k]) / dg[k];
-        else
-            a.own_out[l] = own[k] - (T(0.5) * df[k] / dg[k]);
+    for (int k = 0; k < DNV; ++k) a.own_out[(k + NV0) * ld + i] = sweep_result(a.upper != 0, own[k], df[k], dg[k]);
+}
+
+// Two threads per cell (ELL width <= 6, level-major or coloured): the even
+// lane takes faces 0-2, the odd lane faces 3-5, each with its gathers and
+// fluxes; the odd lane hands its three terms to the even lane (warp
+// shuffles), which adds all six in face order and writes the cell.  Half
+// the dependent memory chain per thread and twice the threads in flight.
+// Same terms, same order as scalar_sweep_cell.
+template <typename T, int NV, int NFV, int NDIMS, bool RANS, int MINB = 1>
+__global__ void __launch_bounds__(256, MINB) scalar_sweep_pair_kernel(ScalarSweepArgs<T> a) {
+    constexpr int NV0 = RANS ? NFV : 0;
+    constexpr int DNV = RANS ? NV - NFV : NFV;
+    constexpr int FB = 3;
+    const long long ld = a.ld;
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int h = (int)(tid & 1);
+    const long long t = a.t0 + (tid >> 1);
+    const bool live = t < a.t1;  // both lanes of a pair agree
+    const int i = live ? (a.cells ? __ldg(a.cells + t) : (int)t) : 0;
+    const int ci = live && a.lcolor ? __ldg(a.lcolor + i) : 0;
+    T own[DNV], dg[DNV];
+    if (live && h == 0) {
+#pragma unroll
+        for (int k = 0; k < DNV; ++k) {
+            own[k] = a.own_in[(k + NV0) * ld + i];
+            dg[k] = a.diag[(k + NV0) * a.diag_vs + i];
+        }
     }
+    bool act[FB] = {false, false, false};
+    T c[FB][DNV];
+    if (live && !no_active_face(a)) {
+        const T rvi = a.rv ? __ldg(a.rv + i) : T(1);
+        int nb[FB];
+#pragma unroll
+        for (int q = 0; q < FB; ++q) {
+            const int p = h * FB + q;
+            nb[q] = p < a.nface ? __ldg(a.nei + p * ld + i) : -1;
+        }
+        face_terms<T, NV, NFV, NDIMS, RANS, false, FB, false>(a, i, ci, rvi, h * FB, nb, act, c, nullptr);
+    }
+    // the odd lane's terms to the even lane
+    unsigned mask = 0;
+#pragma unroll
+    for (int q = 0; q < FB; ++q) mask |= act[q] ? (1u << q) : 0u;
+    const unsigned mask_hi = __shfl_down_sync(0xffffffffu, mask, 1);
+    T chi[FB][DNV];
+#pragma unroll
+    for (int q = 0; q < FB; ++q)
+#pragma unroll
+        for (int k = 0; k < DNV; ++k) chi[q][k] = __shfl_down_sync(0xffffffffu, act[q] ? c[q][k] : T(0), 1);
+    if (!live || h != 0) return;
+    T df[DNV];
+#pragma unroll
+    for (int k = 0; k < DNV; ++k) df[k] = T(0);
+#pragma unroll
+    for (int q = 0; q < FB; ++q)
+        if (act[q])
+#pragma unroll
+            for (int k = 0; k < DNV; ++k) df[k] += c[q][k];
+#pragma unroll
+    for (int q = 0; q < FB; ++q)
+        if (mask_hi & (1u << q))
+#pragma unroll
+            for (int k = 0; k < DNV; ++k) df[k] += chi[q][k];
+#pragma unroll
+    for (int k = 0; k < DNV; ++k) a.own_out[(k + NV0) * ld + i] = sweep_result(a.upper != 0, own[k], df[k], dg[k]);
 }
 
 // {serial,parallel}_pre_lusgs (array layout): lusgs.c:8-37 + 87-113 with

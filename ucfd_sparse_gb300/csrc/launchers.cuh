@@ -49,6 +49,13 @@ template <typename T, int NV, int NFV, int NDIMS, bool RANS>
 static void sweep_go(const ::ucfd::ScalarSweepArgs<T> &a, int block, cudaStream_t s) {
     const long long n = a.t1 - a.t0;
     if (n <= 0) return;
+    if (a.pair && a.nface <= 6) {
+        if (a.regcap == 4)
+            scalar_sweep_pair_kernel<T, NV, NFV, NDIMS, RANS, 4><<<grid_for(2 * n, block), block, 0, s>>>(a);
+        else
+            scalar_sweep_pair_kernel<T, NV, NFV, NDIMS, RANS, 1><<<grid_for(2 * n, block), block, 0, s>>>(a);
+        return;
+    }
     if (a.regcap == 4)
         scalar_sweep_kernel<T, NV, NFV, NDIMS, RANS, 4><<<grid_for(n, block), block, 0, s>>>(a);
     else if (a.regcap == 3)
