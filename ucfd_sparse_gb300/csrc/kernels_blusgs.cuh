@@ -17,10 +17,37 @@
 namespace UCFD_KNS {
 
 // ludcmp: src/lusgs/inverse.h:13-45 (Doolittle, no pivoting, row by row).
-template <typename T, int B>
+// RCP: multiply by the reciprocal of each pivot (B - 1 divisions instead of
+// B(B-1)/2 + B - 1) -- used where the FP64 factors are then rounded to FP32
+// for the sweeps: x * (1/p) differs from x / p by at most a rounding at the
+// 1e-16 level, far below the FP32 rounding that follows.  The FP64 modes
+// keep the reference's divisions.
+template <typename T, int B, bool RCP = false>
 __device__ __forceinline__ void ludcmp_dev(T *A) {
     if constexpr (B == 1) {
         A[0] = T(1) / A[0];
+    } else if constexpr (RCP) {
+        T ip[B];
+        ip[0] = T(1) / A[0];
+#pragma unroll
+        for (int row = 1; row < B; ++row) {
+            const int nr = B * row;
+            A[nr] *= ip[0];
+#pragma unroll
+            for (int col = 1; col < B; ++col) {
+                T v = T(0);
+                if (row > col) {
+#pragma unroll
+                    for (int k = 0; k < col; ++k) v += A[nr + k] * A[col + B * k];
+                    A[nr + col] = (A[nr + col] - v) * ip[col];
+                } else {
+#pragma unroll
+                    for (int k = 0; k < row; ++k) v += A[nr + k] * A[B * k + col];
+                    A[nr + col] -= v;
+                }
+            }
+            if (row + 1 < B) ip[row] = T(1) / A[(B + 1) * row];  // the row's pivot is final now
+        }
     } else {
 #pragma unroll
         for (int row = 1; row < B; ++row) {
@@ -185,7 +212,7 @@ __global__ void fs_blusgs_prepare_kernel(long long N, int P, const int *nei, con
     const long long dbase = ::ucfd::tile_index(k, 0, B2);
 #pragma unroll
     for (int e = 0; e < B2; ++e) D[dbase + (e << 5)] = dm[e];
-    ludcmp_dev<double, B>(dm);
+    ludcmp_dev<double, B, std::is_same<S, float>::value>(dm);
 #pragma unroll
     for (int e = 0; e < B2; ++e) {
         if (LU64) LU64[dbase + (e << 5)] = dm[e];
