@@ -95,6 +95,13 @@ class Port:
             "oracle_pblusgs_precon_apply": (None, [_I, _I, _I, _P, _P, _P, _P, _P, _P, _P]),
             "oracle_gmres": (_I, [_I, _I, _P, _P, _P, _I, _I, _P, _P, _P, _I, _I, _D, _D, _P, _P,
                                   POINTER(c_int), POINTER(c_double), _P]),
+            "oracle_lusubmattrans": (None, [_I, _P, _P]),
+            "oracle_bilu_prepare": (None, [_I, _I, _P, _P, _P, _P]),
+            "oracle_bilu_apply": (None, [_I, _I, _P, _P, _P, _P, _P]),
+            "oracle_ilu_prepare": (None, [_I, _P, _P, _P, _P]),
+            "oracle_ilu_apply": (None, [_I, _P, _P, _P, _P, _P]),
+            "oracle_bicgstab": (_I, [_I, _I, _P, _P, _P, _I, _I, _P, _P, _P, _P, _I, _D, _P, _P,
+                                     POINTER(c_int), POINTER(c_double), _P]),
         }
         for n, (r, a) in sig.items():
             f = getattr(L, n)
@@ -241,6 +248,47 @@ class Port:
                                  P(_f64(b)), byref(it), byref(res), P(hist))
         return x, st, it.value, res.value, hist[:it.value + 1]
 
+    def bilu_factor(self, s: dict):
+        """Block ILU(0) factors (bilu.c:5-62) of s["values"], natural order."""
+        v = _f64(s["values"]).copy()
+        self.L.oracle_bilu_prepare(s["bn"], s["blk"], P(_i32(s["rowptr"])), P(_i32(s["colidx"])),
+                                   P(_i32(s["diagslots"])), P(v))
+        return v
+
+    def bilu_apply(self, s: dict, fvalues, b):
+        b = _f64(b).copy()
+        self.L.oracle_bilu_apply(s["bn"], s["blk"], P(_i32(s["rowptr"])), P(_i32(s["colidx"])),
+                                 P(_i32(s["diagslots"])), P(_f64(fvalues)), P(b))
+        return b
+
+    def ilu_factor(self, s: dict):
+        """Scalar ILU(0) factors (ilu.c:4-47) of a CSR matrix (blk 1)."""
+        v = _f64(s["values"]).copy()
+        self.L.oracle_ilu_prepare(s["bn"], P(_i32(s["rowptr"])), P(_i32(s["colidx"])), P(_i32(s["diagslots"])),
+                                  P(v))
+        return v
+
+    def ilu_apply(self, s: dict, fvalues, b):
+        b = _f64(b).copy()
+        self.L.oracle_ilu_apply(s["bn"], P(_i32(s["rowptr"])), P(_i32(s["colidx"])), P(_i32(s["diagslots"])),
+                                P(_f64(fvalues)), P(b))
+        return b
+
+    def bicgstab(self, s: dict, b, maxiter=50, tol=1e-10, pc="blusgs", icolors=None, x0=None):
+        """BiCGSTAB of bicgstab.c:24-128 -> (x, stat, iters, resnorm, hist)."""
+        bn, blk = s["bn"], s["blk"]
+        kind = {"none": 0, "blusgs": 1, "pblusgs": 2, "bilu": 3, "ilu": 4}[pc]
+        d = self.precon_diag(s) if kind in (1, 2) else np.zeros(1)
+        fv = self.bilu_factor(s) if kind == 3 else self.ilu_factor(s) if kind == 4 else np.zeros(1)
+        ic = _i32(icolors) if icolors is not None else np.zeros(1, dtype=np.int32)
+        x = np.zeros(bn * blk) if x0 is None else _f64(x0).copy()
+        it, res = c_int(), c_double()
+        hist = np.zeros(max(maxiter, 1))
+        st = self.L.oracle_bicgstab(bn, blk, P(_i32(s["rowptr"])), P(_i32(s["colidx"])), P(_f64(s["values"])),
+                                    kind, len(ic) - 1, P(ic), P(_i32(s["diagslots"])), P(d), P(fv), maxiter, tol,
+                                    P(x), P(_f64(b)), byref(it), byref(res), P(hist))
+        return x, st, it.value, res.value, hist[:maxiter]
+
 
 # ---------------------------------------------------------------------------
 # the reference library compiled from its own sources
@@ -291,6 +339,10 @@ class Ref:
             "UCFDPreconPrepare": [_P],
             "UCFDPreconDestroy": [H],
             "UCFDSolverCreateGMRES": [H, _I, _I, _I, _D],
+            "UCFDSolverCreateBICGSTAB": [H, _I, _I, _D],
+            "UCFDPreconSetBILU": [H, _I, _I],
+            "UCFDPreconSetPBILU": [H, _I, _I, _I, _P],
+            "UCFDPreconSetILU": [H, _I],
             "UCFDSolve": [_P, _P, _P, _P, _P],
             "UCFDSolverGetResult": [_P, POINTER(c_int), POINTER(c_int), POINTER(c_double)],
             "UCFDSolverTraceResidualHistory": [_P],
@@ -388,6 +440,67 @@ class Ref:
         self.kry.UCFDSolverGetResidualHistory(sv, P(hist))
         self.kry.UCFDSolverDestroy(byref(sv))
         self.kry.UCFDPreconDestroy(byref(pc))
+        self.kry.UCFDMatDestroy(byref(A))
+        return x, st.value, it.value, res.value, hist
+
+    def _precon(self, s, pc, v, icolors=None):
+        """A reference preconditioner on arrays (v is modified in place by
+        the ILU-type prepares, as in the reference)."""
+        h = c_void_p()
+        keep = [_i32(s["rowptr"]), _i32(s["colidx"]), _i32(s["diagslots"])]
+        self.kry.UCFDPreconCreatefromArrays(byref(h), P(keep[0]), P(keep[1]), P(keep[2]), P(v))
+        if pc == "blusgs":
+            self.kry.UCFDPreconSetBLUSGS(byref(h), s["bn"], s["blk"])
+        elif pc == "bilu":
+            self.kry.UCFDPreconSetBILU(byref(h), s["bn"], s["blk"])
+        elif pc == "pbilu":
+            ic = _i32(icolors)
+            keep.append(ic)
+            self.kry.UCFDPreconSetPBILU(byref(h), s["bn"], s["blk"], len(ic) - 1, P(ic))
+            # pbilu.c:20 shares one column map (iw) among the OpenMP threads of a
+            # colour, so its result is only defined with a single thread
+            gomp = ctypes.CDLL("libgomp.so.1")
+            nt = gomp.omp_get_max_threads()
+            gomp.omp_set_num_threads(1)
+            try:
+                self.kry.UCFDPreconPrepare(h)
+            finally:
+                gomp.omp_set_num_threads(nt)
+            return h, keep
+        elif pc == "ilu":
+            self.kry.UCFDPreconSetILU(byref(h), s["bn"])
+        else:
+            raise ValueError(pc)
+        self.kry.UCFDPreconPrepare(h)
+        return h, keep
+
+    def ilu_factor(self, s, pc="bilu", icolors=None):
+        """The values array after the reference's ILU-type Prepare."""
+        v = _f64(s["values"]).copy()
+        h, keep = self._precon(s, pc, v, icolors)
+        self.kry.UCFDPreconDestroy(byref(h))
+        return v
+
+    def bicgstab(self, s, b, maxiter=50, tol=1e-10, pc="blusgs", icolors=None):
+        """BiCGSTAB of the reference with a preconditioner on a copy of the
+        values (the matrix keeps the originals)."""
+        A, sv = c_void_p(), c_void_p()
+        rp, ci, v = _i32(s["rowptr"]), _i32(s["colidx"]), _f64(s["values"])
+        self.kry.UCFDMatCreateBSR(byref(A), s["bn"], s["blk"], P(rp), P(ci), P(v))
+        pv = v.copy()
+        pc_h, keep = self._precon(s, pc, pv, icolors)
+        n = s["bn"] * s["blk"]
+        self.kry.UCFDSolverCreateBICGSTAB(byref(sv), n, maxiter, tol)
+        self.kry.UCFDSolverTraceResidualHistory(sv)
+        x = np.zeros(n)
+        b = _f64(b)
+        self.kry.UCFDSolve(sv, pc_h, A, P(x), P(b))
+        st, it, res = c_int(), c_int(), c_double()
+        self.kry.UCFDSolverGetResult(sv, byref(st), byref(it), byref(res))
+        hist = np.zeros(maxiter)
+        self.kry.UCFDSolverGetResidualHistory(sv, P(hist))
+        self.kry.UCFDSolverDestroy(byref(sv))
+        self.kry.UCFDPreconDestroy(byref(pc_h))
         self.kry.UCFDMatDestroy(byref(A))
         return x, st.value, it.value, res.value, hist
 

@@ -783,3 +783,273 @@ int oracle_gmres(oint bn, oint blk, const oint *rowptr, const oint *colidx,
     free(H); free(V); free(y); free(w); free(sn); free(cs); free(h2); free(r);
     return stat;
 }
+
+/* ========================================================================
+ * Incomplete factorisations and BiCGSTAB (src/krylov/precon/{ilu,bilu,
+ * pbilu}.c, src/krylov/solver/bicgstab.c).
+ * ====================================================================== */
+
+/* lusubmattrans: src/krylov/utils/inverse.c:79-108.  B := B inv(LU) for an
+ * n x n row-major B and the in-place factors LU of oracle_ludcmp: first
+ * Y U = B column by column, then X L = Y. */
+void oracle_lusubmattrans(oint n, const oreal *LU, oreal *B)
+{
+    if (n == 1) {
+        B[0] *= LU[0];
+        return;
+    }
+    for (oint s = 0; s < n; ++s) B[s * n] /= LU[0];
+    for (oint row = 1; row < n; ++row)
+        for (oint s = 0; s < n; ++s) {
+            oreal v = 0.0;
+            for (oint col = 0; col < row; ++col) v += B[s * n + col] * LU[col * n + row];
+            B[s * n + row] = (B[s * n + row] - v) / LU[row * n + row];
+        }
+    for (oint row = n - 2; row > -1; --row)
+        for (oint s = 0; s < n; ++s) {
+            oreal v = 0.0;
+            for (oint col = row + 1; col < n; ++col) v += B[s * n + col] * LU[col * n + row];
+            B[s * n + row] -= v;
+        }
+}
+
+/* BILUPreconPrepare: src/krylov/precon/bilu.c:5-62.  Block ILU(0) in
+ * natural row order, in place on values: for each lower entry (i,k) in
+ * slot order, A_ik := A_ik inv(A_kk), then A_ij -= A_ik A_kj for every
+ * later slot j of row i whose column row k also holds; finally the
+ * diagonal block is LU-factorised.  iw maps a column of row k to its slot
+ * (the last slot if a column repeats).  PBILUPreconPrepare (pbilu.c:5-79)
+ * computes the same per colour, which on a colour-ordered matrix equals
+ * this natural order. */
+void oracle_bilu_prepare(oint bn, oint blk, const oint *rowptr, const oint *colidx,
+                         const oint *diagslots, oreal *values)
+{
+    const oint b2 = blk * blk;
+    oint *iw = (oint *)malloc(sizeof(oint) * (size_t)bn);
+    oreal aik[256];
+    for (oint i = 0; i < bn; ++i) iw[i] = -1;
+    for (oint i = 0; i < bn; ++i) {
+        const oint st = rowptr[i], ed = diagslots[i], jed = rowptr[i + 1];
+        for (oint kd = st; kd < ed; ++kd) {
+            const oint ck = colidx[kd], kk = diagslots[ck], kst = rowptr[ck], ked = rowptr[ck + 1];
+            oracle_lusubmattrans(blk, &values[(size_t)kk * b2], &values[(size_t)kd * b2]);
+            memcpy(aik, &values[(size_t)kd * b2], sizeof(oreal) * b2);
+            for (oint jj = kst; jj < ked; ++jj) iw[colidx[jj]] = jj;
+            for (oint jj = kd + 1; jj < jed; ++jj) {
+                const oint iwj = iw[colidx[jj]];
+                if (iwj == -1) continue;
+                for (oint row = 0; row < blk; ++row)
+                    for (oint col = 0; col < blk; ++col) {
+                        oreal v = 0.0;
+                        for (oint e = 0; e < blk; ++e)
+                            v += aik[row * blk + e] * values[(size_t)iwj * b2 + e * blk + col];
+                        values[(size_t)jj * b2 + row * blk + col] -= v;
+                    }
+            }
+            for (oint jj = kst; jj < ked; ++jj) iw[colidx[jj]] = -1;
+        }
+        oracle_ludcmp(blk, &values[(size_t)ed * b2]);
+    }
+    free(iw);
+}
+
+/* BILUPreconApply: src/krylov/precon/bilu.c:64-129 (natural order, in
+ * place): forward b_i -= sum_{j<i} L_ij b_j, then backward
+ * b_i = inv(LU_ii) (b_i - sum_{j>i} U_ij b_j).  PBILUPreconApply
+ * (pbilu.c:81-200) equals it on a colour-ordered matrix. */
+void oracle_bilu_apply(oint bn, oint blk, const oint *rowptr, const oint *colidx,
+                       const oint *diagslots, const oreal *values, oreal *b)
+{
+    const oint b2 = blk * blk;
+    oreal arr[16];
+    for (oint i = 0; i < bn; ++i) {
+        for (oint k = 0; k < blk; ++k) arr[k] = b[k + (size_t)i * blk];
+        for (oint j = rowptr[i]; j < diagslots[i]; ++j) {
+            const oint c = colidx[j];
+            for (oint row = 0; row < blk; ++row) {
+                oreal v = 0.0;
+                for (oint col = 0; col < blk; ++col)
+                    v += values[col + row * blk + (size_t)j * b2] * b[col + (size_t)c * blk];
+                arr[row] -= v;
+            }
+        }
+        for (oint k = 0; k < blk; ++k) b[k + (size_t)i * blk] = arr[k];
+    }
+    for (oint i = bn - 1; i > -1; --i) {
+        for (oint k = 0; k < blk; ++k) arr[k] = b[k + (size_t)i * blk];
+        for (oint j = diagslots[i] + 1; j < rowptr[i + 1]; ++j) {
+            const oint c = colidx[j];
+            for (oint row = 0; row < blk; ++row) {
+                oreal v = 0.0;
+                for (oint col = 0; col < blk; ++col)
+                    v += values[col + row * blk + (size_t)j * b2] * b[col + (size_t)c * blk];
+                arr[row] -= v;
+            }
+        }
+        oracle_lusub(blk, &values[(size_t)diagslots[i] * b2], arr);
+        for (oint k = 0; k < blk; ++k) b[(size_t)i * blk + k] = arr[k];
+    }
+}
+
+/* ILUPreconPrepare: src/krylov/precon/ilu.c:4-47 (scalar ILU(0), in
+ * place; the diagonal is kept, not inverted). */
+void oracle_ilu_prepare(oint n, const oint *rowptr, const oint *colidx, const oint *diagslots,
+                        oreal *values)
+{
+    oint *iw = (oint *)malloc(sizeof(oint) * (size_t)n);
+    for (oint i = 0; i < n; ++i) iw[i] = -1;
+    for (oint i = 0; i < n; ++i) {
+        const oint st = rowptr[i], ed = diagslots[i], jed = rowptr[i + 1];
+        for (oint kd = st; kd < ed; ++kd) {
+            const oint ck = colidx[kd], kk = diagslots[ck], kst = rowptr[ck], ked = rowptr[ck + 1];
+            values[kd] /= values[kk];
+            const oreal aik = values[kd];
+            for (oint jj = kst; jj < ked; ++jj) iw[colidx[jj]] = jj;
+            for (oint jj = kd + 1; jj < jed; ++jj) {
+                const oint iwj = iw[colidx[jj]];
+                if (iwj != -1) values[jj] -= aik * values[iwj];
+            }
+            for (oint jj = kst; jj < ked; ++jj) iw[colidx[jj]] = -1;
+        }
+    }
+    free(iw);
+}
+
+/* ILUPreconApply: src/krylov/precon/ilu.c:49-85, with the backward loop
+ * starting after the diagonal slot.  ilu.c:78 starts it at the diagonal
+ * slot itself, which subtracts a_ii b_i before dividing by a_ii; the
+ * intended triangular solve, restated here, excludes it. */
+void oracle_ilu_apply(oint n, const oint *rowptr, const oint *colidx, const oint *diagslots,
+                      const oreal *values, oreal *b)
+{
+    for (oint i = 0; i < n; ++i) {
+        oreal v = b[i];
+        for (oint j = rowptr[i]; j < diagslots[i]; ++j) v -= values[j] * b[colidx[j]];
+        b[i] = v;
+    }
+    for (oint i = n - 1; i > -1; --i) {
+        const oint dd = diagslots[i];
+        oreal v = b[i];
+        for (oint j = dd + 1; j < rowptr[i + 1]; ++j) v -= values[j] * b[colidx[j]];
+        b[i] = v / values[dd];
+    }
+}
+
+/* Preconditioner of oracle_bicgstab: 0 none, 1 BLU-SGS (natural), 2
+ * coloured BLU-SGS (colour ranges), 3 BILU / PBILU with factored values
+ * (fvalues from oracle_bilu_prepare), 4 ILU with factored values. */
+static void or_pc_apply_any(int kind, oint bn, oint blk, oint ncolors, const oint *icolors,
+                            const oint *rowptr, const oint *colidx, const oint *diagslots,
+                            const oreal *values, const oreal *diagvalues, const oreal *fvalues, oreal *b)
+{
+    if (kind == 1)
+        oracle_blusgs_precon_apply(bn, blk, rowptr, colidx, diagslots, values, diagvalues, b);
+    else if (kind == 2)
+        oracle_pblusgs_precon_apply(bn, blk, ncolors, icolors, rowptr, colidx, diagslots, values, diagvalues, b);
+    else if (kind == 3)
+        oracle_bilu_apply(bn, blk, rowptr, colidx, diagslots, fvalues, b);
+    else if (kind == 4)
+        oracle_ilu_apply(bn * blk, rowptr, colidx, diagslots, fvalues, b);
+}
+
+static oreal or_dot(oint n, const oreal *x, const oreal *y)
+{
+    oreal s = 0.0;
+    for (oint i = 0; i < n; ++i) s += x[i] * y[i];
+    return s;
+}
+
+static void or_axpy(oint n, oreal a, const oreal *x, oreal *y)
+{
+    for (oint i = 0; i < n; ++i) y[i] += a * x[i];
+}
+
+/* BICGSTABSolve: src/krylov/solver/bicgstab.c:24-128.  Right-preconditioned
+ * BiCGSTAB with the fused five-term reduction of bicgstab.c:5-22 and the
+ * residual-norm estimate sqrt|ss - 2 w ts + w^2 tt|; stops when it drops
+ * below tol (absolute).  Returns the status of ucfdtypes.h:22-30 (0
+ * converged, 2 iteration limit, 3 rho breakdown, 4 pi breakdown) and
+ * writes the iteration count, the last estimate and (if hist) the
+ * estimate of every iteration. */
+int oracle_bicgstab(oint bn, oint blk, const oint *rowptr, const oint *colidx, const oreal *values,
+                    int pc_kind, oint ncolors, const oint *icolors, const oint *diagslots,
+                    const oreal *diagvalues, const oreal *fvalues, oint maxiter, double tol, oreal *x,
+                    const oreal *b, oint *iters, double *resid, double *hist)
+{
+    const oint n = bn * blk;
+    oreal *r = (oreal *)calloc((size_t)n, sizeof(oreal));
+    oreal *rt = (oreal *)calloc((size_t)n, sizeof(oreal));
+    oreal *p = (oreal *)calloc((size_t)n, sizeof(oreal));
+    oreal *pt = (oreal *)calloc((size_t)n, sizeof(oreal));
+    oreal *v = (oreal *)calloc((size_t)n, sizeof(oreal));
+    oreal *s = (oreal *)calloc((size_t)n, sizeof(oreal));
+    oreal *sh = (oreal *)calloc((size_t)n, sizeof(oreal));
+    oreal *t = (oreal *)calloc((size_t)n, sizeof(oreal));
+    int stat = -1;
+    oint iter = 0;
+    oreal rho, rhoprev = 1.0, alpha = 1.0, omega = 1.0, resnorm = 0.0;
+    memcpy(r, b, sizeof(oreal) * n);
+    oracle_bsr_spmv(bn, blk, rowptr, colidx, values, -1.0, x, 1.0, r);
+    memcpy(rt, r, sizeof(oreal) * n);
+    rho = or_dot(n, rt, r);
+    if (fabs(rho) < 1e-30) {
+        stat = 3;
+        goto done;
+    }
+    while (iter < maxiter) {
+        if (iter == 0) {
+            memcpy(p, r, sizeof(oreal) * n);
+        } else {
+            const oreal beta = (rho / rhoprev) * (alpha / omega);
+            or_axpy(n, -omega, v, p);
+            for (oint i = 0; i < n; ++i) p[i] = beta * p[i];
+            or_axpy(n, 1.0, r, p);
+        }
+        memcpy(pt, p, sizeof(oreal) * n);
+        or_pc_apply_any(pc_kind, bn, blk, ncolors, icolors, rowptr, colidx, diagslots, values, diagvalues,
+                        fvalues, pt);
+        oracle_bsr_spmv(bn, blk, rowptr, colidx, values, 1.0, pt, 0.0, v);
+        const oreal pi = or_dot(n, rt, v);
+        if (fabs(pi) < 1e-30) {
+            stat = 4;
+            break;
+        }
+        alpha = rho / pi;
+        memcpy(s, r, sizeof(oreal) * n);
+        or_axpy(n, -alpha, v, s);
+        memcpy(sh, s, sizeof(oreal) * n);
+        or_pc_apply_any(pc_kind, bn, blk, ncolors, icolors, rowptr, colidx, diagslots, values, diagvalues,
+                        fvalues, sh);
+        oracle_bsr_spmv(bn, blk, rowptr, colidx, values, 1.0, sh, 0.0, t);
+        oreal phi = 0.0, rtt = 0.0, ts = 0.0, tt = 0.0, ss = 0.0;
+        for (oint k = 0; k < n; ++k) {
+            const oreal sk = s[k], tk = t[k], rk = rt[k];
+            phi += rk * sk;
+            rtt += rk * tk;
+            ts += tk * sk;
+            tt += tk * tk;
+            ss += sk * sk;
+        }
+        omega = ts / tt;
+        or_axpy(n, alpha, pt, x);
+        or_axpy(n, omega, sh, x);
+        memcpy(r, s, sizeof(oreal) * n);
+        or_axpy(n, -omega, t, r);
+        const oreal rho_new = phi - omega * rtt;
+        resnorm = sqrt(fabs(ss - 2.0 * omega * ts + omega * omega * tt));
+        if (hist) hist[iter] = resnorm;
+        if (resnorm < tol) {
+            stat = 0;
+            goto done;
+        }
+        rhoprev = rho;
+        rho = rho_new;
+        iter++;
+    }
+done:
+    if (iter == maxiter) stat = 2;
+    *iters = iter;
+    *resid = resnorm;
+    free(r); free(rt); free(p); free(pt); free(v); free(s); free(sh); free(t);
+    return stat;
+}

@@ -83,3 +83,7 @@ def bsr_case(mesh, seed, **_):
 
 def spmv_x(s):
     return np.random.default_rng(7).standard_normal(s["bn"] * s["blk"])
+
+
+def sha(a: np.ndarray) -> str:
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()

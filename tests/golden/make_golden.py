@@ -23,6 +23,10 @@ import sys
 
 import numpy as np
 
+# one OpenMP thread: the reference's reductions then sum in index order, as
+# the restatement does (set before the reference library is loaded)
+os.environ["OMP_NUM_THREADS"] = "1"
+
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
 OUT = os.path.dirname(os.path.abspath(__file__))
@@ -97,6 +101,13 @@ def main(ref_root: str) -> None:
         xs, st, it, res, hist = ref.gmres(s, s["rhs"], m=kw["m"], maxiter=20, tol=tol)
         arrays[f"{name}_gmres_x"] = xs
         meta[f"{name}_gmres"] = dict(stat=st, iters=it, resid=res, tol=tol)
+        # block ILU(0) factors (bilu.c), BiCGSTAB with BLU-SGS and with BILU
+        meta[f"{name}_bilu_sha"] = sha(ref.ilu_factor(s, "bilu"))
+        for pc in ("blusgs", "bilu"):
+            xb, st, it, res, hist = ref.bicgstab(s, s["rhs"], maxiter=20, tol=tol, pc=pc)
+            arrays[f"{name}_bicgstab_{pc}_x"] = xb
+            meta[f"{name}_bicgstab_{pc}"] = dict(stat=st, iters=it, resid=res, tol=tol,
+                                                 hist=[float(h) for h in hist[:it + 1]])
 
     np.savez_compressed(os.path.join(OUT, "golden.npz"), **arrays)
     with open(os.path.join(OUT, "golden.json"), "w") as f:
