@@ -1,14 +1,18 @@
 /*
  * ucfdsolver.h -- Krylov solvers of libucfd_gb300.so.
  *
- * Drop-in for src/krylov/include/ucfdsolver.h:5-31 (GMRES).  GMRES(m) is
+ * Drop-in for src/krylov/include/ucfdsolver.h:5-31 (GMRES, BiCGSTAB).  GMRES(m) is
  * left-preconditioned with classical Gram-Schmidt plus one
  * re-orthogonalisation and Givens rotations, stopping when the absolute
  * true residual ||b - A x|| <= tol is seen at a restart (gmres.c:42-129).
  * Everything runs on the GPU: Arnoldi passes are fused, the Givens / least-
  * squares step runs on the device, and one restart cycle is replayed as a
- * CUDA graph with a single host synchronisation per restart.  x and b may
- * be host or device arrays of n = bn*blk values.
+ * CUDA graph with a single host synchronisation per restart.  BiCGSTAB is
+ * right-preconditioned with the fused five-term reduction and the residual
+ * estimate of bicgstab.c:24-128, stopping when the estimate drops below tol
+ * (absolute); its scalars stay on the device and the host reads the stop
+ * flag every few iterations.  x and b may be host or device arrays of
+ * n = bn*blk values.
  */
 #pragma once
 
@@ -22,6 +26,7 @@ typedef struct _Solver *Solver;   /* ucfdsolver.h:6 */
 
 typedef const char *SolverType;   /* ucfdsolver.h:8-10 */
 #define GMRES "gmres"
+#define BICGSTAB "bicgstab"
 
 /* ucfdsolver.h:17-23, solver.c:5-69 */
 UCFD_EXTERN ucfd_status_t UCFDSolverInit(Solver *solver);
@@ -38,6 +43,9 @@ UCFD_EXTERN ucfd_status_t UCFDSolverCreateGMRES(Solver *solver, UCFDInt n, UCFDI
                                                 UCFDInt maxiter, UCFDReal tol);
 UCFD_EXTERN ucfd_status_t UCFDSolverCreateCUDAGMRES(Solver *solver, UCFDInt n, UCFDInt m,
                                                     UCFDInt maxiter, UCFDReal tol);
+/* ucfdsolver.h:26, bicgstab.c:156-179 */
+UCFD_EXTERN ucfd_status_t UCFDSolverCreateBICGSTAB(Solver *solver, UCFDInt n, UCFDInt maxiter,
+                                                   UCFDReal tol);
 
 /* ---- GB300 extensions ------------------------------------------------ */
 /* UCFD_PREC_FP32: mixed-precision GMRES -- inside each restart cycle the

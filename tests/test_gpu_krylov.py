@@ -128,3 +128,135 @@ def test_gmres_coloured_and_mixed_reach_1e10(prec, port, ucfd):
     xr, st_o, it_o, res_o, _ = port.gmres(s, s["rhs"], m=30, maxiter=50, tol=tol, pc="pblusgs", icolors=ic)
     assert st_o == 0
     assert np.abs(x.cpu().numpy() - xr).max() <= 1e-8 * np.abs(xr).max()
+
+
+# ---- block / scalar ILU(0) and BiCGSTAB -----------------------------------------
+def scalar_case(s):
+    """A CSR matrix (blk 1) on the BSR pattern: the (0, 0) entry of each block."""
+    v = np.ascontiguousarray(np.asarray(s["values"]).reshape(-1, s["blk"], s["blk"])[:, 0, 0])
+    return dict(s, blk=1, values=v)
+
+
+@pytest.mark.parametrize("kind", ["bilu", "pbilu", "ilu"])
+def test_ilu_factors_and_apply_bitexact(kind, port, ucfd):
+    """Prepare factorises on the GPU (FP64, level by level) and, as the
+    reference does, overwrites the caller's values with the factors: bit for
+    bit the oracle's (bilu.c / ilu.c); the apply equals the oracle's."""
+    from ucfd_sparse_gb300.krylov import Precon
+    s0 = cases.bsr_case(mesh=5, seed=4)
+    s, ic = colour_renumbered(s0) if kind == "pbilu" else (s0, None)
+    if kind == "ilu":
+        s = scalar_case(s)
+    vals = np.array(s["values"], dtype=np.float64)
+    pc = Precon(s["rowptr"], s["colidx"], s["diagslots"], vals)
+    if kind == "bilu":
+        pc.set_bilu(s["bn"], s["blk"])
+    elif kind == "pbilu":
+        pc.set_pbilu(s["bn"], s["blk"], len(ic) - 1, ic)
+    else:
+        pc.set_ilu(s["bn"])
+    pc.prepare()
+    fv = port.ilu_factor(s) if kind == "ilu" else port.bilu_factor(s)
+    np.testing.assert_array_equal(vals, fv)
+    b = np.random.default_rng(7).standard_normal(s["bn"] * s["blk"])
+    x = b.copy()
+    pc.apply(x)
+    ref = port.ilu_apply(s, fv, b) if kind == "ilu" else port.bilu_apply(s, fv, b)
+    np.testing.assert_array_equal(x, ref)
+    if kind == "bilu":
+        assert pc.levels() > 2   # natural order: level-scheduled
+
+
+def test_bilu_fp32_apply_close(port, ucfd):
+    from ucfd_sparse_gb300.krylov import Precon
+    s = cases.bsr_case(mesh=5, seed=8)
+    vals = np.array(s["values"], dtype=np.float64)
+    pc = Precon(s["rowptr"], s["colidx"], s["diagslots"], vals)
+    pc.set_bilu(s["bn"], s["blk"])
+    pc.set_precision(2)
+    pc.prepare()
+    b = np.random.default_rng(3).standard_normal(s["bn"] * 5)
+    x = b.copy()
+    pc.apply(x)
+    ref = port.bilu_apply(s, port.bilu_factor(s), b)
+    assert np.abs(x - ref).max() <= 1e-5 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("name", sorted(cases.KRYLOV))
+@pytest.mark.parametrize("pc_kind", ["blusgs", "bilu"])
+@pytest.mark.parametrize("on_device", [False, True])
+def test_bicgstab_matches_reference(name, pc_kind, on_device, golden, ucfd):
+    """BiCGSTAB (bicgstab.c) on the GPU: the reference's status, iteration
+    count and residual history; the solution within 1e-10 of the
+    reference's (the device reductions sum in another order)."""
+    from ucfd_sparse_gb300.krylov import Precon, Solver, SpMat
+    meta, arr = golden
+    s = cases.bsr_case(**cases.KRYLOV[name])
+    g = meta[f"{name}_bicgstab_{pc_kind}"]
+    conv = dev if on_device else np.ascontiguousarray
+    A = SpMat(s["bn"], s["blk"], conv(s["rowptr"]), conv(s["colidx"]), conv(s["values"]), cuda=on_device)
+    pvals = conv(np.array(s["values"], dtype=np.float64))
+    pc = Precon(conv(s["rowptr"]), conv(s["colidx"]), conv(s["diagslots"]), pvals)
+    if pc_kind == "bilu":
+        pc.set_bilu(s["bn"], s["blk"])
+    else:
+        pc.set_blusgs(s["bn"], s["blk"])
+    pc.prepare()
+    n = s["bn"] * s["blk"]
+    sv = Solver(n, 0, 20, g["tol"], kind="bicgstab")
+    sv.trace()
+    x = conv(np.zeros(n))
+    sv.solve(pc, A, x, conv(s["rhs"]))
+    st, it, res = sv.result()
+    assert (st, it) == (g["stat"], g["iters"])
+    np.testing.assert_allclose(sv.history()[:it + 1], g["hist"], rtol=1e-8)
+    xh = x.cpu().numpy() if on_device else x
+    ref = arr[f"{name}_bicgstab_{pc_kind}_x"]
+    assert np.abs(xh - ref).max() <= 1e-10 * np.abs(ref).max()
+
+
+def test_bicgstab_edge_cases(port, ucfd):
+    """Iteration limit 0 (REACH_ITERMAX, no iteration), zero right-hand side
+    (rho breakdown, status 3) and a limit that stops before convergence."""
+    from ucfd_sparse_gb300.krylov import Precon, Solver, SpMat
+    s = cases.bsr_case(mesh=4, seed=2)
+    n = s["bn"] * 5
+    A = SpMat(s["bn"], 5, s["rowptr"], s["colidx"], s["values"])
+    pc = Precon(s["rowptr"], s["colidx"], s["diagslots"], np.array(s["values"]))
+    pc.set_blusgs(s["bn"], 5)
+    pc.prepare()
+    for maxiter, b, want in ((0, s["rhs"], 2), (10, np.zeros(n), 3), (1, s["rhs"], 2)):
+        sv = Solver(n, 0, maxiter, 1e-30, kind="bicgstab")
+        x = np.zeros(n)
+        sv.solve(pc, A, x, np.ascontiguousarray(b))
+        st, it, res = sv.result()
+        xo, sto, ito, reso, _ = port.bicgstab(s, b, maxiter=maxiter, tol=1e-30, pc="blusgs")
+        assert (st, it) == (sto, ito) == (want, ito)
+        assert np.abs(x - xo).max() <= 1e-10 * max(np.abs(xo).max(), 1e-300)
+
+
+@pytest.mark.parametrize("pc_kind", ["pbilu", "pblusgs"])
+def test_bicgstab_coloured_reaches_tolerance(pc_kind, port, ucfd):
+    """Coloured preconditioners on a larger system: converged, and the true
+    residual ||b - A x|| confirms the estimate."""
+    from ucfd_sparse_gb300.krylov import Precon, Solver, SpMat
+    s0 = cases.bsr_case(mesh=12, seed=9)
+    s, ic = colour_renumbered(s0)
+    n = s["bn"] * 5
+    A = SpMat(s["bn"], 5, dev(s["rowptr"]), dev(s["colidx"]), dev(s["values"]), cuda=True)
+    pc = Precon(dev(s["rowptr"]), dev(s["colidx"]), dev(s["diagslots"]), dev(np.array(s["values"])))
+    if pc_kind == "pbilu":
+        pc.set_pbilu(s["bn"], 5, len(ic) - 1, ic, cuda=True)
+    else:
+        pc.set_pblusgs(s["bn"], 5, len(ic) - 1, ic, cuda=True)
+    pc.prepare()
+    tol = 1e-10 * float(np.linalg.norm(s["rhs"]))
+    sv = Solver(n, 0, 100, tol, kind="bicgstab")
+    x = torch.zeros(n, dtype=torch.float64, device="cuda")
+    b = dev(s["rhs"])
+    sv.solve(pc, A, x, b)
+    st, it, res = sv.result()
+    assert st == 0 and res < tol
+    r = b.clone()
+    A.mult(-1.0, x, 1.0, r)
+    assert float(torch.linalg.norm(r)) <= 10 * tol

@@ -155,7 +155,7 @@ def test_pbilu_equals_natural_on_colour_ordered_matrix(port):
 def test_ilu_apply_inverts_its_factors(port):
     """Scalar ILU(0): the factors match the reference (ilu.c prepare) and
     the restated apply -- with the diagonal slot left out of the backward
-    loop, unlike ilu.c:78 -- solves (L U) y = b exactly up to rounding."""
+    loop, unlike ilu.c:81 -- solves (L U) y = b exactly up to rounding."""
     from ucfd_sparse_gb300 import meshgen as mg
     s = mg.bsr_case(4, seed=6)
     ss = dict(s, blk=1, values=np.ascontiguousarray(np.asarray(s["values"]).reshape(-1, 5, 5)[:, 0, 0]))

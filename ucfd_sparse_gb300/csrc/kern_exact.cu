@@ -32,9 +32,12 @@ template void fs_blusgs_subres<double>(int, int, long long, const int *, const i
 template void fs_blusgs_update<double>(int, int, long long, const int *, const int *, const double *, double *, cudaStream_t);
 template void bsr_spmv<double, double>(int, int, int, const int *, const double *, double, const double *, double,
                                        double *, int, cudaStream_t);
-template void pc_prepare<double>(int, int, const int *, const long long *, const double *, double *, double *, cudaStream_t);
-template void pc_lower<double>(int, int, int, int, int, const int *, const double *, const double *, double *, int, cudaStream_t);
-template void pc_upper<double>(int, int, int, int, int, const int *, const double *, const double *, double *, int, cudaStream_t);
+template void pc_prepare<double>(int, int, const int *, const long long *, const double *, double *, double *, int,
+                                 cudaStream_t);
+template void pc_lower<double>(int, int, int, int, int, const int *, const double *, const double *, double *, int,
+                               int, cudaStream_t);
+template void pc_upper<double>(int, int, int, int, int, const int *, const double *, const double *, double *, int,
+                               int, cudaStream_t);
 template void gather_rows<double, double>(int, int, const int *, const double *, double *, cudaStream_t);
 template void scatter_rows<double, double>(int, int, const int *, const double *, double *, cudaStream_t);
 }  // namespace kexact

@@ -36,11 +36,11 @@ namespace kfast {
                                       cudaStream_t);                                                           \
     template void bsr_spmv<T, T>(int, int, int, const int *, const T *, double, const double *, double,        \
                                  double *, int, cudaStream_t);                                                 \
-    template void pc_prepare<T>(int, int, const int *, const long long *, const double *, double *, T *,       \
+    template void pc_prepare<T>(int, int, const int *, const long long *, const double *, double *, T *, int,  \
                                 cudaStream_t);                                                                 \
-    template void pc_lower<T>(int, int, int, int, int, const int *, const T *, const T *, T *, int,            \
+    template void pc_lower<T>(int, int, int, int, int, const int *, const T *, const T *, T *, int, int,       \
                               cudaStream_t);                                                                   \
-    template void pc_upper<T>(int, int, int, int, int, const int *, const T *, const T *, T *, int,            \
+    template void pc_upper<T>(int, int, int, int, int, const int *, const T *, const T *, T *, int, int,       \
                               cudaStream_t);
 UCFD_INST_T(double)
 UCFD_INST_T(float)

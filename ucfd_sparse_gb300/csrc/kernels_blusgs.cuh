@@ -94,6 +94,37 @@ __device__ __forceinline__ void lusub_dev(const T *LU, T *b) {
     }
 }
 
+// lusubmattrans: src/krylov/utils/inverse.c:79-108.  X := X inv(LU) for a
+// row-major B x B block X and factors LU from ludcmp_dev: Y U = X column
+// by column, then X L = Y.
+template <typename T, int B>
+__device__ __forceinline__ void lusubmattrans_dev(const T *LU, T *X) {
+    if constexpr (B == 1) {
+        X[0] *= LU[0];
+    } else {
+#pragma unroll
+        for (int s = 0; s < B; ++s) X[s * B] /= LU[0];
+#pragma unroll
+        for (int row = 1; row < B; ++row)
+#pragma unroll
+            for (int s = 0; s < B; ++s) {
+                T v = T(0);
+#pragma unroll
+                for (int col = 0; col < row; ++col) v += X[s * B + col] * LU[col * B + row];
+                X[s * B + row] = (X[s * B + row] - v) / LU[row * B + row];
+            }
+#pragma unroll
+        for (int row = B - 2; row > -1; --row)
+#pragma unroll
+            for (int s = 0; s < B; ++s) {
+                T v = T(0);
+#pragma unroll
+                for (int col = row + 1; col < B; ++col) v += X[s * B + col] * LU[col * B + row];
+                X[s * B + row] -= v;
+            }
+    }
+}
+
 // rank_blusgs_pack: blusgs.c:17-45.  rhs goes to the internal SoA arrays;
 // the NS diagonal block starts as (1/dt + a0) I, of which only the scalar
 // dd = 1/dt + a0 is stored (the prepare kernel expands it).

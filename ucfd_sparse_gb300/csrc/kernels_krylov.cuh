@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(256) bsr_spmv_kernel(int bn, int P, const int 
 // LU-factor it (FP64), optionally rounding the factors to Tl.
 template <typename Tl, int B>
 __global__ void pc_prepare_kernel(int bn, const int *perm, const long long *dslot,
-                                  const double *values, double *LU64, Tl *LU_l) {
+                                  const double *values, double *LU64, Tl *LU_l, int factor) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= bn) return;
     constexpr int B2 = B * B;
@@ -100,7 +100,9 @@ __global__ void pc_prepare_kernel(int bn, const int *perm, const long long *dslo
     double d[B2];
 #pragma unroll
     for (int e = 0; e < B2; ++e) d[e] = values[s * B2 + e];
-    ludcmp_dev<double, B>(d);
+    // factor == 0: the diagonal block is already factorised (block ILU) or
+    // kept as it is (scalar ILU)
+    if (factor) ludcmp_dev<double, B>(d);
 #pragma unroll
     for (int e = 0; e < B2; ++e) {
         LU64[(long long)e * bn + k] = d[e];
@@ -108,9 +110,17 @@ __global__ void pc_prepare_kernel(int bn, const int *perm, const long long *dslo
     }
 }
 
-// Forward (lower) step of the block SGS apply for rows [t0, t1) of one
-// level: precon/blusgs.c:104-130 (b -> x' in place).
-template <typename T, int B, int PW>
+// Triangular steps of the preconditioners for the rows [t0, t1) of one
+// level, in place on b.  MODE:
+//   0 block SGS (precon/blusgs.c): lower b_i = inv(D_i)(b_i - sum L_ij b_j)
+//     (104-130), upper b_i -= inv(D_i) sum U_ij b_j (132-161);
+//   1 block ILU(0) (precon/bilu.c:64-129): lower b_i -= sum L_ij b_j,
+//     upper b_i = inv(LU_ii)(b_i - sum U_ij b_j) with the factored diagonal;
+//   2 scalar ILU(0) (precon/ilu.c:49-85): as 1 with B = 1, dividing by the
+//     kept diagonal a_ii (LU holds a_ii, not its reciprocal).
+enum { PC_BLUSGS = 0, PC_BILU = 1, PC_ILU = 2 };
+
+template <typename T, int B, int PW, int MODE>
 __global__ void __launch_bounds__(256) pc_lower_kernel(int t0, int t1, int bn, int PL, const int *Lcol,
                                                        const T *Lval, const T *LU, T *b) {
     const int k = t0 + blockIdx.x * blockDim.x + threadIdx.x;
@@ -120,31 +130,107 @@ __global__ void __launch_bounds__(256) pc_lower_kernel(int t0, int t1, int bn, i
 #pragma unroll
     for (int r = 0; r < B; ++r) arr[r] = b[(long long)k * B + r];
     ell_row_products<T, T, T, B, PW, -1>(k, bn, PL, Lcol, Lval, b, arr);
-    T lu[B2];
+    if constexpr (MODE == PC_BLUSGS) {
+        T lu[B2];
 #pragma unroll
-    for (int e = 0; e < B2; ++e) lu[e] = __ldg(LU + (long long)e * bn + k);
-    lusub_dev<T, B>(lu, arr);
+        for (int e = 0; e < B2; ++e) lu[e] = __ldg(LU + (long long)e * bn + k);
+        lusub_dev<T, B>(lu, arr);
+    }
 #pragma unroll
     for (int r = 0; r < B; ++r) b[(long long)k * B + r] = arr[r];
 }
 
-// Backward (upper) step: precon/blusgs.c:132-161 (x = x' - inv(D) U x).
-template <typename T, int B, int PW>
+template <typename T, int B, int PW, int MODE>
 __global__ void __launch_bounds__(256) pc_upper_kernel(int t0, int t1, int bn, int PU, const int *Ucol,
                                                        const T *Uval, const T *LU, T *b) {
     const int k = t0 + blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= t1) return;
     constexpr int B2 = B * B;
     T arr[B];
+    if constexpr (MODE == PC_BLUSGS) {
 #pragma unroll
-    for (int r = 0; r < B; ++r) arr[r] = T(0);
-    ell_row_products<T, T, T, B, PW, +1>(k, bn, PU, Ucol, Uval, b, arr);
-    T lu[B2];
+        for (int r = 0; r < B; ++r) arr[r] = T(0);
+        ell_row_products<T, T, T, B, PW, +1>(k, bn, PU, Ucol, Uval, b, arr);
+    } else {
 #pragma unroll
-    for (int e = 0; e < B2; ++e) lu[e] = __ldg(LU + (long long)e * bn + k);
-    lusub_dev<T, B>(lu, arr);
+        for (int r = 0; r < B; ++r) arr[r] = b[(long long)k * B + r];
+        ell_row_products<T, T, T, B, PW, -1>(k, bn, PU, Ucol, Uval, b, arr);
+    }
+    if constexpr (MODE == PC_ILU) {
+        static_assert(B == 1, "scalar ILU is B = 1");
+        arr[0] = arr[0] / __ldg(LU + k);
+    } else {
+        T lu[B2];
 #pragma unroll
-    for (int r = 0; r < B; ++r) b[(long long)k * B + r] -= arr[r];
+        for (int e = 0; e < B2; ++e) lu[e] = __ldg(LU + (long long)e * bn + k);
+        lusub_dev<T, B>(lu, arr);
+    }
+#pragma unroll
+    for (int r = 0; r < B; ++r) {
+        if constexpr (MODE == PC_BLUSGS) b[(long long)k * B + r] -= arr[r];
+        else b[(long long)k * B + r] = arr[r];
+    }
+}
+
+// One level of the ILU(0) factorisation in place on the caller's BSR
+// values (row-major B x B blocks in CSR slot order), one thread per row
+// (rows[t] for t in [t0, t1), every lower neighbour already final):
+// precon/bilu.c:5-62 (SCALAR false) or precon/ilu.c:4-47 (SCALAR, B = 1).
+// For each lower slot k of row i in order: A_ik := A_ik inv(A_kk)
+// (lusubmattrans; A_ik / a_kk when SCALAR), then A_ij -= A_ik A_kj for
+// every later slot j whose column row k holds (the last such slot of row k,
+// as the reference's column map keeps); finally the diagonal block is
+// LU-factorised (block ILU only).
+template <int B, bool SCALAR>
+__global__ void ilu_factor_kernel(int t0, int t1, const int *rows, const int *rowptr, const int *colidx,
+                                  const int *diagslots, double *vals) {
+    const int t = t0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= t1) return;
+    constexpr int B2 = B * B;
+    const int i = rows ? rows[t] : t;
+    const int st = rowptr[i], ed = diagslots[i], jed = rowptr[i + 1];
+    for (int kd = st; kd < ed; ++kd) {
+        const int ck = colidx[kd], kk = diagslots[ck], kst = rowptr[ck], ked = rowptr[ck + 1];
+        double aik[B2];
+#pragma unroll
+        for (int e = 0; e < B2; ++e) aik[e] = vals[(long long)kd * B2 + e];
+        if constexpr (SCALAR) {
+            aik[0] = aik[0] / vals[kk];
+        } else {
+            double lu[B2];
+#pragma unroll
+            for (int e = 0; e < B2; ++e) lu[e] = vals[(long long)kk * B2 + e];
+            lusubmattrans_dev<double, B>(lu, aik);
+        }
+#pragma unroll
+        for (int e = 0; e < B2; ++e) vals[(long long)kd * B2 + e] = aik[e];
+        for (int jj = kd + 1; jj < jed; ++jj) {
+            const int cj = colidx[jj];
+            int iwj = -1;
+            for (int q = kst; q < ked; ++q)
+                if (colidx[q] == cj) iwj = q;
+            if (iwj < 0) continue;
+            const double *akj = vals + (long long)iwj * B2;
+            double *aij = vals + (long long)jj * B2;
+#pragma unroll
+            for (int r = 0; r < B; ++r)
+#pragma unroll
+                for (int c = 0; c < B; ++c) {
+                    double v = 0.0;
+#pragma unroll
+                    for (int e = 0; e < B; ++e) v += aik[r * B + e] * akj[e * B + c];
+                    aij[r * B + c] -= v;
+                }
+        }
+    }
+    if constexpr (!SCALAR) {
+        double d[B2];
+#pragma unroll
+        for (int e = 0; e < B2; ++e) d[e] = vals[(long long)ed * B2 + e];
+        ludcmp_dev<double, B>(d);
+#pragma unroll
+        for (int e = 0; e < B2; ++e) vals[(long long)ed * B2 + e] = d[e];
+    }
 }
 
 // Vector permutation / precision change between the caller's order and
@@ -360,6 +446,182 @@ __global__ void __launch_bounds__(256) gm_solution_kernel(long long n, const dou
         for (int q = 0; q < k; ++q) s += V[q * ldv + i] * ys[q];
         x[i] = 1.0 * s + 1.0 * x[i];
     }
+}
+
+// ---- BiCGSTAB ----------------------------------------------------------------
+// BICGSTABSolve (src/krylov/solver/bicgstab.c:24-128) with every scalar on
+// the device: an iteration is a fixed sequence of launches with no host
+// round trip.  Once a breakdown, convergence or the iteration limit is
+// recorded (stop), every later kernel of the sequence returns at once, so
+// the host may queue several iterations between its checks.
+struct BcState {
+    double rho, rhoprev, alpha, omega, rho_new, resnorm;
+    int iter, stop, stat, conv;
+};
+
+// Per-block partial sums of (x, y) into part[block] (grid-stride).
+__global__ void __launch_bounds__(256) bc_dot_kernel(long long n, const double *x, const double *y, double *part,
+                                                     const BcState *st) {
+    if (st && st->stop) return;
+    double t = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        t += x[i] * y[i];
+    t = block_sum(t);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+// rho_0 = (r~, r_0), rhoprev = alpha = omega = 1 (bicgstab.c:52-56); a
+// rho breakdown (|rho| < 1e-30, bicgstab.c:59-62) ends the solve.
+__global__ void bc_start_kernel(int nb, const double *part, BcState *st, int maxiter) {
+    double rho = 0.0;
+    for (int b = 0; b < nb; ++b) rho += part[b];
+    st->rho = rho;
+    st->rhoprev = 1.0;
+    st->alpha = 1.0;
+    st->omega = 1.0;
+    st->rho_new = 0.0;
+    st->resnorm = 0.0;
+    st->iter = 0;
+    st->stop = 0;
+    st->stat = -1;
+    st->conv = 0;
+    if (fabs(rho) < 1e-30) {
+        st->stat = 3;
+        st->stop = 1;
+    } else if (maxiter <= 0) {
+        st->stop = 1;
+    }
+}
+
+// p := r (first iteration) or r + beta (p - omega v) as daxpy, dscal, daxpy
+// (bicgstab.c:68-75); pt := p (the preconditioner then works on pt).
+__global__ void __launch_bounds__(256) bc_direction_kernel(long long n, const BcState *st, const double *r,
+                                                           const double *v, double *p, double *pt) {
+    if (st->stop) return;
+    const bool first = st->iter == 0;
+    const double omega = st->omega;
+    const double beta = first ? 0.0 : (st->rho / st->rhoprev) * (st->alpha / st->omega);
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        double q;
+        if (first) {
+            q = r[i];
+        } else {
+            q = p[i] + (-omega) * v[i];
+            q = beta * q;
+            q = q + 1.0 * r[i];
+        }
+        p[i] = q;
+        pt[i] = q;
+    }
+}
+
+// pi = (r~, v); alpha = rho / pi, or a pi breakdown (bicgstab.c:81-86).
+__global__ void bc_alpha_kernel(int nb, const double *part, BcState *st) {
+    if (st->stop) return;
+    double pi = 0.0;
+    for (int b = 0; b < nb; ++b) pi += part[b];
+    if (fabs(pi) < 1e-30) {
+        st->stat = 4;
+        st->stop = 1;
+    } else {
+        st->alpha = st->rho / pi;
+    }
+}
+
+// s := r - alpha v, shat := s (bicgstab.c:89-94).
+__global__ void __launch_bounds__(256) bc_s_kernel(long long n, const BcState *st, const double *r,
+                                                   const double *v, double *sv, double *shat) {
+    if (st->stop) return;
+    const double a = st->alpha;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double q = r[i] + (-a) * v[i];
+        sv[i] = q;
+        shat[i] = q;
+    }
+}
+
+// The fused five-term reduction of bicgstab.c:5-22: per-block partials of
+// (r~,s), (r~,t), (t,s), (t,t), (s,s) into part[5*block + j].
+__global__ void __launch_bounds__(256) bc_fused5_kernel(long long n, const double *rt, const double *sv,
+                                                        const double *t, double *part, const BcState *st) {
+    if (st->stop) return;
+    double a = 0.0, b = 0.0, c = 0.0, d = 0.0, e = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double sk = sv[i], tk = t[i], rk = rt[i];
+        a += rk * sk;
+        b += rk * tk;
+        c += tk * sk;
+        d += tk * tk;
+        e += sk * sk;
+    }
+    a = block_sum(a);
+    b = block_sum(b);
+    c = block_sum(c);
+    d = block_sum(d);
+    e = block_sum(e);
+    if (threadIdx.x == 0) {
+        double *q = part + 5ll * blockIdx.x;
+        q[0] = a;
+        q[1] = b;
+        q[2] = c;
+        q[3] = d;
+        q[4] = e;
+    }
+}
+
+// omega = (t,s)/(t,t), rho_new = phi - omega (r~,t) and the residual
+// estimate sqrt|ss - 2 omega ts + omega^2 tt| (bicgstab.c:101-118);
+// conv when it is below tol.
+__global__ void bc_omega_kernel(int nb, const double *part, BcState *st, double tol, double *hist) {
+    if (st->stop) return;
+    double phi = 0.0, rtt = 0.0, ts = 0.0, tt = 0.0, ss = 0.0;
+    for (int b = 0; b < nb; ++b) {
+        const double *q = part + 5ll * b;
+        phi += q[0];
+        rtt += q[1];
+        ts += q[2];
+        tt += q[3];
+        ss += q[4];
+    }
+    const double omega = ts / tt;
+    st->omega = omega;
+    st->rho_new = phi - omega * rtt;
+    const double res = sqrt(fabs(ss - 2.0 * omega * ts + omega * omega * tt));
+    st->resnorm = res;
+    if (hist) hist[st->iter] = res;
+    st->conv = res < tol ? 1 : 0;
+}
+
+// x += alpha pt; x += omega shat; r := s - omega t (bicgstab.c:106-112).
+__global__ void __launch_bounds__(256) bc_update_kernel(long long n, const BcState *st, const double *pt,
+                                                        const double *shat, const double *sv, const double *t,
+                                                        double *x, double *r) {
+    if (st->stop) return;
+    const double a = st->alpha, w = st->omega;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        double xi = x[i] + a * pt[i];
+        x[i] = xi + w * shat[i];
+        r[i] = sv[i] + (-w) * t[i];
+    }
+}
+
+// Converged, or rhoprev = rho, rho = rho_new, iter++ (bicgstab.c:120-128).
+__global__ void bc_advance_kernel(BcState *st, int maxiter) {
+    if (st->stop) return;
+    if (st->conv) {
+        st->stat = 0;
+        st->stop = 1;
+        return;
+    }
+    st->rhoprev = st->rho;
+    st->rho = st->rho_new;
+    st->iter += 1;
+    if (st->iter >= maxiter) st->stop = 1;
 }
 
 }  // namespace UCFD_KNS

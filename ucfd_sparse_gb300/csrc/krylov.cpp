@@ -126,6 +126,7 @@ struct _Precon {
     int *rowptr = nullptr, *colidx = nullptr, *diagslots = nullptr;
     double *values = nullptr;
     int bn = 0, blk = 0, ncolors = 0;
+    int kind = 0;  // PC_BLUSGS (0), PC_BILU (1), PC_ILU (2) of kernels_krylov.cuh
     std::vector<int> icolors;
     bool colored = false, none = false;
     int prec = UCFD_PREC_FP64;
@@ -156,6 +157,14 @@ struct _Precon {
         }
         for (size_t q = 0; q < ci.size(); ++q)
             UCFD_REQUIRE(ci[q] >= 0 && ci[q] < bn, "colidx[%zu] = %d out of range", q, ci[q]);
+        if (kind != 0) {
+            // the ILU types pair "before the diagonal slot" with "lower row"
+            for (int i = 0; i < bn; ++i)
+                for (int q = rp[i]; q < rp[i + 1]; ++q)
+                    UCFD_REQUIRE(q == ds[i] || (q < ds[i]) == (ci[q] < i),
+                                 "row %d: an ILU preconditioner needs columns below the diagonal before its slot "
+                                 "and columns above it after", i);
+        }
         to_host(values, (size_t)rp[bn] * blk * blk, v);
         if (colored) {
             // colour c = rows [icolors[c], icolors[c+1]); no row may reference
@@ -185,6 +194,7 @@ struct _Precon {
         }
         std::vector<int> end(rp.begin() + 1, rp.end());
         const bool fp32 = prec == UCFD_PREC_FP32;
+        if (kind != 0) factorize(rp, ci, ds, v, s);
         const int *pm = identity ? nullptr : sch.perm.data();
         const int *ip = identity ? nullptr : sch.iperm.data();
         L.build(bn, blk, rp, ci, v, pm, ip, &lo, &mid, fp32, s);
@@ -196,17 +206,47 @@ struct _Precon {
         // the values for the LU come from the caller's array (device view)
         DevBuf<double> vals;
         vals.upload(v.data(), v.size(), s);
+        const int fac = kind == 0 ? 1 : 0;  // the ILU types arrive factored
         if (fp32) {
             LU32.ensure(B2 * bn);
-            kfast::pc_prepare<float>(blk, bn, identity ? nullptr : perm.p, dslot.p, vals.p, LU64.p, LU32.p, s);
+            kfast::pc_prepare<float>(blk, bn, identity ? nullptr : perm.p, dslot.p, vals.p, LU64.p, LU32.p, fac, s);
         } else if (prec == UCFD_PREC_FP64) {
-            kexact::pc_prepare<double>(blk, bn, identity ? nullptr : perm.p, dslot.p, vals.p, LU64.p, nullptr, s);
+            kexact::pc_prepare<double>(blk, bn, identity ? nullptr : perm.p, dslot.p, vals.p, LU64.p, nullptr, fac,
+                                       s);
         } else {
-            kfast::pc_prepare<double>(blk, bn, identity ? nullptr : perm.p, dslot.p, vals.p, LU64.p, nullptr, s);
+            kfast::pc_prepare<double>(blk, bn, identity ? nullptr : perm.p, dslot.p, vals.p, LU64.p, nullptr, fac, s);
         }
         UCFD_CHECK_LAUNCH();
         UCFD_CUDA(cudaStreamSynchronize(s));
         prepared = true;
+    }
+
+    // ILU(0) factorisation on the device, level by level of the schedule
+    // (each row once its lower neighbours are final: the sequential result),
+    // in FP64; the factors replace v and, as in the reference, the caller's
+    // values array.
+    void factorize(const std::vector<int> &rp, const std::vector<int> &ci, const std::vector<int> &ds,
+                   std::vector<double> &v, cudaStream_t s) {
+        DevBuf<int> d_rp, d_ci, d_ds, d_rows;
+        DevBuf<double> d_v;
+        d_rp.upload(rp.data(), rp.size(), s);
+        d_ci.upload(ci.data(), ci.size(), s);
+        d_ds.upload(ds.data(), ds.size(), s);
+        d_rows.upload(sch.perm.data(), sch.perm.size(), s);
+        d_v.upload(v.data(), v.size(), s);
+        const int scalar = kind == 2 ? 1 : 0;
+        for (int l = 0; l < sch.nlev; ++l) {
+            if (prec == UCFD_PREC_FP64)
+                kexact::ilu_factor(blk, scalar, sch.lev_off[l], sch.lev_off[l + 1], d_rows.p, d_rp.p, d_ci.p, d_ds.p,
+                                   d_v.p, s);
+            else
+                kfast::ilu_factor(blk, scalar, sch.lev_off[l], sch.lev_off[l + 1], d_rows.p, d_rp.p, d_ci.p, d_ds.p,
+                                  d_v.p, s);
+        }
+        UCFD_CHECK_LAUNCH();
+        UCFD_CUDA(cudaMemcpyAsync(v.data(), d_v.p, v.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+        UCFD_CUDA(cudaMemcpyAsync(values, d_v.p, v.size() * sizeof(double), cudaMemcpyDefault, s));
+        UCFD_CUDA(cudaStreamSynchronize(s));
     }
 
     // In-place apply to a device vector b [bn*blk] (FP64).
@@ -220,10 +260,10 @@ struct _Precon {
             kfast::gather_rows<double, float>(bn, blk, identity ? nullptr : perm.p, b, x, s);
             for (int l = 0; l < L_; ++l)
                 kfast::pc_lower<float>(blk, sch.lev_off[l], sch.lev_off[l + 1], bn, L.P, L.col.p, L.val32.p, LU32.p, x,
-                                       0, s);
+                                       0, kind, s);
             for (int l = L_ - 1; l >= 0; --l)
                 kfast::pc_upper<float>(blk, sch.lev_off[l], sch.lev_off[l + 1], bn, U.P, U.col.p, U.val32.p, LU32.p, x,
-                                       0, s);
+                                       0, kind, s);
             kfast::scatter_rows<float, double>(bn, blk, identity ? nullptr : perm.p, x, b, s);
         } else {
             double *x = b;
@@ -235,18 +275,18 @@ struct _Precon {
             for (int l = 0; l < L_; ++l) {
                 if (ex)
                     kexact::pc_lower<double>(blk, sch.lev_off[l], sch.lev_off[l + 1], bn, L.P, L.col.p, L.val.p,
-                                             LU64.p, x, 0, s);
+                                             LU64.p, x, 0, kind, s);
                 else
                     kfast::pc_lower<double>(blk, sch.lev_off[l], sch.lev_off[l + 1], bn, L.P, L.col.p, L.val.p,
-                                            LU64.p, x, 0, s);
+                                            LU64.p, x, 0, kind, s);
             }
             for (int l = L_ - 1; l >= 0; --l) {
                 if (ex)
                     kexact::pc_upper<double>(blk, sch.lev_off[l], sch.lev_off[l + 1], bn, U.P, U.col.p, U.val.p,
-                                             LU64.p, x, 0, s);
+                                             LU64.p, x, 0, kind, s);
                 else
                     kfast::pc_upper<double>(blk, sch.lev_off[l], sch.lev_off[l + 1], bn, U.P, U.col.p, U.val.p,
-                                            LU64.p, x, 0, s);
+                                            LU64.p, x, 0, kind, s);
             }
             if (!identity) kfast::scatter_rows<double, double>(bn, blk, perm.p, x, b, s);
         }
@@ -276,6 +316,11 @@ struct _Solver {
     DevBuf<double> sx, sb;
     PinnedBuf<double> h_abeta;
     PinnedBuf<unsigned char> h_st;
+    // BiCGSTAB (bicgstab.h:6-9): r, r~, p, pt, v, s, shat, t, reductions, state
+    bool bicg = false;
+    DevBuf<double> br, brt, bp, bpt, bv, bs, bsh, bt, bpart, bhist;
+    DevBuf<unsigned char> bst;
+    PinnedBuf<unsigned char> h_bst;
 
     void alloc() {
         ldv = ((long long)n + 31) / 32 * 32;
@@ -294,8 +339,73 @@ struct _Solver {
         h_st.ensure(kfast::gm_state_bytes());
     }
 
+    // bicgstab.c:24-128 on the device: every scalar lives in a device state
+    // (kernels_krylov.cuh BcState); the host queues kChunk iterations between
+    // its reads of the stop flag, the kernels of iterations queued after a
+    // stop return at once (the preconditioner and matvec of those only touch
+    // scratch vectors).
+    void solve_bicgstab(SpMat A, Precon pc, double *x, const double *b, cudaStream_t s) {
+        constexpr int kChunk = 4;
+        const long long nn = n;
+        const int nb = kfast::gm_blocks(nn);
+        for (DevBuf<double> *v : {&br, &brt, &bp, &bpt, &bv, &bs, &bsh, &bt}) v->ensure((size_t)n);
+        bpart.ensure((size_t)5 * nb);
+        bst.ensure(kfast::bc_state_bytes());
+        h_bst.ensure(kfast::bc_state_bytes());
+        double *hist_d = nullptr;
+        if (trace && maxiter > 0) {
+            hist.assign(maxiter, 0.0);
+            hist_d = bhist.ensure((size_t)maxiter);
+            UCFD_CUDA(cudaMemsetAsync(hist_d, 0, (size_t)maxiter * sizeof(double), s));
+        }
+        // r = b - A x, r~ = r, rho = (r~, r)
+        UCFD_CUDA(cudaMemcpyAsync(br.p, b, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        A->mult(-1.0, x, 1.0, br.p, false, s);
+        UCFD_CUDA(cudaMemcpyAsync(brt.p, br.p, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        kfast::bc_dot(nn, brt.p, br.p, bpart.p, nullptr, s);
+        kfast::bc_start(nb, bpart.p, bst.p, maxiter, s);
+        struct HostState {
+            double rho, rhoprev, alpha, omega, rho_new, resnorm;
+            int iter, stop, stat, conv;
+        };
+        static_assert(sizeof(HostState) == 64, "device state layout");
+        HostState h{};
+        int queued = 0;
+        for (;;) {
+            for (int q = 0; q < kChunk && queued < maxiter; ++q, ++queued) {
+                kfast::bc_direction(nn, bst.p, br.p, bv.p, bp.p, bpt.p, s);
+                pc->apply(bpt.p, s);
+                A->mult(1.0, bpt.p, 0.0, bv.p, false, s);
+                kfast::bc_dot(nn, brt.p, bv.p, bpart.p, bst.p, s);
+                kfast::bc_alpha(nb, bpart.p, bst.p, s);
+                kfast::bc_s(nn, bst.p, br.p, bv.p, bs.p, bsh.p, s);
+                pc->apply(bsh.p, s);
+                A->mult(1.0, bsh.p, 0.0, bt.p, false, s);
+                kfast::bc_fused5(nn, brt.p, bs.p, bt.p, bpart.p, bst.p, s);
+                kfast::bc_omega(nb, bpart.p, bst.p, tol, hist_d, s);
+                kfast::bc_update(nn, bst.p, bpt.p, bsh.p, bs.p, bt.p, x, br.p, s);
+                kfast::bc_advance(bst.p, maxiter, s);
+            }
+            UCFD_CHECK_LAUNCH();
+            UCFD_CUDA(cudaMemcpyAsync(h_bst.p, bst.p, sizeof(HostState), cudaMemcpyDeviceToHost, s));
+            UCFD_CUDA(cudaStreamSynchronize(s));
+            std::memcpy(&h, h_bst.p, sizeof(HostState));
+            if (h.stop || queued >= maxiter) break;
+        }
+        itnum = h.iter;
+        residual = h.resnorm;
+        stat = h.stat;
+        if (h.iter == maxiter) stat = REACH_ITERMAX;
+        if (hist_d)
+            UCFD_CUDA(cudaMemcpy(hist.data(), hist_d, (size_t)maxiter * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+
     // gmres.c:42-129 on the device.
     void solve(SpMat A, Precon pc, double *x, const double *b, cudaStream_t s) {
+        if (bicg) {
+            solve_bicgstab(A, pc, x, b, s);
+            return;
+        }
         const int ld = m + 1;
         const int nb = kfast::gm_blocks(n);
         const bool mixed = prec == UCFD_PREC_FP32;
@@ -493,6 +603,7 @@ static ucfd_status_t pc_set(Precon *pc, const char *type, UCFDInt bn, UCFDInt bl
     UCFD_REQUIRE(bn > 0 && block > 0 && block <= 7, "bad sizes bn=%d block=%d", bn, block);
     Precon p = *pc;
     p->type_name = type;
+    p->kind = 0;
     p->bn = bn;
     p->blk = block;
     p->colored = icolors != nullptr;
@@ -515,6 +626,25 @@ ucfd_status_t UCFDPreconSetPBLUSGS(Precon *pc, UCFDInt bn, UCFDInt block, UCFDIn
 ucfd_status_t UCFDPreconSetCUDABLUSGS(Precon *pc, UCFDInt bn, UCFDInt block, UCFDInt ncolors, UCFDInt *icolors) {
     if (!icolors) return UCFD_ERR_ARGUMENT;
     return pc_set(pc, CUDABLUSGS, bn, block, ncolors, icolors);
+}
+
+static ucfd_status_t pc_set_ilu(Precon *pc, const char *type, int kind, UCFDInt bn, UCFDInt block,
+                                UCFDInt ncolors, UCFDInt *icolors) {
+    const ucfd_status_t st = pc_set(pc, type, bn, block, ncolors, icolors);
+    if (st == UCFD_SUCCESS) (*pc)->kind = kind;
+    return st;
+}
+ucfd_status_t UCFDPreconSetILU(Precon *pc, UCFDInt n) { return pc_set_ilu(pc, ILU, 2, n, 1, 0, nullptr); }
+ucfd_status_t UCFDPreconSetBILU(Precon *pc, UCFDInt bn, UCFDInt block) {
+    return pc_set_ilu(pc, BILU, 1, bn, block, 0, nullptr);
+}
+ucfd_status_t UCFDPreconSetPBILU(Precon *pc, UCFDInt bn, UCFDInt block, UCFDInt ncolors, UCFDInt *icolors) {
+    if (!icolors) return UCFD_ERR_ARGUMENT;
+    return pc_set_ilu(pc, PBILU, 1, bn, block, ncolors, icolors);
+}
+ucfd_status_t UCFDPreconSetCUDABILU(Precon *pc, UCFDInt bn, UCFDInt block, UCFDInt ncolors, UCFDInt *icolors) {
+    if (!icolors) return UCFD_ERR_ARGUMENT;
+    return pc_set_ilu(pc, CUDABILU, 1, bn, block, ncolors, icolors);
 }
 
 ucfd_status_t UCFDPreconSetPrecision(Precon pc, int precision) {
@@ -593,6 +723,21 @@ static ucfd_status_t gmres_create(Solver *solver, UCFDInt n, UCFDInt m, UCFDInt 
 
 ucfd_status_t UCFDSolverCreateGMRES(Solver *solver, UCFDInt n, UCFDInt m, UCFDInt maxiter, UCFDReal tol) {
     return gmres_create(solver, n, m, maxiter, tol);
+}
+
+ucfd_status_t UCFDSolverCreateBICGSTAB(Solver *solver, UCFDInt n, UCFDInt maxiter, UCFDReal tol) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(solver, "null Solver pointer");
+    UCFD_REQUIRE(n > 0 && maxiter >= 0, "bad BiCGSTAB sizes n=%d maxiter=%d", n, maxiter);
+    ensure_device();
+    std::unique_ptr<_Solver> s(new _Solver());
+    s->type_name = BICGSTAB;
+    s->bicg = true;
+    s->n = n;
+    s->maxiter = maxiter;
+    s->tol = tol;
+    *solver = s.release();
+    UCFD_API_END
 }
 ucfd_status_t UCFDSolverCreateCUDAGMRES(Solver *solver, UCFDInt n, UCFDInt m, UCFDInt maxiter, UCFDReal tol) {
     return gmres_create(solver, n, m, maxiter, tol);

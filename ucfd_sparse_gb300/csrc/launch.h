@@ -79,13 +79,15 @@
                   const double *x, double beta, double *y, int block, cudaStream_t s);             \
     template <typename Tl>                                                                         \
     void pc_prepare(int B, int bn, const int *perm, const long long *dslot, const double *values,  \
-                    double *LU64, Tl *LU_l, cudaStream_t s);                                       \
+                    double *LU64, Tl *LU_l, int factor, cudaStream_t s);                           \
     template <typename T>                                                                          \
     void pc_lower(int B, int t0, int t1, int bn, int PL, const int *Lcol, const T *Lval,           \
-                  const T *LU, T *b, int block, cudaStream_t s);                                   \
+                  const T *LU, T *b, int block, int mode, cudaStream_t s);                         \
     template <typename T>                                                                          \
     void pc_upper(int B, int t0, int t1, int bn, int PU, const int *Ucol, const T *Uval,           \
-                  const T *LU, T *b, int block, cudaStream_t s);                                   \
+                  const T *LU, T *b, int block, int mode, cudaStream_t s);                         \
+    void ilu_factor(int B, int scalar, int t0, int t1, const int *rows, const int *rowptr,         \
+                    const int *colidx, const int *diagslots, double *vals, cudaStream_t s);        \
     template <typename Ts, typename Td>                                                            \
     void gather_rows(int bn, int B, const int *perm, const Ts *src, Td *dst, cudaStream_t s);      \
     template <typename Ts, typename Td>                                                            \
@@ -125,6 +127,22 @@
     void gm_solution(long long n, const double *V, long long ldv, const double *y,                 \
                      const void *st, double *x, cudaStream_t s);                                   \
     size_t gm_state_bytes();                                                                       \
+    /* ---- BiCGSTAB pieces ---- */                                                                \
+    size_t bc_state_bytes();                                                                       \
+    void bc_dot(long long n, const double *x, const double *y, double *part, const void *st,       \
+                cudaStream_t s);                                                                   \
+    void bc_start(int nb, const double *part, void *st, int maxiter, cudaStream_t s);              \
+    void bc_direction(long long n, const void *st, const double *r, const double *v, double *p,   \
+                      double *pt, cudaStream_t s);                                                 \
+    void bc_alpha(int nb, const double *part, void *st, cudaStream_t s);                           \
+    void bc_s(long long n, const void *st, const double *r, const double *v, double *sv,          \
+              double *shat, cudaStream_t s);                                                       \
+    void bc_fused5(long long n, const double *rt, const double *sv, const double *t, double *part, \
+                   const void *st, cudaStream_t s);                                                \
+    void bc_omega(int nb, const double *part, void *st, double tol, double *hist, cudaStream_t s);  \
+    void bc_update(long long n, const void *st, const double *pt, const double *shat,             \
+                   const double *sv, const double *t, double *x, double *r, cudaStream_t s);       \
+    void bc_advance(void *st, int maxiter, cudaStream_t s);                                        \
     void norm2_to(long long n, const double *x, double *part, double *out, cudaStream_t s);
 
 namespace kexact {

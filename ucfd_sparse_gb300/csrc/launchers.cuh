@@ -428,44 +428,74 @@ void bsr_spmv(int B, int bn, int P, const int *col, const Tv *val, double alpha,
 
 template <typename Tl>
 void pc_prepare(int B, int bn, const int *perm, const long long *dslot, const double *values,
-                double *LU64, Tl *LU_l, cudaStream_t s) {
+                double *LU64, Tl *LU_l, int factor, cudaStream_t s) {
     if (bn <= 0) return;
     UCFD_KSW(B, (pc_prepare_kernel<Tl, BB><<<grid_for(bn, 128), 128, 0, s>>>(bn, perm, dslot, values, LU64,
-                                                                             LU_l)));
+                                                                             LU_l, factor)));
+}
+
+// Triangular steps, mode PC_BLUSGS / PC_BILU / PC_ILU (kernels_krylov.cuh).
+template <typename T, int MODE, bool LOWER>
+static void pc_step_go(int B, unsigned g, int block, cudaStream_t s, int t0, int t1, int bn, int P,
+                       const int *col, const T *val, const T *LU, T *b) {
+    if constexpr (MODE == PC_ILU) {
+        if (B != 1) ::ucfd::fail(UCFD_ERR_ARGUMENT, "scalar ILU needs block size 1 (got %d)", B);
+        if constexpr (LOWER) pc_lower_kernel<T, 1, 0, MODE><<<g, block, 0, s>>>(t0, t1, bn, P, col, val, LU, b);
+        else pc_upper_kernel<T, 1, 0, MODE><<<g, block, 0, s>>>(t0, t1, bn, P, col, val, LU, b);
+        return;
+    } else {
+        if (B == 5 && P <= 6) {
+            if (P <= 4) {
+                if constexpr (LOWER) pc_lower_kernel<T, 5, 4, MODE><<<g, block, 0, s>>>(t0, t1, bn, P, col, val, LU, b);
+                else pc_upper_kernel<T, 5, 4, MODE><<<g, block, 0, s>>>(t0, t1, bn, P, col, val, LU, b);
+            } else {
+                if constexpr (LOWER) pc_lower_kernel<T, 5, 6, MODE><<<g, block, 0, s>>>(t0, t1, bn, P, col, val, LU, b);
+                else pc_upper_kernel<T, 5, 6, MODE><<<g, block, 0, s>>>(t0, t1, bn, P, col, val, LU, b);
+            }
+            return;
+        }
+        if constexpr (LOWER) {
+            UCFD_KSW(B, (pc_lower_kernel<T, BB, 0, MODE><<<g, block, 0, s>>>(t0, t1, bn, P, col, val, LU, b)));
+        } else {
+            UCFD_KSW(B, (pc_upper_kernel<T, BB, 0, MODE><<<g, block, 0, s>>>(t0, t1, bn, P, col, val, LU, b)));
+        }
+    }
+}
+
+template <typename T, bool LOWER>
+static void pc_step(int B, int t0, int t1, int bn, int P, const int *col, const T *val, const T *LU, T *b,
+                    int block, int mode, cudaStream_t s) {
+    if (t1 <= t0) return;
+    if (block <= 0) block = kBlock;
+    const unsigned g = grid_for(t1 - t0, block);
+    if (mode == PC_BILU) pc_step_go<T, PC_BILU, LOWER>(B, g, block, s, t0, t1, bn, P, col, val, LU, b);
+    else if (mode == PC_ILU) pc_step_go<T, PC_ILU, LOWER>(B, g, block, s, t0, t1, bn, P, col, val, LU, b);
+    else pc_step_go<T, PC_BLUSGS, LOWER>(B, g, block, s, t0, t1, bn, P, col, val, LU, b);
 }
 
 template <typename T>
 void pc_lower(int B, int t0, int t1, int bn, int PL, const int *Lcol, const T *Lval, const T *LU, T *b,
-              int block, cudaStream_t s) {
-    if (t1 <= t0) return;
-    if (block <= 0) block = kBlock;
-    const unsigned g = grid_for(t1 - t0, block);
-    if (B == 5 && PL <= 4) {
-        pc_lower_kernel<T, 5, 4><<<g, block, 0, s>>>(t0, t1, bn, PL, Lcol, Lval, LU, b);
-        return;
-    }
-    if (B == 5 && PL <= 6) {
-        pc_lower_kernel<T, 5, 6><<<g, block, 0, s>>>(t0, t1, bn, PL, Lcol, Lval, LU, b);
-        return;
-    }
-    UCFD_KSW(B, (pc_lower_kernel<T, BB, 0><<<g, block, 0, s>>>(t0, t1, bn, PL, Lcol, Lval, LU, b)));
+              int block, int mode, cudaStream_t s) {
+    pc_step<T, true>(B, t0, t1, bn, PL, Lcol, Lval, LU, b, block, mode, s);
 }
 
 template <typename T>
 void pc_upper(int B, int t0, int t1, int bn, int PU, const int *Ucol, const T *Uval, const T *LU, T *b,
-              int block, cudaStream_t s) {
+              int block, int mode, cudaStream_t s) {
+    pc_step<T, false>(B, t0, t1, bn, PU, Ucol, Uval, LU, b, block, mode, s);
+}
+
+// One level of the ILU(0) factorisation (rows[t], t in [t0, t1)).
+void ilu_factor(int B, int scalar, int t0, int t1, const int *rows, const int *rowptr, const int *colidx,
+                const int *diagslots, double *vals, cudaStream_t s) {
     if (t1 <= t0) return;
-    if (block <= 0) block = kBlock;
-    const unsigned g = grid_for(t1 - t0, block);
-    if (B == 5 && PU <= 4) {
-        pc_upper_kernel<T, 5, 4><<<g, block, 0, s>>>(t0, t1, bn, PU, Ucol, Uval, LU, b);
+    const unsigned g = grid_for(t1 - t0, 128);
+    if (scalar) {
+        if (B != 1) ::ucfd::fail(UCFD_ERR_ARGUMENT, "scalar ILU needs block size 1 (got %d)", B);
+        ilu_factor_kernel<1, true><<<g, 128, 0, s>>>(t0, t1, rows, rowptr, colidx, diagslots, vals);
         return;
     }
-    if (B == 5 && PU <= 6) {
-        pc_upper_kernel<T, 5, 6><<<g, block, 0, s>>>(t0, t1, bn, PU, Ucol, Uval, LU, b);
-        return;
-    }
-    UCFD_KSW(B, (pc_upper_kernel<T, BB, 0><<<g, block, 0, s>>>(t0, t1, bn, PU, Ucol, Uval, LU, b)));
+    UCFD_KSW(B, (ilu_factor_kernel<BB, false><<<g, 128, 0, s>>>(t0, t1, rows, rowptr, colidx, diagslots, vals)));
 }
 
 template <typename Ts, typename Td>
@@ -604,6 +634,41 @@ __global__ void norm_finalize_kernel(int nblocks, const double *part, double *ou
 void norm2_to(long long n, const double *x, double *part, double *out, cudaStream_t s) {
     gm_sumsq_kernel<<<gm_blocks(n), kBlock, 0, s>>>(n, x, part);
     norm_finalize_kernel<<<1, 1, 0, s>>>(gm_blocks(n), part, out);
+}
+
+// ---- BiCGSTAB ----------------------------------------------------------------
+size_t bc_state_bytes() { return sizeof(BcState); }
+
+void bc_dot(long long n, const double *x, const double *y, double *part, const void *st, cudaStream_t s) {
+    bc_dot_kernel<<<gm_blocks(n), kBlock, 0, s>>>(n, x, y, part, (const BcState *)st);
+}
+void bc_start(int nb, const double *part, void *st, int maxiter, cudaStream_t s) {
+    bc_start_kernel<<<1, 1, 0, s>>>(nb, part, (BcState *)st, maxiter);
+}
+void bc_direction(long long n, const void *st, const double *r, const double *v, double *p, double *pt,
+                  cudaStream_t s) {
+    bc_direction_kernel<<<gm_blocks(n), kBlock, 0, s>>>(n, (const BcState *)st, r, v, p, pt);
+}
+void bc_alpha(int nb, const double *part, void *st, cudaStream_t s) {
+    bc_alpha_kernel<<<1, 1, 0, s>>>(nb, part, (BcState *)st);
+}
+void bc_s(long long n, const void *st, const double *r, const double *v, double *sv, double *shat,
+          cudaStream_t s) {
+    bc_s_kernel<<<gm_blocks(n), kBlock, 0, s>>>(n, (const BcState *)st, r, v, sv, shat);
+}
+void bc_fused5(long long n, const double *rt, const double *sv, const double *t, double *part, const void *st,
+               cudaStream_t s) {
+    bc_fused5_kernel<<<gm_blocks(n), kBlock, 0, s>>>(n, rt, sv, t, part, (const BcState *)st);
+}
+void bc_omega(int nb, const double *part, void *st, double tol, double *hist, cudaStream_t s) {
+    bc_omega_kernel<<<1, 1, 0, s>>>(nb, part, (BcState *)st, tol, hist);
+}
+void bc_update(long long n, const void *st, const double *pt, const double *shat, const double *sv,
+               const double *t, double *x, double *r, cudaStream_t s) {
+    bc_update_kernel<<<gm_blocks(n), kBlock, 0, s>>>(n, (const BcState *)st, pt, shat, sv, t, x, r);
+}
+void bc_advance(void *st, int maxiter, cudaStream_t s) {
+    bc_advance_kernel<<<1, 1, 0, s>>>((BcState *)st, maxiter);
 }
 
 }  // namespace UCFD_KNS

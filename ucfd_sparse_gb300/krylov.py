@@ -57,6 +57,18 @@ class Precon:
         call("UCFDPreconSetCUDABLUSGS" if cuda else "UCFDPreconSetPBLUSGS", byref(self._h), bn, block, ncolors,
              ptr(icolors))
 
+    def set_bilu(self, bn, block):
+        call("UCFDPreconSetBILU", byref(self._h), bn, block)
+
+    def set_pbilu(self, bn, block, ncolors, icolors, cuda=False):
+        icolors = np.ascontiguousarray(icolors, dtype=np.int32)
+        self._keep.append(icolors)
+        call("UCFDPreconSetCUDABILU" if cuda else "UCFDPreconSetPBILU", byref(self._h), bn, block, ncolors,
+             ptr(icolors))
+
+    def set_ilu(self, n):
+        call("UCFDPreconSetILU", byref(self._h), n)
+
     def set_precision(self, prec):
         call("UCFDPreconSetPrecision", self._h, prec)
 
@@ -83,10 +95,16 @@ class Precon:
 
 
 class Solver:
-    def __init__(self, n, m, maxiter, tol, cuda=False):
+    """GMRES(m) (the default) or, with kind="bicgstab", BiCGSTAB (m unused)."""
+
+    def __init__(self, n, m, maxiter, tol, cuda=False, kind="gmres"):
         load()
         self._h = c_void_p()
-        call("UCFDSolverCreateCUDAGMRES" if cuda else "UCFDSolverCreateGMRES", byref(self._h), n, m, maxiter, tol)
+        if kind == "bicgstab":
+            call("UCFDSolverCreateBICGSTAB", byref(self._h), n, maxiter, tol)
+        else:
+            call("UCFDSolverCreateCUDAGMRES" if cuda else "UCFDSolverCreateGMRES", byref(self._h), n, m, maxiter,
+                 tol)
         self.maxiter = maxiter
 
     def set_precision(self, prec):

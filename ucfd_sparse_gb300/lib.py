@@ -141,6 +141,11 @@ SIGNATURES = {
     "UCFDSolverTraceResidualHistory": (_I, [_P]),
     "UCFDSolverGetResidualHistory": (_I, [_P, _P]),
     "UCFDSolverCreateGMRES": (_I, [POINTER(c_void_p), _I, _I, _I, _D]),
+    "UCFDSolverCreateBICGSTAB": (_I, [POINTER(c_void_p), _I, _I, _D]),
+    "UCFDPreconSetILU": (_I, [POINTER(c_void_p), _I]),
+    "UCFDPreconSetBILU": (_I, [POINTER(c_void_p), _I, _I]),
+    "UCFDPreconSetPBILU": (_I, [POINTER(c_void_p), _I, _I, _I, _P]),
+    "UCFDPreconSetCUDABILU": (_I, [POINTER(c_void_p), _I, _I, _I, _P]),
     "UCFDSolverCreateCUDAGMRES": (_I, [POINTER(c_void_p), _I, _I, _I, _D]),
     "UCFDSolverSetPrecision": (_I, [_P, _I]),
     "UCFDSolverSetHappyTol": (_I, [_P, _D]),
