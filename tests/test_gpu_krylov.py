@@ -260,3 +260,99 @@ def test_bicgstab_coloured_reaches_tolerance(pc_kind, port, ucfd):
     r = b.clone()
     A.mult(-1.0, x, 1.0, r)
     assert float(torch.linalg.norm(r)) <= 10 * tol
+
+
+def _fill(dst, src):
+    """Writes src into the caller-owned array dst in place (host or device)."""
+    if isinstance(dst, torch.Tensor):
+        dst.copy_(torch.from_numpy(np.ascontiguousarray(src)))
+    else:
+        np.copyto(dst, src)
+
+
+@pytest.mark.parametrize("kind", ["pblusgs", "pbilu"])
+@pytest.mark.parametrize("on_device", [False, True])
+def test_reprepare_with_new_values(kind, on_device, port, ucfd):
+    """A second Prepare after new values were written into the same array
+    (structure unchanged: the structure built by the first Prepare is kept
+    and only the values are gathered on the device) gives, bit for bit, the
+    factors and apply of the oracle on the new values."""
+    from ucfd_sparse_gb300.krylov import Precon
+    s1, ic = colour_renumbered(cases.bsr_case(mesh=5, seed=3))
+    s2, ic2 = colour_renumbered(cases.bsr_case(mesh=5, seed=11))
+    for k in ("rowptr", "colidx", "diagslots"):
+        np.testing.assert_array_equal(s1[k], s2[k])   # same mesh: same structure
+    assert ic == ic2 and not np.array_equal(s1["values"], s2["values"])
+    conv = dev if on_device else np.ascontiguousarray
+    vals = conv(np.array(s1["values"], dtype=np.float64))
+    pc = Precon(conv(s1["rowptr"]), conv(s1["colidx"]), conv(s1["diagslots"]), vals)
+    icn = np.array(ic, dtype=np.int32)
+    if kind == "pbilu":
+        pc.set_pbilu(s1["bn"], 5, len(ic) - 1, icn)
+    else:
+        pc.set_pblusgs(s1["bn"], 5, len(ic) - 1, icn)
+    b = np.random.default_rng(5).standard_normal(s1["bn"] * 5)
+    for s in (s1, s2):
+        _fill(vals, s["values"])
+        pc.prepare()
+        x = b.copy()
+        pc.apply(x)
+        if kind == "pbilu":
+            fv = port.bilu_factor(s)
+            got = vals.cpu().numpy() if on_device else vals
+            np.testing.assert_array_equal(got, fv)
+            ref = port.bilu_apply(s, fv, b)
+        else:
+            ref = port.precon_apply(s, b, icolors=ic)
+        np.testing.assert_array_equal(x, ref)
+
+
+@pytest.mark.parametrize("on_device", [False, True])
+def test_reprepare_detects_structure_change(on_device, port, ucfd):
+    """Another matrix of the same size written into the same rowptr /
+    colidx / diagslots arrays changes their fingerprints: Prepare rebuilds
+    the schedule and layout, and the apply is the oracle's on the new
+    matrix."""
+    from ucfd_sparse_gb300.krylov import Precon
+    s0 = cases.bsr_case(mesh=4, seed=8)
+    s1, _ = colour_renumbered(s0)
+    assert s0["rowptr"][-1] == s1["rowptr"][-1] and not np.array_equal(s0["colidx"], s1["colidx"])
+    conv = dev if on_device else np.ascontiguousarray
+    arrs = {k: conv(np.array(s0[k])) for k in ("rowptr", "colidx", "diagslots", "values")}
+    pc = Precon(arrs["rowptr"], arrs["colidx"], arrs["diagslots"], arrs["values"])
+    pc.set_blusgs(s0["bn"], 5)
+    b = np.random.default_rng(6).standard_normal(s0["bn"] * 5)
+    for s in (s0, s1):
+        for k in arrs:
+            _fill(arrs[k], s[k])
+        pc.prepare()
+        x = b.copy()
+        pc.apply(x)
+        np.testing.assert_array_equal(x, port.precon_apply(s, b))
+
+
+@pytest.mark.parametrize("on_device", [False, True])
+def test_spmat_update_values(on_device, ucfd):
+    """UCFDMatUpdateValues re-gathers the values on the device: the product
+    equals a new matrix created on the new values, bit for bit, for the
+    FP64 values and the FP32 copy; a changed structure is rebuilt."""
+    from ucfd_sparse_gb300.krylov import SpMat
+    s1 = cases.bsr_case(mesh=4, seed=1)
+    s2 = cases.bsr_case(mesh=4, seed=2)
+    s3, _ = colour_renumbered(s1)
+    conv = dev if on_device else np.ascontiguousarray
+    arrs = {k: conv(np.array(s1[k])) for k in ("rowptr", "colidx", "values")}
+    A = SpMat(s1["bn"], 5, arrs["rowptr"], arrs["colidx"], arrs["values"], cuda=on_device)
+    x = cases.spmv_x(s1)
+    y = np.zeros_like(x)
+    A.mult(1.0, x, 0.0, y, fp32=True)   # makes the FP32 copy, refreshed by updates
+    for s in (s2, s3):
+        for k in arrs:
+            _fill(arrs[k], s[k])
+        A.update_values()
+        F = SpMat(s["bn"], 5, s["rowptr"], s["colidx"], s["values"])
+        for fp32 in (False, True):
+            y, yf = np.zeros_like(x), np.zeros_like(x)
+            A.mult(1.0, x, 0.0, y, fp32=fp32)
+            F.mult(1.0, x, 0.0, yf, fp32=fp32)
+            np.testing.assert_array_equal(y, yf)

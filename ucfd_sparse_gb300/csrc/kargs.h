@@ -20,6 +20,17 @@ UCFD_HD inline long long tile_index(long long k, long long j, long long m) {
 }
 UCFD_HD inline long long tiled_size(long long N, long long m) { return ((N + 31) >> 5) * m * 32; }
 
+// Term of the structure fingerprints (sum over i, wrapping): the splitmix64
+// finaliser (Steele, Lea and Flood 2014) of the index in the high word and
+// the value in the low word.  The same function on the host and the device.
+UCFD_HD inline unsigned long long fingerprint_mix(long long i, int v) {
+    unsigned long long z = ((unsigned long long)i << 32) ^ (unsigned)v;
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
 // One launch of the scalar LU-SGS sweep over a range of cells that are
 // independent of each other (one colour or one level).
 template <typename T>

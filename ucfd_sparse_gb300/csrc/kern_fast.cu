@@ -62,6 +62,8 @@ template void gather_rows<double, double>(int, int, const int *, const double *,
 template void scatter_rows<double, double>(int, int, const int *, const double *, double *, cudaStream_t);
 template void gather_rows<double, float>(int, int, const int *, const double *, float *, cudaStream_t);
 template void scatter_rows<float, double>(int, int, const int *, const float *, double *, cudaStream_t);
+template void ell_gather<double>(int, int, int, const int *, const double *, double *, cudaStream_t);
+template void ell_gather<float>(int, int, int, const int *, const double *, float *, cudaStream_t);
 template void convert<double, float>(long long, const double *, float *, cudaStream_t);
 template void convert<float, double>(long long, const float *, double *, cudaStream_t);
 template void axpy_into<float>(long long, const float *, double *, cudaStream_t);

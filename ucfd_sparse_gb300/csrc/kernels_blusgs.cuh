@@ -190,10 +190,25 @@ __global__ void __launch_bounds__(256) jmat_face_major_kernel(long long nF, cons
     for (int q = threadIdx.x; q < nf * R; q += blockDim.x) out[q] = tile[(q / R) * LD + q % R];
 }
 
+// x with its sign bit XORed with the top bit of hi_mask (0 or 0x80000000):
+// x or -x, bit for bit.  Done as an integer XOR of the high word in PTX so
+// the flip stays an integer operation instead of a floating-point negation
+// that would occupy the FP64 pipe.
+__device__ __forceinline__ double xor_sign(double x, unsigned hi_mask) {
+    unsigned hi;
+    asm("xor.b32 %0, %1, %2;" : "=r"(hi) : "r"((unsigned)__double2hiint(x)), "r"(hi_mask));
+    return __hiloint2double((int)hi, __double2loint(x));
+}
+
 // pre_blusgs: blusgs.c:200-246, plus the gather of each cell-face's
 // off-diagonal block (the half the sweeps use) into the ELL layout.
 // The block starts from dd[k] I when dd is given (NS pack), else from D.
 // jt holds the face-major records written by jmat_face_major_kernel.
+// The side's sign goes into the face factor once per face: the diagonal
+// term (side == 1 ? h0 : -h1) * fv is computed as (side == 1 ? h0 : h1) *
+// (side == 1 ? fv : -fv), the same value bit for bit (a product's sign is
+// the XOR of its operands' signs, its magnitude rounds the same), and the
+// stored off-diagonal value -h0 is a sign-bit flip.
 template <typename S, int B>
 __global__ void fs_blusgs_prepare_kernel(long long N, int P, const int *nei, const int *slot,
                                          const int8_t *side, const double *fa, const double *rv,
@@ -216,8 +231,10 @@ __global__ void fs_blusgs_prepare_kernel(long long N, int P, const int *nei, con
     for (int p = 0; p < P; ++p) {
         if (nei[p * N + k] < 0) break;
         const long long s = slot[p * N + k];
-        const int sd = side[p * N + k];
+        const bool pos = side[p * N + k] == 1;
         const double fv = fa[p * N + k] * rv[k];
+        const double fvs = pos ? fv : -fv;
+        const unsigned neg = pos ? 0u : 0x80000000u;
         double h[R];
         const double2 *rec = reinterpret_cast<const double2 *>(jt + s * R);
 #pragma unroll
@@ -231,9 +248,8 @@ __global__ void fs_blusgs_prepare_kernel(long long N, int P, const int *nei, con
 #pragma unroll
             for (int c = 0; c < B; ++c) {
                 const double h0 = h[r * B + c], h1 = h[B2 + r * B + c];
-                const double val = (sd == 1) ? h0 : -h1;
-                dm[c + r * B] += val * fv;
-                const double jv = (sd == 1) ? h1 : -h0;
+                dm[c + r * B] += (pos ? h0 : h1) * fvs;    // == (pos ? h0 : -h1) * fv
+                const double jv = xor_sign(pos ? h1 : h0, neg);  // == pos ? h1 : -h0
                 const long long o = jbase + ((long long)(p * B2 + r * B + c) << 5);
                 J_s[o] = (S)jv;
                 if (J64) J64[o] = jv;

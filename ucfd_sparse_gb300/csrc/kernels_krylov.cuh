@@ -88,6 +88,46 @@ __global__ void __launch_bounds__(256) bsr_spmv_kernel(int bn, int P, const int 
     }
 }
 
+// Values of a CSR-of-blocks array (row-major B x B blocks in slot order)
+// into the ELL-of-blocks layout: ELL entry (p, k) takes the block at slot
+// src[p*bn + k] (src < 0: padding, zeros).  One thread per ELL entry: the
+// writes coalesce over k, and a thread's B*B reads are one contiguous block
+// requested all at once.  T = float rounds the FP64 values.
+template <typename T, int B>
+__global__ void __launch_bounds__(256) ell_gather_kernel(int bn, int P, const int *src, const double *vals,
+                                                         T *out) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= (long long)P * bn) return;
+    constexpr int B2 = B * B;
+    const int p = (int)(t / bn);
+    const int k = (int)(t - (long long)p * bn);
+    const int q = __ldg(src + t);
+    T *o = out + (long long)p * B2 * bn + k;
+    double v[B2];
+    if (q >= 0) {
+        const double *blk = vals + (long long)q * B2;
+#pragma unroll
+        for (int e = 0; e < B2; ++e) v[e] = __ldg(blk + e);
+    } else {
+#pragma unroll
+        for (int e = 0; e < B2; ++e) v[e] = 0.0;
+    }
+#pragma unroll
+    for (int e = 0; e < B2; ++e) o[(long long)e * bn] = (T)v[e];
+}
+
+// Order-independent 64-bit fingerprint of an int array: out += sum over i
+// of fingerprint_mix(i, a[i]) (wrapping), so a structure cached from an
+// earlier call can be recognised without copying the array to the host.
+__global__ void __launch_bounds__(256) fingerprint_kernel(long long n, const int *a, unsigned long long *out) {
+    unsigned long long h = 0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        h += ::ucfd::fingerprint_mix(i, a[i]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) h += __shfl_down_sync(0xffffffffu, h, o);
+    if ((threadIdx.x & 31) == 0 && h) atomicAdd(out, h);
+}
+
 // BLUSGSPreconPrepare: precon/blusgs.c:7-26 -- copy each diagonal block and
 // LU-factor it (FP64), optionally rounding the factors to Tl.
 template <typename Tl, int B>

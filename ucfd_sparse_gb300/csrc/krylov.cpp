@@ -28,48 +28,96 @@ cudaStream_t kstream() {
     return s;
 }
 
-// Row-major CSR-of-blocks (host) -> ELL-of-blocks (device).
+// Row-major CSR-of-blocks -> ELL-of-blocks (device).  The structure -- each
+// ELL entry's column and the CSR slot whose block it holds -- is built on
+// the host once; the values are gathered on the device from the caller's
+// block array (ell_gather), so a new set of values costs one device pass.
 struct EllBlocks {
     int bn = 0, B = 0, P = 0;
-    DevBuf<int> col;
+    DevBuf<int> col, src;
     DevBuf<double> val;
     DevBuf<float> val32;
 
     // rows: internal row k takes original row perm[k] (perm null: identity);
     // entries [first[k], last[k]) of that row; columns mapped through iperm.
-    void build(int bn_, int B_, const std::vector<int> &rp, const std::vector<int> &ci,
-               const std::vector<double> &vals, const int *perm, const int *iperm, const std::vector<int> *lo,
-               const std::vector<int> *hi, bool fp32, cudaStream_t s) {
+    void build(int bn_, int B_, const std::vector<int> &rp, const std::vector<int> &ci, const int *perm,
+               const int *iperm, const std::vector<int> *lo, const std::vector<int> *hi, cudaStream_t s) {
         bn = bn_;
         B = B_;
-        const long long B2 = (long long)B * B;
         P = 0;
         for (int k = 0; k < bn; ++k) {
             const int r = perm ? perm[k] : k;
             const int a = lo ? (*lo)[r] : rp[r], b = hi ? (*hi)[r] : rp[r + 1];
             P = std::max(P, b - a);
         }
-        const int Pa = std::max(P, 1);
-        std::vector<int> c((size_t)Pa * bn, -1);
-        std::vector<double> v((size_t)Pa * B2 * bn, 0.0);
+        const size_t slots = (size_t)std::max(P, 1) * bn;
+        std::vector<int> c(slots, -1), q(slots, -1);
         for (int k = 0; k < bn; ++k) {
             const int r = perm ? perm[k] : k;
             const int a = lo ? (*lo)[r] : rp[r], b = hi ? (*hi)[r] : rp[r + 1];
             for (int p = 0; p < b - a; ++p) {
-                const int q = a + p;
-                c[(size_t)p * bn + k] = iperm ? iperm[ci[q]] : ci[q];
-                for (long long e = 0; e < B2; ++e) v[((size_t)p * B2 + e) * bn + k] = vals[(size_t)q * B2 + e];
+                c[(size_t)p * bn + k] = iperm ? iperm[ci[a + p]] : ci[a + p];
+                q[(size_t)p * bn + k] = a + p;
             }
         }
         col.upload(c.data(), c.size(), s);
-        val.upload(v.data(), v.size(), s);
-        if (fp32) {
-            std::vector<float> f(v.begin(), v.end());
-            val32.upload(f.data(), f.size(), s);
-        }
+        src.upload(q.data(), q.size(), s);
         UCFD_CUDA(cudaStreamSynchronize(s));
     }
+
+    // Blocks of the caller's values (device, [nnzb][B][B]) into val (FP64)
+    // and/or val32 (rounded to FP32).
+    void gather(const double *vals, bool fp64, bool fp32, cudaStream_t s) {
+        const size_t n = (size_t)std::max(P, 1) * B * B * bn;
+        if (fp64) {
+            val.ensure(n);
+            kfast::ell_gather<double>(B, bn, P, src.p, vals, val.p, s);
+        }
+        if (fp32) {
+            val32.ensure(n);
+            kfast::ell_gather<float>(B, bn, P, src.p, vals, val32.p, s);
+        }
+    }
 };
+
+// Fingerprints (kargs.h fingerprint_mix) of up to three int arrays in host
+// or device memory; arrays with n <= 0 give 0.
+struct Fingerprint {
+    unsigned long long h[3] = {0, 0, 0};
+    bool operator==(const Fingerprint &o) const { return h[0] == o.h[0] && h[1] == o.h[1] && h[2] == o.h[2]; }
+};
+
+Fingerprint fingerprint_arrays(const int *const a[3], const long long n[3], DevBuf<unsigned long long> &acc,
+                               cudaStream_t s) {
+    Fingerprint f;
+    bool any_dev = false;
+    for (int j = 0; j < 3; ++j) {
+        if (!a[j] || n[j] <= 0) continue;
+        if (is_device_ptr(a[j])) {
+            if (!any_dev) acc.zero(3, s);
+            any_dev = true;
+            kfast::fingerprint(n[j], a[j], acc.p + j, s);
+        } else {
+            for (long long i = 0; i < n[j]; ++i) f.h[j] += fingerprint_mix(i, a[j][i]);
+        }
+    }
+    if (any_dev) {
+        unsigned long long d[3];
+        UCFD_CUDA(cudaMemcpyAsync(d, acc.p, sizeof d, cudaMemcpyDeviceToHost, s));
+        UCFD_CUDA(cudaStreamSynchronize(s));
+        for (int j = 0; j < 3; ++j)
+            if (a[j] && n[j] > 0 && is_device_ptr(a[j])) f.h[j] = d[j];
+    }
+    return f;
+}
+
+// One int of a caller array (host or device).
+int read_int(const int *p) {
+    int v = 0;
+    if (is_device_ptr(p)) UCFD_CUDA(cudaMemcpy(&v, p, sizeof v, cudaMemcpyDeviceToHost));
+    else v = *p;
+    return v;
+}
 
 }  // namespace
 
@@ -85,25 +133,45 @@ struct _SpMat {
     bool ready = false;
     DevBuf<double> sx, sy;
 
+    DevBuf<double> vstage;
+    DevBuf<unsigned long long> fpacc;
+    Fingerprint fp;
+    int nnzb = -1;
+
+    // Structure (host, validated) and values (device gather).  The structure
+    // is rebuilt only when the fingerprints of rowptr / colidx differ from the
+    // ones it was built from.
     void load(bool fp32) {
-        std::vector<int> rp, ci;
-        std::vector<double> v;
-        to_host(rowptr, (size_t)bn + 1, rp);
-        UCFD_REQUIRE(rp[0] == 0, "rowptr[0] must be 0");
-        for (int i = 0; i < bn; ++i) UCFD_REQUIRE(rp[i + 1] >= rp[i], "rowptr must be non-decreasing");
-        to_host(colidx, (size_t)rp[bn], ci);
-        for (size_t q = 0; q < ci.size(); ++q)
-            UCFD_REQUIRE(ci[q] >= 0 && ci[q] < bn, "colidx[%zu] = %d out of range", q, ci[q]);
-        to_host(values, (size_t)rp[bn] * blk * blk, v);
-        ell.build(bn, blk, rp, ci, v, nullptr, nullptr, nullptr, nullptr, fp32, kstream());
+        cudaStream_t s = kstream();
+        const int nnz_now = read_int(rowptr + bn);
+        UCFD_REQUIRE(nnz_now >= 0, "rowptr[bn] = %d is negative", nnz_now);
+        const int *arr[3] = {rowptr, colidx, nullptr};
+        const long long len[3] = {(long long)bn + 1, (long long)nnz_now, 0};
+        const Fingerprint f = fingerprint_arrays(arr, len, fpacc, s);
+        if (!ready || nnz_now != nnzb || !(f == fp)) {
+            std::vector<int> rp, ci;
+            to_host(rowptr, (size_t)bn + 1, rp);
+            UCFD_REQUIRE(rp[0] == 0, "rowptr[0] must be 0");
+            for (int i = 0; i < bn; ++i) UCFD_REQUIRE(rp[i + 1] >= rp[i], "rowptr must be non-decreasing");
+            to_host(colidx, (size_t)rp[bn], ci);
+            for (size_t q = 0; q < ci.size(); ++q)
+                UCFD_REQUIRE(ci[q] >= 0 && ci[q] < bn, "colidx[%zu] = %d out of range", q, ci[q]);
+            ell.build(bn, blk, rp, ci, nullptr, nullptr, nullptr, nullptr, s);
+            nnzb = rp[bn];
+            fp = f;
+        }
+        const double *vd = device_view<double>(values, (size_t)nnzb * blk * blk, vstage, s);
+        ell.gather(vd, true, fp32, s);
+        UCFD_CHECK_LAUNCH();
+        UCFD_CUDA(cudaStreamSynchronize(s));
         ready = true;
     }
     void ensure32() {
         if (!ell.val32.p) {
-            std::vector<double> v((size_t)ell.P * blk * blk * bn);
-            UCFD_CUDA(cudaMemcpy(v.data(), ell.val.p, v.size() * sizeof(double), cudaMemcpyDeviceToHost));
-            std::vector<float> f(v.begin(), v.end());
-            ell.val32.upload(f.data(), f.size(), kstream());
+            const long long n = (long long)std::max(ell.P, 1) * blk * blk * bn;
+            ell.val32.ensure(n);
+            kfast::convert<double, float>(n, ell.val.p, ell.val32.p, kstream());
+            UCFD_CHECK_LAUNCH();
             UCFD_CUDA(cudaStreamSynchronize(kstream()));
         }
     }
@@ -140,23 +208,29 @@ struct _Precon {
     DevBuf<float> LU32, tmp32;
     DevBuf<double> stage_b;
 
-    void prepare() {
-        if (none) {
-            prepared = true;
-            return;
-        }
-        UCFD_REQUIRE(bn > 0 && blk > 0, "preconditioner type not set (UCFDPreconSetBLUSGS / SetPBLUSGS)");
+    // Structure cache: built from rowptr / colidx / diagslots (and the
+    // colours) at the first Prepare, rebuilt when their fingerprints change
+    // or a Set call resets it.
+    bool have_structure = false;
+    Fingerprint fp;
+    int nnzb = -1;
+    DevBuf<unsigned long long> fpacc;
+    DevBuf<int> d_rp, d_ci, d_ds, d_rows;  // ILU factorisation
+    DevBuf<double> vstage;
+
+    void build_structure(cudaStream_t s) {
         std::vector<int> rp, ci, ds;
-        std::vector<double> v;
         to_host(rowptr, (size_t)bn + 1, rp);
+        UCFD_REQUIRE(rp[0] == 0, "rowptr[0] must be 0");
+        for (int i = 0; i < bn; ++i) UCFD_REQUIRE(rp[i + 1] >= rp[i], "rowptr must be non-decreasing");
         to_host(colidx, (size_t)rp[bn], ci);
         to_host(diagslots, (size_t)bn, ds);
+        for (size_t q = 0; q < ci.size(); ++q)
+            UCFD_REQUIRE(ci[q] >= 0 && ci[q] < bn, "colidx[%zu] = %d out of range", q, ci[q]);
         for (int i = 0; i < bn; ++i) {
             UCFD_REQUIRE(ds[i] >= rp[i] && ds[i] < rp[i + 1], "diagslots[%d] = %d outside row %d", i, ds[i], i);
             UCFD_REQUIRE(ci[ds[i]] == i, "diagslots[%d] does not point at the diagonal block", i);
         }
-        for (size_t q = 0; q < ci.size(); ++q)
-            UCFD_REQUIRE(ci[q] >= 0 && ci[q] < bn, "colidx[%zu] = %d out of range", q, ci[q]);
         if (kind != 0) {
             // the ILU types pair "before the diagonal slot" with "lower row"
             for (int i = 0; i < bn; ++i)
@@ -165,7 +239,6 @@ struct _Precon {
                                  "row %d: an ILU preconditioner needs columns below the diagonal before its slot "
                                  "and columns above it after", i);
         }
-        to_host(values, (size_t)rp[bn] * blk * blk, v);
         if (colored) {
             // colour c = rows [icolors[c], icolors[c+1]); no row may reference
             // another row of its own colour (otherwise the reference result
@@ -184,7 +257,6 @@ struct _Precon {
         identity = true;
         for (int k = 0; k < bn; ++k)
             if (sch.perm[k] != k) identity = false;
-        cudaStream_t s = kstream();
         if (!identity) perm.upload(sch.perm.data(), bn, s);
         std::vector<int> lo(bn), mid(bn), hi(bn);
         for (int i = 0; i < bn; ++i) {
@@ -193,60 +265,86 @@ struct _Precon {
             hi[i] = ds[i] + 1;
         }
         std::vector<int> end(rp.begin() + 1, rp.end());
-        const bool fp32 = prec == UCFD_PREC_FP32;
-        if (kind != 0) factorize(rp, ci, ds, v, s);
         const int *pm = identity ? nullptr : sch.perm.data();
         const int *ip = identity ? nullptr : sch.iperm.data();
-        L.build(bn, blk, rp, ci, v, pm, ip, &lo, &mid, fp32, s);
-        U.build(bn, blk, rp, ci, v, pm, ip, &hi, &end, fp32, s);
+        L.build(bn, blk, rp, ci, pm, ip, &lo, &mid, s);
+        U.build(bn, blk, rp, ci, pm, ip, &hi, &end, s);
         std::vector<long long> dsl(ds.begin(), ds.end());
         dslot.upload(dsl.data(), bn, s);
+        if (kind != 0) {
+            d_rp.upload(rp.data(), rp.size(), s);
+            d_ci.upload(ci.data(), ci.size(), s);
+            d_ds.upload(ds.data(), ds.size(), s);
+            d_rows.upload(sch.perm.data(), sch.perm.size(), s);
+        }
+        UCFD_CUDA(cudaStreamSynchronize(s));
+        nnzb = rp[bn];
+        have_structure = true;
+    }
+
+    void prepare() {
+        if (none) {
+            prepared = true;
+            return;
+        }
+        UCFD_REQUIRE(bn > 0 && blk > 0, "preconditioner type not set (UCFDPreconSetBLUSGS / SetPBLUSGS)");
+        cudaStream_t s = kstream();
+        const int nnz_now = read_int(rowptr + bn);
+        UCFD_REQUIRE(nnz_now >= 0, "rowptr[bn] = %d is negative", nnz_now);
+        const int *arr[3] = {rowptr, colidx, diagslots};
+        const long long len[3] = {(long long)bn + 1, (long long)nnz_now, (long long)bn};
+        const Fingerprint f = fingerprint_arrays(arr, len, fpacc, s);
+        if (!have_structure || nnz_now != nnzb || !(f == fp)) {
+            have_structure = false;
+            build_structure(s);
+            fp = f;
+        }
+        const bool fp32 = prec == UCFD_PREC_FP32;
         const long long B2 = (long long)blk * blk;
+        const size_t nv = (size_t)nnzb * B2;
+        // the caller's values on the device (the ILU types factorise them in
+        // place there and, for a host array, copy the factors back)
+        const bool vdev = is_device_ptr(values);
+        double *vd = values;
+        if (!vdev) {
+            vstage.upload(values, nv, s);
+            vd = vstage.p;
+        }
+        if (kind != 0) {
+            factorize(vd, s);
+            if (!vdev) UCFD_CUDA(cudaMemcpyAsync(values, vd, nv * sizeof(double), cudaMemcpyDeviceToHost, s));
+        }
+        L.gather(vd, !fp32, fp32, s);
+        U.gather(vd, !fp32, fp32, s);
         LU64.ensure(B2 * bn);
-        // the values for the LU come from the caller's array (device view)
-        DevBuf<double> vals;
-        vals.upload(v.data(), v.size(), s);
         const int fac = kind == 0 ? 1 : 0;  // the ILU types arrive factored
         if (fp32) {
             LU32.ensure(B2 * bn);
-            kfast::pc_prepare<float>(blk, bn, identity ? nullptr : perm.p, dslot.p, vals.p, LU64.p, LU32.p, fac, s);
+            kfast::pc_prepare<float>(blk, bn, identity ? nullptr : perm.p, dslot.p, vd, LU64.p, LU32.p, fac, s);
         } else if (prec == UCFD_PREC_FP64) {
-            kexact::pc_prepare<double>(blk, bn, identity ? nullptr : perm.p, dslot.p, vals.p, LU64.p, nullptr, fac,
-                                       s);
+            kexact::pc_prepare<double>(blk, bn, identity ? nullptr : perm.p, dslot.p, vd, LU64.p, nullptr, fac, s);
         } else {
-            kfast::pc_prepare<double>(blk, bn, identity ? nullptr : perm.p, dslot.p, vals.p, LU64.p, nullptr, fac, s);
+            kfast::pc_prepare<double>(blk, bn, identity ? nullptr : perm.p, dslot.p, vd, LU64.p, nullptr, fac, s);
         }
         UCFD_CHECK_LAUNCH();
         UCFD_CUDA(cudaStreamSynchronize(s));
         prepared = true;
     }
 
-    // ILU(0) factorisation on the device, level by level of the schedule
-    // (each row once its lower neighbours are final: the sequential result),
-    // in FP64; the factors replace v and, as in the reference, the caller's
-    // values array.
-    void factorize(const std::vector<int> &rp, const std::vector<int> &ci, const std::vector<int> &ds,
-                   std::vector<double> &v, cudaStream_t s) {
-        DevBuf<int> d_rp, d_ci, d_ds, d_rows;
-        DevBuf<double> d_v;
-        d_rp.upload(rp.data(), rp.size(), s);
-        d_ci.upload(ci.data(), ci.size(), s);
-        d_ds.upload(ds.data(), ds.size(), s);
-        d_rows.upload(sch.perm.data(), sch.perm.size(), s);
-        d_v.upload(v.data(), v.size(), s);
+    // ILU(0) factorisation in place on the device values v (FP64), level by
+    // level of the schedule (each row once its lower neighbours are final:
+    // the sequential result).
+    void factorize(double *v, cudaStream_t s) {
         const int scalar = kind == 2 ? 1 : 0;
         for (int l = 0; l < sch.nlev; ++l) {
             if (prec == UCFD_PREC_FP64)
                 kexact::ilu_factor(blk, scalar, sch.lev_off[l], sch.lev_off[l + 1], d_rows.p, d_rp.p, d_ci.p, d_ds.p,
-                                   d_v.p, s);
+                                   v, s);
             else
                 kfast::ilu_factor(blk, scalar, sch.lev_off[l], sch.lev_off[l + 1], d_rows.p, d_rp.p, d_ci.p, d_ds.p,
-                                  d_v.p, s);
+                                  v, s);
         }
         UCFD_CHECK_LAUNCH();
-        UCFD_CUDA(cudaMemcpyAsync(v.data(), d_v.p, v.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
-        UCFD_CUDA(cudaMemcpyAsync(values, d_v.p, v.size() * sizeof(double), cudaMemcpyDefault, s));
-        UCFD_CUDA(cudaStreamSynchronize(s));
     }
 
     // In-place apply to a device vector b [bn*blk] (FP64).
@@ -613,6 +711,7 @@ static ucfd_status_t pc_set(Precon *pc, const char *type, UCFDInt bn, UCFDInt bl
         p->ncolors = ncolors;
     }
     p->prepared = false;
+    p->have_structure = false;
     UCFD_API_END
 }
 

@@ -88,6 +88,10 @@
                   const T *LU, T *b, int block, int mode, cudaStream_t s);                         \
     void ilu_factor(int B, int scalar, int t0, int t1, const int *rows, const int *rowptr,         \
                     const int *colidx, const int *diagslots, double *vals, cudaStream_t s);        \
+    template <typename T>                                                                          \
+    void ell_gather(int B, int bn, int P, const int *src, const double *vals, T *out,              \
+                    cudaStream_t s);                                                               \
+    void fingerprint(long long n, const int *a, unsigned long long *out, cudaStream_t s);          \
     template <typename Ts, typename Td>                                                            \
     void gather_rows(int bn, int B, const int *perm, const Ts *src, Td *dst, cudaStream_t s);      \
     template <typename Ts, typename Td>                                                            \

@@ -434,6 +434,18 @@ void pc_prepare(int B, int bn, const int *perm, const long long *dslot, const do
                                                                              LU_l, factor)));
 }
 
+template <typename T>
+void ell_gather(int B, int bn, int P, const int *src, const double *vals, T *out, cudaStream_t s) {
+    const long long n = (long long)P * bn;
+    if (n <= 0) return;
+    UCFD_KSW(B, (ell_gather_kernel<T, BB><<<grid_for(n), kBlock, 0, s>>>(bn, P, src, vals, out)));
+}
+
+void fingerprint(long long n, const int *a, unsigned long long *out, cudaStream_t s) {
+    if (n <= 0) return;
+    fingerprint_kernel<<<grid_for(n < (1ll << 22) ? n : (1ll << 22)), kBlock, 0, s>>>(n, a, out);
+}
+
 // Triangular steps, mode PC_BLUSGS / PC_BILU / PC_ILU (kernels_krylov.cuh).
 template <typename T, int MODE, bool LOWER>
 static void pc_step_go(int B, unsigned g, int block, cudaStream_t s, int t0, int t1, int bn, int P,
