@@ -181,12 +181,12 @@ class Problem:
         self.S.set_blusgs(e["jmat"])
         self.nlev = self.S.levels()
 
-    def tune(self, reps=3):
+    def tune(self, reps=3, cache=None):
         """Launch autotuner on the packed system (outside any timed region)."""
         S = self.S
         S.blusgs_pack(0, 0.0)
         S.blusgs_ns_prepare()
-        cfg = S.autotune(reps=reps)
+        cfg = S.autotune(reps=reps, cache=cache)
         cfg.pop("source", None)
         return cfg
 
@@ -296,7 +296,7 @@ def run_gpu(args):
     nlev = P32.nlev
     tuned = {}
     if not args.no_autotune:
-        tuned = {"fp32": P32.tune(), "fp64_fma": P64.tune()}
+        tuned = {"fp32": P32.tune(cache=args.autotune_cache), "fp64_fma": P64.tune(cache=args.autotune_cache)}
 
     def timed(P, steps, warm, inner, tag):
         for _ in range(warm):
@@ -473,7 +473,7 @@ def run_lusgs(args):
         S.set_lusgs(g["fspr"], g["tfspr"])
         S.lusgs_pack(0, 1.0, 0.0)
         if not args.no_autotune:
-            tuned = S.autotune(reps=2)                   # block size x register build (state restored)
+            tuned = S.autotune(reps=2, cache=args.autotune_cache)  # block size x register build (state restored)
             tuned.pop("source", None)
             res.setdefault("launch", tuned)
         hist = np.zeros(args.iters)
@@ -735,7 +735,7 @@ def run_kernels(args):
     stream = torch.cuda.Stream(device=device)
     P = Problem(case, lc, 2, stream, device)
     S = P.S
-    tuned = P.tune() if not args.no_autotune else None
+    tuned = P.tune(cache=args.autotune_cache) if not args.no_autotune else None
     S.blusgs_reset()
 
     def timed(fn, reps):
@@ -807,6 +807,9 @@ def main(argv=None):
     ap.add_argument("--max-pairs", type=int, default=400)
     ap.add_argument("--ref-pairs", type=int, default=1)
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")
+    ap.add_argument("--autotune-cache", default=None,
+                    help="JSON file of launch choices: reused when it holds one for the system, else written "
+                         "(a profiled run can then repeat the choices of an unprofiled one)")
     ap.add_argument("--coloring", default="index", choices=["index", "bfs"],
                     help="greedy colouring visiting cells by index or in breadth-first order")
     ap.add_argument("--workload", default="blusgs", choices=["blusgs", "lusgs", "gmres", "colored", "kernels"],

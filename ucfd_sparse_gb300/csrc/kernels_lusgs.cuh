@@ -14,8 +14,17 @@
 
 namespace UCFD_KNS {
 
+// a / b.  FP32: one approximate reciprocal and a product (at most two ulp
+// off, __fdividef); the FP32 sweeps are not bit-matched to the reference,
+// and the division is a long instruction sequence in a kernel that is
+// bound by its instruction issue.  FP64 keeps the correctly rounded
+// division of the reference.
+__device__ __forceinline__ float div_sweep(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double div_sweep(double a, double b) { return a / b; }
+
 // ns_flux_container: flux.c:29-67.  The pressure floor rewrites the energy
-// of the local copy u (flux.c:51-56), exactly as the reference does.
+// of the local copy u (flux.c:51-56), exactly as the reference does.  In
+// FP32 the two divisions by rho are products with one reciprocal.
 template <typename T, int NFV, int NDIMS>
 __device__ __forceinline__ void ns_flux(T gamma, T pmin, T *u, const T *nf, T *f) {
     T rho = u[0];
@@ -26,11 +35,19 @@ __device__ __forceinline__ void ns_flux(T gamma, T pmin, T *u, const T *nf, T *f
         contrav += u[i + 1] * nf[i];
         temp += u[i + 1] * u[i + 1];
     }
-    contrav /= rho;
-    T p = (gamma - T(1)) * (et - T(0.5) * temp / rho);
+    T ke;  // 0.5 * temp / rho
+    if constexpr (sizeof(T) == 4) {
+        const T irho = div_sweep(T(1), rho);
+        contrav *= irho;
+        ke = T(0.5) * temp * irho;
+    } else {
+        contrav /= rho;
+        ke = T(0.5) * temp / rho;
+    }
+    T p = (gamma - T(1)) * (et - ke);
     if (p < pmin) {
         p = pmin;
-        et = p / (gamma - T(1)) + T(0.5) * temp / rho;
+        et = p / (gamma - T(1)) + ke;
         u[NFV - 1] = et;
     }
     T ht = et + p;
@@ -47,7 +64,7 @@ __device__ __forceinline__ void rans_flux(const T *u, const T *nf, T *f) {
     T contrav = T(0);
 #pragma unroll
     for (int i = 0; i < NDIMS; ++i) contrav += u[i + 1] * nf[i];
-    contrav /= rho;
+    contrav = div_sweep(contrav, rho);
 #pragma unroll
     for (int i = 0; i < NT; ++i) f[i] = u[NFV + i] * contrav;
 }
@@ -136,76 +153,108 @@ __global__ void __launch_bounds__(256, MINB) scalar_sweep_persistent_kernel(Scal
 __device__ __forceinline__ float mul_rn(float x, float y) { return __fmul_rn(x, y); }
 __device__ __forceinline__ double mul_rn(double x, double y) { return __dmul_rn(x, y); }
 
-// Faces f0 .. f0+FB-1 of cell i (neighbours nb[]): the colour / level test,
-// every gather of an active face before any flux is evaluated (latency
-// hiding; inactive faces load nothing), then each active face's term
-// ((F(u+du) - F(u)) - kappa lam du) * area * rcp_vol of lusgs.c:143-205,
-// added to df in face order (ACC) or stored in c[q][k] for the caller to
-// add in face order.
-template <typename T, int NV, int NFV, int NDIMS, bool RANS, bool COHERENT, int FB, bool ACC>
-__device__ __forceinline__ void face_terms(const ScalarSweepArgs<T> &a, int i, int ci, T rvi, int f0,
-                                           const int *nb, bool *act, T (*c)[RANS ? NV - NFV : NFV], T *df) {
+// Active faces among the NB face slots f0 .. f0+NB-1 of a cell (neighbours
+// nb[q], -1 for none): bit q is set when the neighbour of slot q belongs to
+// this sweep (a lower colour / level for the lower sweep, a higher one for
+// the upper sweep).
+template <typename T, int NB>
+__device__ __forceinline__ unsigned active_faces(const ScalarSweepArgs<T> &a, int ci, const int *nb) {
+    unsigned m = 0;
+#pragma unroll
+    for (int q = 0; q < NB; ++q) {
+        bool act;
+        if (a.lcolor) {
+            const int cn = nb[q] >= 0 ? __ldg(a.lcolor + nb[q]) : ci;
+            act = a.upper ? (cn > ci) : (cn < ci);
+        } else {
+            act = nb[q] >= 0 && (a.upper ? (nb[q] >= a.hi) : (nb[q] < a.lo));
+        }
+        m |= act ? (1u << q) : 0u;
+    }
+    return m;
+}
+
+// Terms of the next (up to) KB active faces of a cell, taken from the mask
+// m of its slots f0 + q (neighbours nb[q], NB slots) lowest slot first, so
+// the k-th term is that of the k-th active face in face order; the faces
+// taken are cleared from m and their number is returned.  Every lane of a
+// warp works on its own k-th active face at step k, so a warp runs as many
+// face steps as its busiest lane has active faces (not one per slot that
+// any lane has active).  All gathers of the step's faces are issued before
+// any flux is evaluated (latency hiding).  Each face's term
+// ((F(u+du) - F(u)) - kappa lam du) * area * rcp_vol (lusgs.c:143-205) is
+// added to df in order (ACC) or stored in c[k] for the caller to add.
+template <typename T, int NV, int NFV, int NDIMS, bool RANS, bool COHERENT, int NB, int KB, bool ACC>
+__device__ __forceinline__ int face_terms(const ScalarSweepArgs<T> &a, int i, T rvi, int f0, const int *nb,
+                                          unsigned &m, T (*c)[RANS ? NV - NFV : NFV], T *df) {
     constexpr int NV0 = RANS ? NFV : 0;
     constexpr int DNV = RANS ? NV - NFV : NFV;
     const long long ld = a.ld;
+    bool on[KB];
+    int fk[KB], gk[KB];
 #pragma unroll
-    for (int q = 0; q < FB; ++q) {
-        if (a.lcolor) {
-            const int cn = nb[q] >= 0 ? __ldg(a.lcolor + nb[q]) : ci;
-            act[q] = a.upper ? (cn > ci) : (cn < ci);
-        } else {
-            act[q] = nb[q] >= 0 && (a.upper ? (nb[q] >= a.hi) : (nb[q] < a.lo));
-        }
+    for (int k = 0; k < KB; ++k) {
+        on[k] = m != 0u;
+        const int q = on[k] ? __ffs(m) - 1 : 0;
+        m &= m - 1u;
+        int g = nb[0];
+#pragma unroll
+        for (int r = 1; r < NB; ++r) g = (q == r) ? nb[r] : g;
+        fk[k] = f0 + q;
+        gk[k] = g;
     }
-    T uu[FB][NV], dn[FB][DNV], nf[FB][NDIMS], fv[FB], kl[FB];
+    T uu[KB][NV], dn[KB][DNV], nf[KB][NDIMS], fv[KB], kl[KB];
 #pragma unroll
-    for (int q = 0; q < FB; ++q) {
-        if (!act[q]) continue;
-        const int g = nb[q];
+    for (int k = 0; k < KB; ++k) {
+        if (!on[k]) continue;
+        const int g = gk[k];
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
             // only the variables the flux reads are loaded
             const bool need = RANS ? (v <= NDIMS || v >= NFV) : (v < NFV);
-            uu[q][v] = need ? __ldg(a.u + v * ld + g) : T(0);
+            uu[k][v] = need ? __ldg(a.u + v * ld + g) : T(0);
         }
 #pragma unroll
-        for (int k = 0; k < DNV; ++k)
-            dn[q][k] = COHERENT ? __ldcg(a.nbsrc + (k + NV0) * ld + g) : a.nbsrc[(k + NV0) * ld + g];
-        const int f = f0 + q;
+        for (int j = 0; j < DNV; ++j)
+            dn[k][j] = COHERENT ? __ldcg(a.nbsrc + (j + NV0) * ld + g) : a.nbsrc[(j + NV0) * ld + g];
+        const int f = fk[k];
 #pragma unroll
-        for (int d = 0; d < NDIMS; ++d) nf[q][d] = __ldg(a.nrm + (f * NDIMS + d) * ld + i);
-        fv[q] = __ldg(a.fa + f * ld + i);
-        kl[q] = __ldg(a.lam + f * ld + i);
+        for (int d = 0; d < NDIMS; ++d) nf[k][d] = __ldg(a.nrm + (f * NDIMS + d) * ld + i);
+        fv[k] = __ldg(a.fa + f * ld + i);
+        kl[k] = __ldg(a.lam + f * ld + i);
     }
+    int n = 0;
 #pragma unroll
-    for (int q = 0; q < FB; ++q) {
-        if (!act[q]) continue;
-        T *u = uu[q];
+    for (int k = 0; k < KB; ++k) {
+        if (!on[k]) continue;
+        ++n;
+        T *u = uu[k];
         T du[NV], f0v[DNV], f1v[DNV];
 #pragma unroll
         for (int v = 0; v < NV; ++v) du[v] = T(0);
 #pragma unroll
-        for (int k = 0; k < DNV; ++k) du[k + NV0] = dn[q][k];
-        const T fvq = a.rv ? fv[q] * rvi : fv[q];
+        for (int j = 0; j < DNV; ++j) du[j + NV0] = dn[k][j];
+        const T fvk = a.rv ? fv[k] * rvi : fv[k];
         // diff_flux: lusgs.c:143-155 (du += u before either flux)
 #pragma unroll
         for (int v = 0; v < NV; ++v) du[v] += u[v];
         if constexpr (RANS) {
-            rans_flux<T, NFV, NDIMS, NV - NFV>(u, nf[q], f0v);
-            rans_flux<T, NFV, NDIMS, NV - NFV>(du, nf[q], f1v);
+            rans_flux<T, NFV, NDIMS, NV - NFV>(u, nf[k], f0v);
+            rans_flux<T, NFV, NDIMS, NV - NFV>(du, nf[k], f1v);
         } else {
-            ns_flux<T, NFV, NDIMS>(a.gamma, a.pmin, u, nf[q], f0v);
-            ns_flux<T, NFV, NDIMS>(a.gamma, a.pmin, du, nf[q], f1v);
+            ns_flux<T, NFV, NDIMS>(a.gamma, a.pmin, u, nf[k], f0v);
+            ns_flux<T, NFV, NDIMS>(a.gamma, a.pmin, du, nf[k], f1v);
         }
-        const T klq = a.kappa * kl[q];
+        const T klk = a.kappa * kl[k];
 #pragma unroll
-        for (int k = 0; k < DNV; ++k) {
-            const T dfj = f1v[k] - f0v[k];
-            const T term = mul_rn(dfj - klq * dn[q][k], fvq);
-            if constexpr (ACC) df[k] += term;
-            else c[q][k] = term;
+        for (int j = 0; j < DNV; ++j) {
+            const T dfj = f1v[j] - f0v[j];
+            const T term = mul_rn(dfj - klk * dn[k][j], fvk);
+            if constexpr (ACC) df[j] += term;
+            else c[k][j] = term;
         }
     }
+    return n;
 }
 
 // In the level-major layout the first level of a lower sweep and the last
@@ -218,7 +267,7 @@ __device__ __forceinline__ bool no_active_face(const ScalarSweepArgs<T> &a) {
 // The cell's new increment from its own input, diagonal and df.
 template <typename T>
 __device__ __forceinline__ T sweep_result(bool upper, T own, T df, T dg) {
-    return !upper ? (own - T(0.5) * df) / dg : own - (T(0.5) * df / dg);
+    return !upper ? div_sweep(own - T(0.5) * df, dg) : own - div_sweep(T(0.5) * df, dg);
 }
 
 template <typename T, int NV, int NFV, int NDIMS, bool RANS, bool COHERENT>
@@ -239,27 +288,26 @@ __device__ __forceinline__ void scalar_sweep_cell(const ScalarSweepArgs<T> &a, i
     }
     const T rvi = a.rv ? __ldg(a.rv + i) : T(1);
 
-    // Faces three at a time (about 80 registers: occupancy for the gathers'
-    // latency); the terms are added to df in the reference's face order.
+    // Active faces three at a time (about 80 registers: occupancy for the
+    // gathers' latency); the terms are added to df in the reference's face
+    // order.
     constexpr int FB = 3;
-    auto batch = [&](int f0, const int *nb) {
-        bool act[FB];
-        face_terms<T, NV, NFV, NDIMS, RANS, COHERENT, FB, true>(a, i, ci, rvi, f0, nb, act, nullptr, df);
-    };
     if (no_active_face(a)) {
     } else if (a.nface <= 2 * FB) {
-        // every neighbour index of the cell up front, two unrolled batches
+        // every neighbour index of the cell up front, then its active faces
         int nba[2 * FB];
 #pragma unroll
         for (int p = 0; p < 2 * FB; ++p) nba[p] = p < a.nface ? __ldg(a.nei + p * ld + i) : -1;
-        batch(0, nba);
-        if (a.nface > FB) batch(FB, nba + FB);
+        unsigned m = active_faces<T, 2 * FB>(a, ci, nba);
+        face_terms<T, NV, NFV, NDIMS, RANS, COHERENT, 2 * FB, FB, true>(a, i, rvi, 0, nba, m, nullptr, df);
+        if (m) face_terms<T, NV, NFV, NDIMS, RANS, COHERENT, 2 * FB, FB, true>(a, i, rvi, 0, nba, m, nullptr, df);
     } else {
         for (int f0 = 0; f0 < a.nface; f0 += FB) {
             int nb[FB];
 #pragma unroll
             for (int q = 0; q < FB; ++q) nb[q] = (f0 + q < a.nface) ? __ldg(a.nei + (f0 + q) * ld + i) : -1;
-            batch(f0, nb);
+            unsigned m = active_faces<T, FB>(a, ci, nb);
+            face_terms<T, NV, NFV, NDIMS, RANS, COHERENT, FB, FB, true>(a, i, rvi, f0, nb, m, nullptr, df);
         }
     }
 #pragma unroll
@@ -292,7 +340,7 @@ __global__ void __launch_bounds__(256, MINB) scalar_sweep_pair_kernel(ScalarSwee
             dg[k] = a.diag[(k + NV0) * a.diag_vs + i];
         }
     }
-    bool act[FB] = {false, false, false};
+    int n = 0;  // active faces of this lane, terms in c[0 .. n-1] in face order
     T c[FB][DNV];
     if (live && !no_active_face(a)) {
         const T rvi = a.rv ? __ldg(a.rv + i) : T(1);
@@ -302,30 +350,28 @@ __global__ void __launch_bounds__(256, MINB) scalar_sweep_pair_kernel(ScalarSwee
             const int p = h * FB + q;
             nb[q] = p < a.nface ? __ldg(a.nei + p * ld + i) : -1;
         }
-        face_terms<T, NV, NFV, NDIMS, RANS, false, FB, false>(a, i, ci, rvi, h * FB, nb, act, c, nullptr);
+        unsigned m = active_faces<T, FB>(a, ci, nb);
+        n = face_terms<T, NV, NFV, NDIMS, RANS, false, FB, FB, false>(a, i, rvi, h * FB, nb, m, c, nullptr);
     }
     // the odd lane's terms to the even lane
-    unsigned mask = 0;
-#pragma unroll
-    for (int q = 0; q < FB; ++q) mask |= act[q] ? (1u << q) : 0u;
-    const unsigned mask_hi = __shfl_down_sync(0xffffffffu, mask, 1);
+    const int n_hi = __shfl_down_sync(0xffffffffu, n, 1);
     T chi[FB][DNV];
 #pragma unroll
     for (int q = 0; q < FB; ++q)
 #pragma unroll
-        for (int k = 0; k < DNV; ++k) chi[q][k] = __shfl_down_sync(0xffffffffu, act[q] ? c[q][k] : T(0), 1);
+        for (int k = 0; k < DNV; ++k) chi[q][k] = __shfl_down_sync(0xffffffffu, q < n ? c[q][k] : T(0), 1);
     if (!live || h != 0) return;
     T df[DNV];
 #pragma unroll
     for (int k = 0; k < DNV; ++k) df[k] = T(0);
 #pragma unroll
     for (int q = 0; q < FB; ++q)
-        if (act[q])
+        if (q < n)
 #pragma unroll
             for (int k = 0; k < DNV; ++k) df[k] += c[q][k];
 #pragma unroll
     for (int q = 0; q < FB; ++q)
-        if (mask_hi & (1u << q))
+        if (q < n_hi)
 #pragma unroll
             for (int k = 0; k < DNV; ++k) df[k] += chi[q][k];
 #pragma unroll
