@@ -246,6 +246,43 @@ def cpu_baseline(case, pairs=1, repeats=1):
                       f"available", "seconds": best}
 
 
+def lusgs_cpu_baseline(c, iters=1):
+    """One bounded sample of the reference's scalar LU-SGS CPU path on the
+    same mesh: `iters` pseudo-time iterations of Pack, NS + RANS Prepare,
+    lower and upper sweeps (serial, natural order, as lusgs.c) and Update."""
+    from oracle import oracle as orc
+    kind = "reference" if orc.ref_available() else "port"
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    impl = orc.Ref(fast=True) if kind == "reference" else orc.Port(fast=True)
+    dsrc = np.zeros_like(c["rhs"])
+    t0 = time.perf_counter()
+    impl.flowsys_lusgs_step(c, c["upts"], c["rhs"], c["dt"], dsrc, c["fspr"], c["tfspr"], rans=True, nsteps=iters)
+    sec = time.perf_counter() - t0
+    N = c["nlocal"]
+    return {"value": N * iters / sec, "unit": UNIT, "cores": threads, "kind": kind, "seconds": sec,
+            "sample": f"{iters} iteration(s) of Pack+NS/RANS Prepare+lower/upper sweeps+Update on all {N} cells, "
+                      f"FP64; sweeps serial in natural order as in lusgs.c, {threads} OpenMP threads available"}
+
+
+def krylov_cpu_baseline(s, icolors, tol):
+    """The reference's CPU GMRES(30) and BiCGSTAB with the coloured BLU-SGS
+    preconditioner (OpenMP SpMV / preconditioner as in the reference) on a
+    BSR system, to the absolute tolerance tol: seconds and iterations."""
+    from oracle import oracle as orc
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    port = orc.Port(fast=True)
+    out = {"kind": "port", "cores": threads}
+    t0 = time.perf_counter()
+    _, st, it, res, _ = port.gmres(s, s["rhs"], m=30, maxiter=100, tol=tol, pc="pblusgs", icolors=icolors)
+    out["gmres"] = {"s": time.perf_counter() - t0, "stat": st, "restarts": it, "resid": res}
+    t0 = time.perf_counter()
+    _, st, it, res, _ = port.bicgstab(s, s["rhs"], maxiter=200, tol=tol, pc="pblusgs", icolors=icolors)
+    out["bicgstab"] = {"s": time.perf_counter() - t0, "stat": st, "iters": it, "resid": res}
+    return out
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     dist = dist_init("gloo")
@@ -531,6 +568,13 @@ def run_lusgs(args):
            "loop_frac_of_peak": bytes_iter * args.iters / (best * 1e-3) / 1e9 / peak,
            "resid_fp64": [res[0]["resid_first"], res[0]["resid_last"]],
            "clocks": res[0]["clocks"], "generation_s": gen_s, "launch": res.get("launch")}
+    if args.cpu_iters > 0:
+        del g, up
+        torch.cuda.empty_cache()
+        # a bounded sample: the serial sweeps take over a minute per iteration at 256^3
+        cm = min(m, args.cpu_mesh or 128)
+        cc = c if cm == m else mg.lusgs_flowsys_case(cm, nvars=6, seed=args.seed, rhs_scale=1e-3)
+        out["cpu_baseline"] = lusgs_cpu_baseline(cc, iters=args.cpu_iters)
     print(json.dumps(out))
 
 
@@ -546,14 +590,17 @@ def run_gmres(args):
     from ucfd_sparse_gb300.krylov import Precon, Solver, SpMat
     _build.build()
     lib.load()
+
+    def coloured_case(mesh):
+        s0 = mg.bsr_case(mesh, seed=args.seed)
+        tab = np.where(s0["nei"] >= 0, s0["nei"], np.arange(s0["bn"])[None, :]).astype(np.int32)
+        ic, rg, lc = cl.greedy_coloring(tab)
+        new = np.empty(s0["bn"], dtype=np.int64)
+        new[ic] = np.arange(s0["bn"])
+        return mg.renumber_bsr(s0, new), rg
+
     t0 = time.perf_counter()
-    s0 = mg.bsr_case(args.mesh, seed=args.seed)
-    tab = np.where(s0["nei"] >= 0, s0["nei"], np.arange(s0["bn"])[None, :]).astype(np.int32)
-    ic, rg, lc = cl.greedy_coloring(tab)
-    new = np.empty(s0["bn"], dtype=np.int64)
-    new[ic] = np.arange(s0["bn"])
-    s = mg.renumber_bsr(s0, new)
-    del s0
+    s, rg = coloured_case(args.mesh)
     gen_s = time.perf_counter() - t0
     bn = s["bn"]
     n = bn * 5
@@ -666,6 +713,37 @@ def run_gmres(args):
                     "fp32_frac": b32 / (sp[True] * 1e-3) / 1e9 / peak},
            "bicgstab_fp64": bic,
            "generation_s": gen_s}
+    del A, d, x, y
+    torch.cuda.empty_cache()
+    # the reference's CPU solvers beside the GPU ones, on a smaller system of
+    # the same construction (the full one takes minutes on the host cores)
+    if args.cpu_mesh is None:
+        args.cpu_mesh = 48
+    if args.cpu_mesh > 0:
+        sc, rgc = coloured_case(args.cpu_mesh)
+        icc = np.array([0] + rgc, dtype=np.int32)
+        tolc = 1e-10 * float(np.linalg.norm(sc["rhs"]))
+        cpu = krylov_cpu_baseline(sc, icc, tolc)
+        dc = {k: T(sc[k]) for k in ("rowptr", "colidx", "values", "diagslots", "rhs")}
+        Ac = SpMat(sc["bn"], 5, dc["rowptr"], dc["colidx"], dc["values"], cuda=True)
+        gpu = {}
+        for kind in ("gmres", "bicgstab"):
+            pc = Precon(dc["rowptr"], dc["colidx"], dc["diagslots"], dc["values"])
+            pc.set_pblusgs(sc["bn"], 5, len(rgc), icc, cuda=True)
+            pc.prepare()
+            sv = Solver(sc["bn"] * 5, 30, 100 if kind == "gmres" else 200, tolc, cuda=True, kind=kind)
+            xc = torch.zeros(sc["bn"] * 5, dtype=torch.float64, device=dev)
+            sv.solve(pc, Ac, xc, dc["rhs"])  # warm-up
+            xc.zero_()
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            sv.solve(pc, Ac, xc, dc["rhs"])
+            torch.cuda.synchronize()
+            gpu[kind] = {"s": time.perf_counter() - t, "stat": sv.result()[0], "iters": sv.result()[1]}
+            del pc, sv
+        out["cpu_baseline"] = dict(cpu, sample=f"FP64 GMRES(30) and BiCGSTAB with the coloured BLU-SGS to 1e-10 "
+                                                f"relative on Kuhn tets of a {args.cpu_mesh}^3 box ({sc['bn']} cells)",
+                                   gpu_same_system=gpu)
     print(json.dumps(out))
 
 
@@ -714,6 +792,71 @@ def run_colored(args):
     el = time.perf_counter() - t
     out["cpu_port"] = {"s_per_step": el / args.iters, "cell_updates_per_s": N * args.iters / el,
                        "threads": os.cpu_count()}
+    print(json.dumps(out))
+
+
+def run_adjoint(args):
+    """Differentiable colored LU-SGS step (C4 shape: jittered, permuted hex,
+    greedy colouring): forward alone and forward + backward (the transposed
+    sweeps giving d/d rhs, dt, fspr), FP64 and FP32, CUDA events over
+    args.steps calls after args.warmup; beside it the reference's CPU
+    forward step (the adjoint has no reference counterpart)."""
+    import torch
+
+    from oracle import oracle as orc
+    from ucfd_sparse_gb300 import _build, lib
+    from ucfd_sparse_gb300 import coloredlusgs as cl
+    from ucfd_sparse_gb300 import meshgen as mg
+    from ucfd_sparse_gb300.adjoint import ColoredMesh, lusgs_step
+    _build.build()
+    lib.load()
+    m = args.mesh
+    c = mg.lusgs_case(m, jitter=0.2, permute=True, seed=args.seed)
+    N = c["neles"]
+    icolor, ranges, lcolor = cl.greedy_coloring(c["nei_ele"])
+    mesh = ColoredMesh(c["nei_ele"], c["fnorm_vol"], c["vec_fnorm"], icolor, ranges)
+    dev = torch.device("cuda:0")
+    stream = torch.cuda.current_stream(dev)
+    out = {"workload": "adjoint", "unit": UNIT,
+           "config": {"workload": f"differentiable colored LU-SGS step, {m}^3 jittered permuted hex ({N} cells), "
+                                  f"greedy colouring ({len(ranges)} colours), gradients w.r.t. rhs, dt, fspr",
+                      "cells": N, "colors": len(ranges)}}
+    for dt_ in (torch.float64, torch.float32):
+        T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev, dt_)
+        x = {k: T(c[k]).requires_grad_(True) for k in ("rhs", "dt", "fspr")}
+        up = T(c["upts"])
+        g = torch.randn(c["rhs"].shape, dtype=dt_, device=dev)
+        res = {}
+        for mode in ("forward", "forward_backward"):
+            def once():
+                if mode == "forward":
+                    with torch.no_grad():
+                        lusgs_step(x["rhs"], x["dt"], x["fspr"], mesh, up)
+                else:
+                    for v in x.values():
+                        v.grad = None
+                    (lusgs_step(x["rhs"], x["dt"], x["fspr"], mesh, up) * g).sum().backward()
+            for _ in range(max(args.warmup, 3)):
+                once()
+            torch.cuda.synchronize()
+            e0, e1 = _events(stream)
+            e0.record(stream)
+            for _ in range(args.steps):
+                once()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / args.steps
+            res[mode] = {"ms": ms, "cell_updates_per_s": N / (ms * 1e-3)}
+        out["fp64" if dt_ == torch.float64 else "fp32"] = res
+    # the reference's CPU forward step on the same arrays
+    c["lcolor"] = mg.colors_from_icolor(icolor, ranges)
+    port = orc.Port(fast=True)
+    t = time.perf_counter()
+    port.legacy_step(c, icolor, ranges, c["lcolor"], nsteps=1)
+    el = time.perf_counter() - t
+    out["cpu_baseline"] = {"value": N / el, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+                           "sample": f"one colored LU-SGS forward step (pre, lower and upper sweeps by colour, "
+                                     f"update), FP64, on all {N} cells"}
     print(json.dumps(out))
 
 
@@ -812,9 +955,15 @@ def main(argv=None):
                          "(a profiled run can then repeat the choices of an unprofiled one)")
     ap.add_argument("--coloring", default="index", choices=["index", "bfs"],
                     help="greedy colouring visiting cells by index or in breadth-first order")
-    ap.add_argument("--workload", default="blusgs", choices=["blusgs", "lusgs", "gmres", "colored", "kernels"],
+    ap.add_argument("--workload", default="blusgs",
+                    choices=["blusgs", "lusgs", "gmres", "colored", "kernels", "adjoint"],
                     help="blusgs: the headline line; the others measure the remaining configurations")
     ap.add_argument("--iters", type=int, default=200, help="iterations of the lusgs/colored workloads")
+    ap.add_argument("--cpu-mesh", type=int, default=None,
+                    help="box of the smaller system the reference's CPU path runs on (gmres: 48, 0 skips; "
+                         "lusgs: at most 128)")
+    ap.add_argument("--cpu-iters", type=int, default=1,
+                    help="lusgs workload: pseudo-time iterations of the reference's CPU path (0: skip)")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3
@@ -828,6 +977,8 @@ def main(argv=None):
         run_colored(args)
     elif args.workload == "kernels":
         run_kernels(args)
+    elif args.workload == "adjoint":
+        run_adjoint(args)
     else:
         run_gpu(args)
 
