@@ -34,8 +34,8 @@ sys.path.insert(0, ROOT)
 METRIC = "LU-SGS cell-updates/s & HBM GB/s @2.1M cells; FP32+refine vs FP64 @1e-10"
 UNIT = "cell-updates/s"
 # DRAM bytes per cell update of the unrolled FP32 block sweep measured by
-# ncu on the 64^3 mesh (profiles/fs_blusgs_sweep_float5_64cubed.md)
-SWEEP_TRAFFIC_PER_CELL = 866.0
+# ncu on the 96^3 mesh (profiles/fs_blusgs_sweep_float5_96cubed.md)
+SWEEP_TRAFFIC_PER_CELL = 847.0
 
 
 # ---------------------------------------------------------------------------
@@ -397,7 +397,7 @@ def run_gpu(args):
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "kernel": kname, "threads_per_block": cfg32["threads_per_block"],
                 "algorithmic_bytes_per_launch": launch_bytes, "launch_ms": sweep_ms / nlev,
-                "traffic_source": "ncu 64^3 capture, 866 B per cell update, scaled by cells per launch",
+                "traffic_source": "ncu 96^3 capture, 847 B per cell update, scaled by cells per launch",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s"}
 
     # ---- end to end through the C-ABI with pinned host buffers -------------

@@ -6,7 +6,8 @@
  * CUDABSR) accept host or device arrays and copy them into device memory
  * at creation (the reference keeps the pointers; after changing the values
  * in place call UCFDMatUpdateValues).  UCFDMatMult takes host or device
- * vectors.  BSR blocks are row-major [nnzb][blk][blk] and vectors AoS
+ * vectors; with beta == 0 it does not read y (the reference forms beta*y
+ * regardless).  BSR blocks are row-major [nnzb][blk][blk] and vectors AoS
  * [bn][blk] (sparsemat.c:57-101).
  */
 #pragma once

@@ -11,7 +11,9 @@
  * right-preconditioned with the fused five-term reduction and the residual
  * estimate of bicgstab.c:24-128, stopping when the estimate drops below tol
  * (absolute); its scalars stay on the device and the host reads the stop
- * flag every few iterations.  x and b may be host or device arrays of
+ * flag every few iterations.  Where s = r - alpha v is exactly zero the
+ * reference's omega = (t,s)/(t,t) is 0/0; here omega = 0 and the solve
+ * ends converged.  x and b may be host or device arrays of
  * n = bn*blk values.
  */
 #pragma once

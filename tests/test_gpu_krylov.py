@@ -38,6 +38,25 @@ def test_spmv_bitexact(name, on_device, golden, ucfd):
     np.testing.assert_array_equal(y, arr[f"{name}_spmv"])
 
 
+@pytest.mark.parametrize("fp32", [False, True])
+def test_spmv_beta_zero_does_not_read_y(fp32, port, ucfd):
+    """y = A x with beta = 0 over a y full of NaN: y is not read (the
+    product equals the oracle's with a zero y)."""
+    from ucfd_sparse_gb300.krylov import SpMat
+    s = cases.bsr_case(mesh=4, seed=5)
+    A = SpMat(s["bn"], s["blk"], dev(s["rowptr"]), dev(s["colidx"]), dev(s["values"]), cuda=True)
+    x = cases.spmv_x(s)
+    y = torch.full((x.size,), float("nan"), dtype=torch.float64, device="cuda")
+    A.mult(2.0, dev(x), 0.0, y, fp32=fp32)
+    got = y.cpu().numpy()
+    ref = port.bsr_spmv(s, x, alpha=2.0, beta=0.0, y=np.zeros_like(x))
+    assert np.isfinite(got).all()
+    if fp32:
+        assert np.abs(got - ref).max() <= 2e-6 * np.abs(ref).max()
+    else:
+        np.testing.assert_array_equal(got, ref)
+
+
 def test_spmv_fp32_values(golden, ucfd):
     from ucfd_sparse_gb300.krylov import SpMat
     meta, arr = golden
@@ -356,3 +375,62 @@ def test_spmat_update_values(on_device, ucfd):
             A.mult(1.0, x, 0.0, y, fp32=fp32)
             F.mult(1.0, x, 0.0, yf, fp32=fp32)
             np.testing.assert_array_equal(y, yf)
+
+
+def _block_diagonal(bn, blk, seed):
+    """A matrix with only diagonal blocks (no L or U entries at all)."""
+    rng = np.random.default_rng(seed)
+    v = rng.standard_normal((bn, blk, blk)) * 0.1 + np.eye(blk) * 2.0
+    idx = np.arange(bn, dtype=np.int32)
+    return dict(bn=bn, blk=blk, rowptr=np.arange(bn + 1, dtype=np.int32), colidx=idx, diagslots=idx.copy(),
+                values=np.ascontiguousarray(v.reshape(-1)), rhs=rng.standard_normal(bn * blk))
+
+
+@pytest.mark.parametrize("bn", [1, 7])
+@pytest.mark.parametrize("kind", ["blusgs", "pblusgs", "bilu", "ilu"])
+def test_precon_without_off_diagonal_blocks(bn, kind, port, ucfd):
+    """Block-diagonal systems (an empty strictly lower and upper part) and a
+    single block row: Prepare, apply and SpMV equal the oracle bit for bit,
+    and BiCGSTAB solves them."""
+    from ucfd_sparse_gb300.krylov import Precon, Solver, SpMat
+    s = _block_diagonal(bn, 1 if kind == "ilu" else 5, seed=bn)
+    blk = s["blk"]
+    vals = np.array(s["values"])
+    pc = Precon(s["rowptr"], s["colidx"], s["diagslots"], vals)
+    if kind == "blusgs":
+        pc.set_blusgs(bn, blk)
+    elif kind == "pblusgs":
+        pc.set_pblusgs(bn, blk, 1, np.array([0, bn], dtype=np.int32))
+    elif kind == "bilu":
+        pc.set_bilu(bn, blk)
+    else:
+        pc.set_ilu(bn)
+    pc.prepare()
+    b = s["rhs"]
+    x = b.copy()
+    pc.apply(x)
+    if kind in ("blusgs", "pblusgs"):
+        ref = port.precon_apply(s, b, icolors=[0, bn] if kind == "pblusgs" else None)
+    elif kind == "bilu":
+        fv = port.bilu_factor(s)
+        np.testing.assert_array_equal(vals, fv)
+        ref = port.bilu_apply(s, fv, b)
+    else:
+        fv = port.ilu_factor(s)
+        np.testing.assert_array_equal(vals, fv)
+        ref = port.ilu_apply(s, fv, b)
+    np.testing.assert_array_equal(x, ref)
+    A = SpMat(bn, blk, s["rowptr"], s["colidx"], s["values"])
+    y = np.zeros(bn * blk)
+    A.mult(1.0, b, 0.0, y)
+    np.testing.assert_array_equal(y, port.bsr_spmv(s, b))
+    if kind != "ilu":
+        pc2 = Precon(s["rowptr"], s["colidx"], s["diagslots"], np.array(s["values"]))
+        pc2.set_blusgs(bn, blk)
+        pc2.prepare()
+        tol = 1e-12 * float(np.linalg.norm(b))
+        sv = Solver(bn * blk, 0, 20, tol, kind="bicgstab")
+        xs = np.zeros(bn * blk)
+        sv.solve(pc2, A, xs, np.ascontiguousarray(b))
+        assert sv.result()[0] == 0
+        assert np.linalg.norm(port.bsr_spmv(s, xs) - b) <= 1e-10 * np.linalg.norm(b)

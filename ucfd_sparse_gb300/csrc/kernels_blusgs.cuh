@@ -278,6 +278,10 @@ __global__ void fs_blusgs_prepare_kernel(long long N, int P, const int *nei, con
 // order of the products and subtractions is kept; padding entries only
 // skip their contribution).  PW == 0 is the generic runtime-width loop.
 //
+// Everything but the neighbour increments du is read once per sweep (the
+// J and LU tiles, rhs, nei, fa) and is loaded with the streaming
+// (evict-first) policy, so that du, gathered at every neighbour, keeps L2.
+//
 // DEP (PW > 0 only): launched as a programmatic dependent of the previous
 // sweep launch (one colour after the other).  The grid lets its own
 // dependent start at once, then loads every input the previous launch
@@ -303,15 +307,15 @@ __global__ void __launch_bounds__(256) fs_blusgs_sweep_kernel(int t0, int t1, lo
     const S *Jk = J + ::ucfd::tile_index(k, 0, (long long)P * B2);
     S b[B];
 #pragma unroll
-    for (int r = 0; r < B; ++r) b[r] = rhs[(var0 + r) * N + k];
+    for (int r = 0; r < B; ++r) b[r] = __ldcs(rhs + (var0 + r) * N + k);
     const S rvk = rv[k];
     if constexpr (PW > 0) {
         int nb[PW];
         S fv[PW];
 #pragma unroll
         for (int p = 0; p < PW; ++p) {
-            nb[p] = __ldg(nei + p * N + k);
-            fv[p] = __ldg(fa + p * N + k) * rvk;
+            nb[p] = __ldcs(nei + p * N + k);
+            fv[p] = __ldcs(fa + p * N + k) * rvk;
         }
         if constexpr (DEP) asm volatile("griddepcontrol.wait;" ::: "memory");
         S x[PW][B];
@@ -326,7 +330,7 @@ __global__ void __launch_bounds__(256) fs_blusgs_sweep_kernel(int t0, int t1, lo
             const S *Jp = Jk + ((long long)p * B2 << 5);
             S jv[B2];
 #pragma unroll
-            for (int e = 0; e < B2; ++e) jv[e] = __ldg(Jp + (e << 5));
+            for (int e = 0; e < B2; ++e) jv[e] = __ldcs(Jp + (e << 5));
             if (nb[p] >= 0) {
 #pragma unroll
                 for (int r = 0; r < B; ++r) {
@@ -339,9 +343,9 @@ __global__ void __launch_bounds__(256) fs_blusgs_sweep_kernel(int t0, int t1, lo
         }
     } else {
         for (int p = 0; p < P; ++p) {
-            const int nb = __ldg(nei + p * N + k);
+            const int nb = __ldcs(nei + p * N + k);
             if (nb < 0) break;
-            const S fv = __ldg(fa + p * N + k) * rvk;
+            const S fv = __ldcs(fa + p * N + k) * rvk;
             S x[B];
 #pragma unroll
             for (int c = 0; c < B; ++c) x[c] = du[(var0 + c) * N + nb];
@@ -350,7 +354,7 @@ __global__ void __launch_bounds__(256) fs_blusgs_sweep_kernel(int t0, int t1, lo
             for (int r = 0; r < B; ++r) {
                 S val = S(0);
 #pragma unroll
-                for (int c = 0; c < B; ++c) val += __ldg(Jp + ((r * B + c) << 5)) * x[c];
+                for (int c = 0; c < B; ++c) val += __ldcs(Jp + ((r * B + c) << 5)) * x[c];
                 b[r] -= val * fv;
             }
         }
@@ -358,7 +362,7 @@ __global__ void __launch_bounds__(256) fs_blusgs_sweep_kernel(int t0, int t1, lo
     S lu[B2];
     const S *LUk = LU + ::ucfd::tile_index(k, 0, B2);
 #pragma unroll
-    for (int e = 0; e < B2; ++e) lu[e] = __ldg(LUk + (e << 5));
+    for (int e = 0; e < B2; ++e) lu[e] = __ldcs(LUk + (e << 5));
     lusub_dev<S, B>(lu, b);
 #pragma unroll
     for (int r = 0; r < B; ++r) du[(var0 + r) * N + k] = b[r];
@@ -386,17 +390,17 @@ __global__ void __launch_bounds__(128) fs_blusgs_sweep_small_kernel(int t0, int 
     float b[B], fv[PW], jv[PW][B2], lu[B2];
     int nb[PW];
 #pragma unroll
-    for (int r = 0; r < B; ++r) b[r] = rhs[(var0 + r) * N + k];
+    for (int r = 0; r < B; ++r) b[r] = __ldcs(rhs + (var0 + r) * N + k);
     const float rvk = rv[k];
 #pragma unroll
     for (int p = 0; p < PW; ++p) {
-        nb[p] = __ldg(nei + p * N + k);
-        fv[p] = __ldg(fa + p * N + k) * rvk;
+        nb[p] = __ldcs(nei + p * N + k);
+        fv[p] = __ldcs(fa + p * N + k) * rvk;
 #pragma unroll
-        for (int e = 0; e < B2; ++e) jv[p][e] = __ldg(Jk + ((p * B2 + e) << 5));
+        for (int e = 0; e < B2; ++e) jv[p][e] = __ldcs(Jk + ((p * B2 + e) << 5));
     }
 #pragma unroll
-    for (int e = 0; e < B2; ++e) lu[e] = __ldg(LUk + (e << 5));
+    for (int e = 0; e < B2; ++e) lu[e] = __ldcs(LUk + (e << 5));
     asm volatile("griddepcontrol.wait;" ::: "memory");
     float x[PW][B];
 #pragma unroll

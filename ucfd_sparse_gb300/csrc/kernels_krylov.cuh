@@ -12,20 +12,33 @@
 
 namespace UCFD_KNS {
 
+// A read-only load: streaming (evict-first, ld.global.cs) when CS, else
+// through the read-only cache.
+template <bool CS, typename T>
+__device__ __forceinline__ T ld_once(const T *p) {
+    if constexpr (CS) return __ldcs(p);
+    else return __ldg(p);
+}
+
 // acc[r] += SGN * sum over the ELL row k of (block_p x_{col_p})[r], entries in
 // stored order, each block product summed over its columns first (the
 // reference's order, sparsemat.c:82-97, blusgs.c:113-124).  PW > 0: the
 // row width is at most PW and the loop is unrolled so that every column
 // index, then every gathered x and block value, is requested up front;
 // PW == 0: runtime-width loop.  Padding entries (column < 0) end the row.
-template <typename Tv, typename Tx, typename Ta, int B, int PW, int SGN>
+// CS: columns and block values, read once per product, are loaded with the
+// streaming (evict-first) policy so that the gathered vector x, which every
+// row reads at its neighbours, stays in L2 (the matvec; the preconditioner
+// sweeps keep cached loads, which measured faster there: the last colour of
+// the lower sweep is the first of the upper one).
+template <typename Tv, typename Tx, typename Ta, int B, int PW, int SGN, bool CS = false>
 __device__ __forceinline__ void ell_row_products(long long k, int bn, int P, const int *col, const Tv *val,
                                                  const Tx *x, Ta *acc) {
     constexpr int B2 = B * B;
     if constexpr (PW > 0) {
         int c[PW];
 #pragma unroll
-        for (int p = 0; p < PW; ++p) c[p] = p < P ? __ldg(col + (long long)p * bn + k) : -1;
+        for (int p = 0; p < PW; ++p) c[p] = p < P ? ld_once<CS>(col + (long long)p * bn + k) : -1;
         Ta xv[PW][B];
 #pragma unroll
         for (int p = 0; p < PW; ++p) {
@@ -43,7 +56,7 @@ __device__ __forceinline__ void ell_row_products(long long k, int bn, int P, con
                 for (int r = 0; r < B; ++r) {
                     Ta v = Ta(0);
 #pragma unroll
-                    for (int cc = 0; cc < B; ++cc) v += (Ta)__ldg(vp + (long long)(r * B + cc) * bn) * xv[p][cc];
+                    for (int cc = 0; cc < B; ++cc) v += (Ta)ld_once<CS>(vp + (long long)(r * B + cc) * bn) * xv[p][cc];
                     if (SGN > 0) acc[r] += v;
                     else acc[r] -= v;
                 }
@@ -51,7 +64,7 @@ __device__ __forceinline__ void ell_row_products(long long k, int bn, int P, con
         }
     } else {
         for (int p = 0; p < P; ++p) {
-            const int c = __ldg(col + (long long)p * bn + k);
+            const int c = ld_once<CS>(col + (long long)p * bn + k);
             if (c < 0) break;
             Ta xv[B];
 #pragma unroll
@@ -61,7 +74,7 @@ __device__ __forceinline__ void ell_row_products(long long k, int bn, int P, con
             for (int r = 0; r < B; ++r) {
                 Ta v = Ta(0);
 #pragma unroll
-                for (int cc = 0; cc < B; ++cc) v += (Ta)__ldg(vp + (long long)(r * B + cc) * bn) * xv[cc];
+                for (int cc = 0; cc < B; ++cc) v += (Ta)ld_once<CS>(vp + (long long)(r * B + cc) * bn) * xv[cc];
                 if (SGN > 0) acc[r] += v;
                 else acc[r] -= v;
             }
@@ -70,7 +83,10 @@ __device__ __forceinline__ void ell_row_products(long long k, int bn, int P, con
 }
 
 // SpMV_BSR: sparsemat.c:57-101 -- y = alpha*A*x + beta*y.  Tv is the type
-// of the stored values, Ta the accumulation type.
+// of the stored values, Ta the accumulation type.  With beta == 0 y is not
+// read (the BLAS convention): the reference forms beta*y regardless, which
+// turns an uninitialised y holding NaN or Inf into NaN; for a finite y the
+// results agree (up to the sign of a zero).
 template <typename Tv, typename Ta, int B, int PW>
 __global__ void __launch_bounds__(256) bsr_spmv_kernel(int bn, int P, const int *col, const Tv *val,
                                                        double alpha, const double *x, double beta,
@@ -80,11 +96,11 @@ __global__ void __launch_bounds__(256) bsr_spmv_kernel(int bn, int P, const int 
     Ta acc[B];
 #pragma unroll
     for (int r = 0; r < B; ++r) acc[r] = Ta(0);
-    ell_row_products<Tv, double, Ta, B, PW, +1>(i, bn, P, col, val, x, acc);
+    ell_row_products<Tv, double, Ta, B, PW, +1, true>(i, bn, P, col, val, x, acc);
 #pragma unroll
     for (int r = 0; r < B; ++r) {
         const long long o = (long long)i * B + r;
-        y[o] = alpha * (double)acc[r] + beta * y[o];
+        y[o] = beta == 0.0 ? alpha * (double)acc[r] : alpha * (double)acc[r] + beta * y[o];
     }
 }
 
@@ -627,7 +643,10 @@ __global__ void bc_omega_kernel(int nb, const double *part, BcState *st, double 
         tt += q[3];
         ss += q[4];
     }
-    const double omega = ts / tt;
+    // (t, t) == 0 means s == 0 (t = A inv(M) s): x + alpha pt already solves
+    // the system.  The reference divides regardless (0/0 = NaN, after which
+    // it never converges); omega = 0 gives r = s = 0 and a zero estimate.
+    const double omega = tt != 0.0 ? ts / tt : 0.0;
     st->omega = omega;
     st->rho_new = phi - omega * rtt;
     const double res = sqrt(fabs(ss - 2.0 * omega * ts + omega * omega * tt));

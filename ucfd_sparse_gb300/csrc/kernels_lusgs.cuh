@@ -181,7 +181,10 @@ __device__ __forceinline__ unsigned active_faces(const ScalarSweepArgs<T> &a, in
 // warp works on its own k-th active face at step k, so a warp runs as many
 // face steps as its busiest lane has active faces (not one per slot that
 // any lane has active).  All gathers of the step's faces are issued before
-// any flux is evaluated (latency hiding).  Each face's term
+// any flux is evaluated (latency hiding).  (The geometry stays on cached
+// loads: at step k the lanes of a warp read different face rows of the same
+// cells, which later steps find in L1; streaming loads measured slower.)
+// Each face's term
 // ((F(u+du) - F(u)) - kappa lam du) * area * rcp_vol (lusgs.c:143-205) is
 // added to df in order (ACC) or stored in c[k] for the caller to add.
 template <typename T, int NV, int NFV, int NDIMS, bool RANS, bool COHERENT, int NB, int KB, bool ACC>
