@@ -190,14 +190,23 @@ class Problem:
         cfg.pop("source", None)
         return cfg
 
-    def step(self, rtol, max_pairs, inner):
+    def step(self, rtol, max_pairs, inner, calls=None):
+        """One pseudo-time step; with `calls` (a dict) the host wall time of
+        each C-ABI call is added to it (the calls on host inputs are
+        synchronous, so this is each call's whole cost)."""
         S = self.S
-        S.blusgs_pack(0, 0.0)
-        S.blusgs_ns_prepare()
-        S.blusgs_reset()
-        pairs, rel = S.blusgs_solve(rtol, max_pairs, inner)
-        S.blusgs_update(0)
-        return pairs, rel
+        steps = (("pack", lambda: S.blusgs_pack(0, 0.0)), ("prepare", S.blusgs_ns_prepare),
+                 ("reset", S.blusgs_reset), ("solve", lambda: S.blusgs_solve(rtol, max_pairs, inner)),
+                 ("update", lambda: S.blusgs_update(0)))
+        out = None
+        for name, f in steps:
+            t = time.perf_counter()
+            r = f()
+            if calls is not None:
+                calls[name] = calls.get(name, 0.0) + time.perf_counter() - t
+            if name == "solve":
+                out = r
+        return out
 
     def h2d_bytes(self):
         c = self.case
@@ -410,10 +419,19 @@ def run_gpu(args):
     barrier(dist, device)
     t0 = time.perf_counter()
     pe = []
+    calls = {}
     for _ in range(args.steps):
-        pe.append(Ph.step(args.rtol, args.max_pairs, args.inner)[0])
+        pe.append(Ph.step(args.rtol, args.max_pairs, args.inner, calls)[0])
     torch.cuda.synchronize()
     e2e_s = reduce_max((time.perf_counter() - t0) / args.steps, dist, device)
+    # the same pinned jmat copied alone (torch copy, one transfer): the host link's rate for it
+    jdev = torch.empty(Ph.e["jmat"].shape, dtype=Ph.e["jmat"].dtype, device=device)
+    torch.cuda.synchronize()
+    tj = time.perf_counter()
+    jdev.copy_(Ph.e["jmat"], non_blocking=True)
+    torch.cuda.synchronize()
+    jmat_gbps = Ph.e["jmat"].numel() * 8 / (time.perf_counter() - tj) / 1e9
+    del jdev
     e2e_val = reduce_sum(N * statistics.mean(pe) / e2e_s, dist, device) if dist else N * statistics.mean(pe) / e2e_s
 
     out = None
@@ -436,7 +454,9 @@ def run_gpu(args):
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": Ph.h2d_bytes(),
-                    "d2h_bytes_per_step": Ph.d2h_bytes(), "ms_per_step": e2e_s * 1e3},
+                    "d2h_bytes_per_step": Ph.d2h_bytes(), "ms_per_step": e2e_s * 1e3,
+                    "ms_per_call": {k: v * 1e3 / args.steps for k, v in calls.items()},
+                    "jmat_copy_GBps": jmat_gbps},
             "gpu_launches": launches_per_step(nlev, int(round(pairs_mean)), args.inner, True) * args.steps,
             "clocks": clocks,
             "launch": tuned or "defaults (--no-autotune)",

@@ -50,11 +50,15 @@ UCFD_EXTERN ucfd_status_t UCFDSolverCreateBICGSTAB(Solver *solver, UCFDInt n, UC
                                                    UCFDReal tol);
 
 /* ---- GB300 extensions ------------------------------------------------ */
-/* UCFD_PREC_FP32: mixed-precision GMRES -- inside each restart cycle the
+/* UCFD_PREC_FP64 (default): the reference's arithmetic in every product.
+ * UCFD_PREC_FP64_FMA: the same sums with fused multiply-adds (not
+ * bit-matched to the reference).
+ * UCFD_PREC_FP32: mixed-precision GMRES -- inside each restart cycle the
  * matrix-vector products use FP32 values and the preconditioner runs in
  * FP32, while the Arnoldi orthogonalisation, Givens/least-squares solve and
  * the true residual b - A x at every restart stay FP64 (iterative
- * refinement).  Before the first UCFDSolve. */
+ * refinement; the residual's product with fused multiply-adds).  Before
+ * the first UCFDSolve. */
 UCFD_EXTERN ucfd_status_t UCFDSolverSetPrecision(Solver solver, int precision);
 /* Happy-breakdown tolerance (default 1e-12, solver.c:11). */
 UCFD_EXTERN ucfd_status_t UCFDSolverSetHappyTol(Solver solver, UCFDReal haptol);

@@ -125,7 +125,7 @@ def test_gmres_matches_oracle(name, golden, port, ucfd):
     assert res <= g["tol"]
 
 
-@pytest.mark.parametrize("prec", [0, 2])
+@pytest.mark.parametrize("prec", [0, 1, 2])
 def test_gmres_coloured_and_mixed_reach_1e10(prec, port, ucfd):
     from ucfd_sparse_gb300.krylov import Precon, Solver, SpMat
     s0 = cases.bsr_case(mesh=8, seed=2)

@@ -175,11 +175,16 @@ struct _SpMat {
             UCFD_CUDA(cudaStreamSynchronize(kstream()));
         }
     }
-    // y = alpha A x + beta y on device vectors
-    void mult(double alpha, const double *x, double beta, double *y, bool fp32, cudaStream_t s) {
-        if (fp32) {
+    // y = alpha A x + beta y on device vectors.  kind: UCFD_PREC_FP64 the
+    // reference's arithmetic (separate multiply and add, bit-exact),
+    // UCFD_PREC_FP64_FMA the same sums with fused multiply-adds (half the FP64
+    // instructions), UCFD_PREC_FP32 FP32 values and accumulation.
+    void mult(double alpha, const double *x, double beta, double *y, int kind, cudaStream_t s) {
+        if (kind == UCFD_PREC_FP32) {
             ensure32();
             kfast::bsr_spmv<float, float>(blk, bn, ell.P, ell.col.p, ell.val32.p, alpha, x, beta, y, 0, s);
+        } else if (kind == UCFD_PREC_FP64_FMA) {
+            kfast::bsr_spmv<double, double>(blk, bn, ell.P, ell.col.p, ell.val.p, alpha, x, beta, y, 0, s);
         } else {
             kexact::bsr_spmv<double, double>(blk, bn, ell.P, ell.col.p, ell.val.p, alpha, x, beta, y, 0, s);
         }
@@ -445,6 +450,8 @@ struct _Solver {
     void solve_bicgstab(SpMat A, Precon pc, double *x, const double *b, cudaStream_t s) {
         constexpr int kChunk = 4;
         const long long nn = n;
+        // the reference's products (bit-exact) unless the solver runs with FMA
+        const int mk = prec == UCFD_PREC_FP64_FMA ? UCFD_PREC_FP64_FMA : UCFD_PREC_FP64;
         const int nb = kfast::gm_blocks(nn);
         for (DevBuf<double> *v : {&br, &brt, &bp, &bpt, &bv, &bs, &bsh, &bt}) v->ensure((size_t)n);
         bpart.ensure((size_t)5 * nb);
@@ -458,7 +465,7 @@ struct _Solver {
         }
         // r = b - A x, r~ = r, rho = (r~, r)
         UCFD_CUDA(cudaMemcpyAsync(br.p, b, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-        A->mult(-1.0, x, 1.0, br.p, false, s);
+        A->mult(-1.0, x, 1.0, br.p, mk, s);
         UCFD_CUDA(cudaMemcpyAsync(brt.p, br.p, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
         kfast::bc_dot(nn, brt.p, br.p, bpart.p, nullptr, s);
         kfast::bc_start(nb, bpart.p, bst.p, maxiter, s);
@@ -473,12 +480,12 @@ struct _Solver {
             for (int q = 0; q < kChunk && queued < maxiter; ++q, ++queued) {
                 kfast::bc_direction(nn, bst.p, br.p, bv.p, bp.p, bpt.p, s);
                 pc->apply(bpt.p, s);
-                A->mult(1.0, bpt.p, 0.0, bv.p, false, s);
+                A->mult(1.0, bpt.p, 0.0, bv.p, mk, s);
                 kfast::bc_dot(nn, brt.p, bv.p, bpart.p, bst.p, s);
                 kfast::bc_alpha(nb, bpart.p, bst.p, s);
                 kfast::bc_s(nn, bst.p, br.p, bv.p, bs.p, bsh.p, s);
                 pc->apply(bsh.p, s);
-                A->mult(1.0, bsh.p, 0.0, bt.p, false, s);
+                A->mult(1.0, bsh.p, 0.0, bt.p, mk, s);
                 kfast::bc_fused5(nn, brt.p, bs.p, bt.p, bpart.p, bst.p, s);
                 kfast::bc_omega(nb, bpart.p, bst.p, tol, hist_d, s);
                 kfast::bc_update(nn, bst.p, bpt.p, bsh.p, bs.p, bt.p, x, br.p, s);
@@ -514,9 +521,10 @@ struct _Solver {
         if (trace) hist.assign(std::max(maxiter, 0), 0.0);
         stat = INITIALIZED;
         while (iter < maxiter) {
-            // r = b - A x, abeta = ||r||  (true residual, FP64 values)
+            // r = b - A x, abeta = ||r||  (true residual, FP64 values; with FMA in
+            // the FMA and mixed modes, which are not bit-matched to the reference)
             UCFD_CUDA(cudaMemcpyAsync(r.p, b, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-            A->mult(-1.0, x, 1.0, r.p, false, s);
+            A->mult(-1.0, x, 1.0, r.p, prec == UCFD_PREC_FP64 ? UCFD_PREC_FP64 : UCFD_PREC_FP64_FMA, s);
             kfast::norm2_to(n, r.p, part.p, abeta.p, s);
             UCFD_CUDA(cudaMemcpyAsync(h_abeta.p, abeta.p, sizeof(double), cudaMemcpyDeviceToHost, s));
             UCFD_CUDA(cudaStreamSynchronize(s));
@@ -532,7 +540,7 @@ struct _Solver {
             kfast::gm_scale(n, st.p, r.p, V.p, s);
             for (int j = 0; j < m; ++j) {
                 const double *vj = V.p + (size_t)j * ldv;
-                A->mult(1.0, vj, 0.0, w.p, mixed, s);
+                A->mult(1.0, vj, 0.0, w.p, prec, s);
                 pc->apply(w.p, s);
                 const int K = j + 1;
                 double *Hc = H.p + (size_t)j * ld;
@@ -647,7 +655,7 @@ static ucfd_status_t mat_mult(UCFDReal alpha, SpMat mat, UCFDReal *x, UCFDReal b
     const double *xd = device_view<double>(x, n, mat->sx, s);
     const bool ydev = is_device_ptr(y);
     double *yd = ydev ? y : const_cast<double *>(device_view<double>(y, n, mat->sy, s));
-    mat->mult(alpha, xd, beta, yd, fp32, s);
+    mat->mult(alpha, xd, beta, yd, fp32 ? UCFD_PREC_FP32 : UCFD_PREC_FP64, s);
     UCFD_CHECK_LAUNCH();
     if (!ydev) UCFD_CUDA(cudaMemcpyAsync(y, yd, n * sizeof(double), cudaMemcpyDeviceToHost, s));
     UCFD_CUDA(cudaStreamSynchronize(s));
