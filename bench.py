@@ -230,6 +230,15 @@ def launches_per_step(nlev, pairs, inner, mixed):
 # CPU baseline (the oracle: the reference's CPU path restated, or the
 # reference itself where it was compiled on this machine)
 # ---------------------------------------------------------------------------
+def headline_config(args, N, ncolors, ws):
+    """The workload of the headline line (both arms)."""
+    return {"workload": f"BLU-SGS 5x5 face Jacobians, {args.mesh}^3 jittered (+-0.2h) randomly permuted "
+                        f"hex ({N} cells), greedy colouring in {args.coloring} order ({ncolors} colours), "
+                        f"solve to rtol {args.rtol:g} per pseudo-time step", "cells": N, "colors": ncolors,
+            "coloring": args.coloring, "inner_sweeps": args.inner, "fp64_check_every": args.check,
+            "l2": "inputs larger than L2 (no flush needed)", "parallelism": f"replicas x{ws}"}
+
+
 def cpu_baseline(case, pairs=1, repeats=1):
     """One bounded sample: Pack, NS Prepare, `pairs` sweep pairs with
     SubResidual, Update on the full mesh, with the reference's CPU code
@@ -298,8 +307,10 @@ def run_reference(args):
     if rank != 0:
         barrier(dist)
         return
+    from ucfd_sparse_gb300 import coloredlusgs as cl
     case = make_case(args.mesh)
     N = case["nlocal"]
+    ncolors = len(cl.greedy_coloring_csr(case["rowptr"], case["colidx"], order=args.coloring)[1])
     for _ in range(max(args.warmup, 0)):
         cpu_baseline(case, pairs=args.ref_pairs)
     times = []
@@ -311,8 +322,7 @@ def run_reference(args):
     out = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": T * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": {"workload": f"BLU-SGS 5x5, {args.mesh}^3 jittered permuted hex ({N} cells), CPU sample of "
-                                  f"{args.ref_pairs} sweep pair(s) per step", "cells": N},
+           "config": headline_config(args, N, ncolors, ws),
            "cpu_baseline": {"value": val, "unit": UNIT, "cores": r["cores"], "kind": r["kind"], "sample": r["sample"]},
            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
@@ -441,12 +451,7 @@ def run_gpu(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 sweeps + f64 refinement/LU/residual", "data": "synthetic",
-            "config": {"workload": f"BLU-SGS 5x5 face Jacobians, {args.mesh}^3 jittered (+-0.2h) randomly permuted "
-                                   f"hex ({N} cells), greedy colouring in {args.coloring} order ({len(rg)} colours), "
-                                   f"solve to rtol {args.rtol:g} per pseudo-time step", "cells": N, "colors": len(rg),
-                       "coloring": args.coloring,
-                       "inner_sweeps": args.inner, "fp64_check_every": args.check, "l2": "inputs larger than L2 (no flush needed)",
-                       "parallelism": f"replicas x{ws}"},
+            "config": headline_config(args, N, len(rg), ws),
             "pairs_per_step": pairs_mean, "relres": max(rel32),
             "fp64": {"ms_per_step": ms64, "pairs_per_step": statistics.mean(pairs64), "relres": max(rel64),
                      "value": N * statistics.mean(pairs64) / (ms64 * 1e-3)},

@@ -56,3 +56,5 @@ def test_reference_arm_under_torchrun_rank0_only():
     assert j["impl"] == "reference" and j["value"] > 0 and j["n_gpus"] == 2
     assert j["cpu_baseline"]["kind"] in ("reference", "port")
     assert j["e2e"]["h2d_bytes_per_step"] == 0
+    # the same workload description as the GPU arm's line
+    assert j["config"]["workload"].startswith("BLU-SGS 5x5 face Jacobians") and j["config"]["colors"] > 1
