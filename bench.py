@@ -656,10 +656,12 @@ def run_gmres(args):
         sv.solve(pc, A, x, d["rhs"])  # warm-up
         x.zero_()
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("gmres_fp64" if prec == 1 else "gmres_mixed")
         t = time.perf_counter()
         sv.solve(pc, A, x, d["rhs"])
         torch.cuda.synchronize()
         el = time.perf_counter() - t
+        torch.cuda.nvtx.range_pop()
         st, it, r = sv.result()
         res[prec] = dict(s=el, stat=st, restarts=it, resid=r / (tol / 1e-10), arnoldi=sv.arnoldi_steps(),
                          prepare_ms=reprep_ms)
@@ -705,10 +707,12 @@ def run_gmres(args):
         sv.solve(pc, A, x, d["rhs"])  # warm-up
         x.zero_()
         torch.cuda.synchronize()
+        torch.cuda.nvtx.range_push("bicgstab_" + pc_kind)
         t = time.perf_counter()
         sv.solve(pc, A, x, d["rhs"])
         torch.cuda.synchronize()
         el = time.perf_counter() - t
+        torch.cuda.nvtx.range_pop()
         st, it, r = sv.result()
         bic[pc_kind] = dict(s=el, stat=st, iters=it, resid=r / (tol / 1e-10), first_prepare_s=prep_s,
                             prepare_ms=reprep_ms)

@@ -337,38 +337,114 @@ __device__ __forceinline__ void gm_block_partials(const double *acc, int KK, dou
     }
 }
 
-// Per-block partial dots h[k] = sum_i V[k][i] * w[i], k < K <= KM.
+// Basis vectors whose entries a thread of the orthogonalisation kernels
+// holds in registers at once (all K when K <= 16, else chunks of 8).
 template <int KM>
-__global__ void __launch_bounds__(256, (KM > 8 ? 3 : 4)) gm_dots_kernel(long long n, int K, const double *V, long long ldv,
-                                                      const double *w, double *part) {
+__host__ __device__ constexpr int gm_chunk() { return KM <= 16 ? KM : 8; }
+
+__device__ __forceinline__ double2 ld_pair(const double *row, long long j) {
+    return reinterpret_cast<const double2 *>(row)[j];
+}
+
+// Per-block partial dots h[k] = sum_i V[k][i] * w[i], k < K <= KM.  A thread
+// takes two adjacent entries per step with 16-byte loads (every basis row
+// starts on a 32-entry boundary) and requests the pair of every vector of a
+// chunk before the first product, so each thread keeps many loads in flight;
+// an odd last entry is added by the first thread.  (A layout spreading the
+// vectors over the warps of a block, with the sums meeting in shared memory,
+// measured slower: its barriers and idle warps at small K cost more than the
+// occupancy it gains.)
+template <int KM>
+__global__ void __launch_bounds__(256, 2) gm_dots_kernel(long long n, int K, const double *V, long long ldv,
+                                                         const double *w, double *part) {
+    constexpr int CH = gm_chunk<KM>();
     double acc[KM];
 #pragma unroll
     for (int k = 0; k < KM; ++k) acc[k] = 0.0;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x) {
-        const double wi = w[i];
+    const long long n2 = n >> 1;
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n2;
+         j += (long long)gridDim.x * blockDim.x) {
+        const double2 wi = ld_pair(w, j);
+#pragma unroll
+        for (int k0 = 0; k0 < KM; k0 += CH) {
+            double2 v[CH];
+#pragma unroll
+            for (int c = 0; c < CH; ++c) v[c] = k0 + c < K ? ld_pair(V + (k0 + c) * ldv, j) : make_double2(0.0, 0.0);
+#pragma unroll
+            for (int c = 0; c < CH; ++c) {
+                acc[k0 + c] += v[c].x * wi.x;
+                acc[k0 + c] += v[c].y * wi.y;
+            }
+        }
+    }
+    if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+        const double wi = w[n - 1];
 #pragma unroll
         for (int k = 0; k < KM; ++k)
-            if (k < K) acc[k] += V[k * ldv + i] * wi;
+            if (k < K) acc[k] += V[k * ldv + n - 1] * wi;
     }
     gm_block_partials<KM>(acc, K, part);
 }
 
 // w_out = w - V h (gemvcol with alpha -1, beta 1), then either the partial
-// dots V^T w_out (mode 0) or the partial sum of w_out^2 (mode 1).  The
-// second pass over V re-reads the values this thread just loaded (L1).
+// dots V^T w_out (mode 0) or the partial sum of w_out^2 (mode 1).  Two
+// adjacent entries per thread and step, as in gm_dots_kernel; with K <= 16
+// the loaded entries of V stay in registers for the second product, with
+// more vectors the chunks are loaded again (from L1 / L2).  With more than
+// 8 vectors one block per SM (up to 255 registers, no spills) still keeps
+// over 100 KB of loads in flight per SM.
 template <int KM>
-__global__ void __launch_bounds__(256, (KM > 8 ? 2 : 4)) gm_update_kernel(long long n, int K, const double *V, long long ldv,
-                                                        const double *h, double *w, int mode,
-                                                        double *part) {
+__global__ void __launch_bounds__(256, (KM > 8 ? 1 : 2)) gm_update_kernel(long long n, int K, const double *V,
+                                                                          long long ldv, const double *h, double *w,
+                                                                          int mode, double *part) {
+    constexpr int CH = gm_chunk<KM>();
     double acc[KM];
 #pragma unroll
     for (int k = 0; k < KM; ++k) acc[k] = 0.0;
     __shared__ double hs[KM];
     if (threadIdx.x < KM) hs[threadIdx.x] = threadIdx.x < K ? h[threadIdx.x] : 0.0;
     __syncthreads();
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x) {
+    const long long n2 = n >> 1;
+    for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n2;
+         j += (long long)gridDim.x * blockDim.x) {
+        double sx = 0.0, sy = 0.0;
+        double2 v[CH];
+#pragma unroll
+        for (int k0 = 0; k0 < KM; k0 += CH) {
+#pragma unroll
+            for (int c = 0; c < CH; ++c) v[c] = k0 + c < K ? ld_pair(V + (k0 + c) * ldv, j) : make_double2(0.0, 0.0);
+#pragma unroll
+            for (int c = 0; c < CH; ++c) {
+                sx += v[c].x * hs[k0 + c];
+                sy += v[c].y * hs[k0 + c];
+            }
+        }
+        const double2 wo = ld_pair(w, j);
+        double2 wn;
+        wn.x = -1.0 * sx + 1.0 * wo.x;
+        wn.y = -1.0 * sy + 1.0 * wo.y;
+        reinterpret_cast<double2 *>(w)[j] = wn;
+        if (mode == 0) {
+#pragma unroll
+            for (int k0 = 0; k0 < KM; k0 += CH) {
+                if (CH < KM) {
+#pragma unroll
+                    for (int c = 0; c < CH; ++c)
+                        v[c] = k0 + c < K ? ld_pair(V + (k0 + c) * ldv, j) : make_double2(0.0, 0.0);
+                }
+#pragma unroll
+                for (int c = 0; c < CH; ++c) {
+                    acc[k0 + c] += v[c].x * wn.x;
+                    acc[k0 + c] += v[c].y * wn.y;
+                }
+            }
+        } else {
+            acc[0] += wn.x * wn.x;
+            acc[0] += wn.y * wn.y;
+        }
+    }
+    if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+        const long long i = n - 1;
         double s = 0.0;
 #pragma unroll
         for (int k = 0; k < KM; ++k)
@@ -386,14 +462,24 @@ __global__ void __launch_bounds__(256, (KM > 8 ? 2 : 4)) gm_update_kernel(long l
     gm_block_partials<KM>(acc, mode == 0 ? K : 1, part);
 }
 
-// Sum the per-block partials: out[k] = sum_b part[b][k] (one block, fixed order).
-__global__ void gm_reduce_kernel(int nblocks, int K, const double *part, double *out, int accumulate) {
-    const int k = threadIdx.x;
-    if (k >= K) return;
+// Sum of part[b * stride] over b < nb by a whole block: a fixed assignment
+// of partials to threads and a fixed tree, so every call gives the same
+// value; valid in thread 0.
+__device__ __forceinline__ double block_sum_partials(const double *part, int nb, long long stride) {
     double s = 0.0;
-    for (int b = 0; b < nblocks; ++b) s += part[(long long)b * kMaxK + k];
-    if (accumulate) out[k] += 1.0 * s;
-    else out[k] = s;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) s += part[b * stride];
+    return block_sum(s);
+}
+
+// Sum the per-block partials: out[k] = sum_b part[b][k] (block k, fixed order).
+__global__ void __launch_bounds__(256) gm_reduce_kernel(int nblocks, const double *part, double *out,
+                                                        int accumulate) {
+    const int k = blockIdx.x;
+    const double s = block_sum_partials(part + k, nblocks, kMaxK);
+    if (threadIdx.x == 0) {
+        if (accumulate) out[k] += 1.0 * s;
+        else out[k] = s;
+    }
 }
 
 // Sum of squares partials (one value per block) into *out (sqrt applied).
@@ -417,10 +503,10 @@ struct GmState {
 };
 
 // Cycle start: beta = sqrt(sum), y[0] = beta, inv = 1/beta, flags reset.
-__global__ void gm_cycle_begin_kernel(int nblocks, const double *part, GmState *st, double *y,
-                                      double *out_norm) {
-    double s = 0.0;
-    for (int b = 0; b < nblocks; ++b) s += part[(long long)b * kMaxK];
+__global__ void __launch_bounds__(256) gm_cycle_begin_kernel(int nblocks, const double *part, GmState *st,
+                                                             double *y, double *out_norm) {
+    const double s = block_sum_partials(part, nblocks, kMaxK);
+    if (threadIdx.x != 0) return;
     const double beta = sqrt(s);
     st->beta = beta;
     st->inv = 1.0 / beta;
@@ -447,12 +533,12 @@ __global__ void gm_scale_kernel(long long n, const GmState *st, const double *sr
 // the Givens residual estimate |y[j+1]| falls below rel_floor * beta, the
 // accuracy an FP32 operator can deliver; the FP64 restart then refreshes the
 // true residual.
-__global__ void gm_givens_kernel(int j, int ld, int nblocks, const double *part_norm, double *H,
-                                 const double *h2, double *cs, double *sn, double *y, double haptol,
-                                 double rel_floor, GmState *st) {
-    if (st->stop) return;
-    double s = 0.0;
-    for (int b = 0; b < nblocks; ++b) s += part_norm[(long long)b * kMaxK];
+__global__ void __launch_bounds__(256) gm_givens_kernel(int j, int ld, int nblocks, const double *part_norm,
+                                                        double *H, const double *h2, double *cs, double *sn,
+                                                        double *y, double haptol, double rel_floor, GmState *st) {
+    if (st->stop) return;  // the same for every thread of the block
+    const double s = block_sum_partials(part_norm, nblocks, kMaxK);
+    if (threadIdx.x != 0) return;
     double *Hc = H + (long long)j * ld;
     for (int i = 0; i <= j; ++i) Hc[i] += 1.0 * h2[i];
     const double hsub = sqrt(s);

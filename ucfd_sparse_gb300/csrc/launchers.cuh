@@ -597,7 +597,8 @@ void gm_update(long long n, int K, const double *V, long long ldv, const double 
 }
 
 void gm_reduce(int nblocks, int K, const double *part, double *out, int accumulate, cudaStream_t s) {
-    gm_reduce_kernel<<<1, kMaxK, 0, s>>>(nblocks, K, part, out, accumulate);
+    if (K <= 0) return;
+    gm_reduce_kernel<<<K, kBlock, 0, s>>>(nblocks, part, out, accumulate);
 }
 
 void gm_sumsq(long long n, const double *x, double *part, cudaStream_t s) {
@@ -605,7 +606,7 @@ void gm_sumsq(long long n, const double *x, double *part, cudaStream_t s) {
 }
 
 void gm_cycle_begin(int nblocks, const double *part, void *st, double *y, double *out_norm, cudaStream_t s) {
-    gm_cycle_begin_kernel<<<1, 1, 0, s>>>(nblocks, part, (GmState *)st, y, out_norm);
+    gm_cycle_begin_kernel<<<1, kBlock, 0, s>>>(nblocks, part, (GmState *)st, y, out_norm);
 }
 
 void gm_scale(long long n, const void *st, const double *src, double *dst, cudaStream_t s) {
@@ -614,8 +615,8 @@ void gm_scale(long long n, const void *st, const double *src, double *dst, cudaS
 
 void gm_givens(int j, int ld, int nblocks, const double *part_norm, double *H, const double *h2, double *cs,
                double *sn, double *y, double haptol, double rel_floor, void *st, cudaStream_t s) {
-    gm_givens_kernel<<<1, 1, 0, s>>>(j, ld, nblocks, part_norm, H, h2, cs, sn, y, haptol, rel_floor,
-                                     (GmState *)st);
+    gm_givens_kernel<<<1, kBlock, 0, s>>>(j, ld, nblocks, part_norm, H, h2, cs, sn, y, haptol, rel_floor,
+                                          (GmState *)st);
 }
 
 void gm_backsub(int ld, const double *H, double *y, const void *st, cudaStream_t s) {
@@ -636,16 +637,15 @@ void axpy_norm(long long n, const S *x, S *y, double *part, double *out, cudaStr
     sqrt_sum_kernel<<<1, 1024, 0, s>>>(nb, part, out);
 }
 
-__global__ void norm_finalize_kernel(int nblocks, const double *part, double *out) {
-    double t = 0.0;
-    for (int b = 0; b < nblocks; ++b) t += part[(long long)b * kMaxK];
-    *out = sqrt(t);
+__global__ void __launch_bounds__(256) norm_finalize_kernel(int nblocks, const double *part, double *out) {
+    const double t = block_sum_partials(part, nblocks, kMaxK);
+    if (threadIdx.x == 0) *out = sqrt(t);
 }
 
 // out = ||x||_2 (two-pass, fixed order).
 void norm2_to(long long n, const double *x, double *part, double *out, cudaStream_t s) {
     gm_sumsq_kernel<<<gm_blocks(n), kBlock, 0, s>>>(n, x, part);
-    norm_finalize_kernel<<<1, 1, 0, s>>>(gm_blocks(n), part, out);
+    norm_finalize_kernel<<<1, kBlock, 0, s>>>(gm_blocks(n), part, out);
 }
 
 // ---- BiCGSTAB ----------------------------------------------------------------
