@@ -605,8 +605,10 @@ def run_lusgs(args):
 
 def run_gmres(args):
     """GMRES(30) with the coloured BLU-SGS preconditioner on the Kuhn-tet
-    BSR 5x5 system, to a 1e-10 relative residual: FP64 and mixed
-    (FP32 matvec + FP32 preconditioner inside FP64 Arnoldi/refinement)."""
+    BSR 5x5 system, to a 1e-10 relative residual: FP64 with fused
+    multiply-adds (the `fp64` entry) and mixed (FP32 matvec + FP32
+    preconditioner inside FP64 Arnoldi/refinement); BiCGSTAB (FP64) with the
+    coloured BLU-SGS and the coloured block ILU(0)."""
     import torch
 
     from ucfd_sparse_gb300 import _build, lib
