@@ -218,7 +218,7 @@ class Problem:
 
 def launches_per_step(nlev, pairs, inner, mixed):
     outer = math.ceil(pairs / inner) if pairs else 0
-    n = 1 + 1 + 1                                  # pack, prepare, update
+    n = 1 + 2 + 1                                  # pack, prepare (jmat transpose + diagonal/LU), update
     n += 2                                         # initial residual + reduction
     n += outer * 2 + pairs * 2 * nlev              # residual per outer loop, sweeps
     if mixed:
