@@ -388,11 +388,11 @@ __global__ void __launch_bounds__(256, 2) gm_dots_kernel(long long n, int K, con
 
 // w_out = w - V h (gemvcol with alpha -1, beta 1), then either the partial
 // dots V^T w_out (mode 0) or the partial sum of w_out^2 (mode 1).  Two
-// adjacent entries per thread and step, as in gm_dots_kernel; with K <= 16
-// the loaded entries of V stay in registers for the second product, with
-// more vectors the chunks are loaded again (from L1 / L2).  With more than
-// 8 vectors one block per SM (up to 255 registers, no spills) still keeps
-// over 100 KB of loads in flight per SM.
+// adjacent entries per thread and step, as in gm_dots_kernel, the loaded
+// entries of V staying in registers for the second product; for more than 16
+// vectors one entry per thread, so that all of them still fit.  With more
+// than 8 vectors one block per SM (up to 255 registers, no spills) still
+// keeps over 100 KB of loads in flight per SM.
 template <int KM>
 __global__ void __launch_bounds__(256, (KM > 8 ? 1 : 2)) gm_update_kernel(long long n, int K, const double *V,
                                                                           long long ldv, const double *h, double *w,
@@ -404,6 +404,29 @@ __global__ void __launch_bounds__(256, (KM > 8 ? 1 : 2)) gm_update_kernel(long l
     __shared__ double hs[KM];
     if (threadIdx.x < KM) hs[threadIdx.x] = threadIdx.x < K ? h[threadIdx.x] : 0.0;
     __syncthreads();
+    if constexpr (KM > 16) {
+        // one entry per thread: all K values of V stay in registers for the
+        // second product (pairs of 32 vectors would not fit)
+        for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+             i += (long long)gridDim.x * blockDim.x) {
+            double v[KM];
+#pragma unroll
+            for (int k = 0; k < KM; ++k) v[k] = k < K ? V[k * ldv + i] : 0.0;
+            double sq = 0.0;
+#pragma unroll
+            for (int k = 0; k < KM; ++k) sq += v[k] * hs[k];
+            const double wn = -1.0 * sq + 1.0 * w[i];
+            w[i] = wn;
+            if (mode == 0) {
+#pragma unroll
+                for (int k = 0; k < KM; ++k) acc[k] += v[k] * wn;
+            } else {
+                acc[0] += wn * wn;
+            }
+        }
+        gm_block_partials<KM>(acc, mode == 0 ? K : 1, part);
+        return;
+    }
     const long long n2 = n >> 1;
     for (long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x; j < n2;
          j += (long long)gridDim.x * blockDim.x) {
