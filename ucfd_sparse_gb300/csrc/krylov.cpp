@@ -1,10 +1,14 @@
 // krylov.cpp -- SpMat / Precon / Solver objects (ucfdmat.h, ucfdprecon.h,
 // ucfdsolver.h) on the GPU.
 //
-// Matrices and preconditioners are copied to the device once, into the
-// ELL-of-blocks layout of kernels_krylov.cuh.  GMRES(m) keeps every vector,
-// the Hessenberg matrix and the Givens state on the device; the host reads
-// one residual norm (and the cycle state) per restart.
+// Matrices and preconditioners live on the device in the ELL-of-blocks
+// layout of kernels_krylov.cuh.  Their structure (schedule, columns, the CSR
+// slot behind every ELL entry) is built on the host once and kept while the
+// fingerprints of rowptr / colidx / diagslots stay the same; new values are
+// gathered, factorised and LU-factored on the device.  GMRES(m) keeps every
+// vector, the Hessenberg matrix and the Givens state on the device; the host
+// reads one residual norm (and the cycle state) per restart.  BiCGSTAB keeps
+// its scalars on the device and reads its stop flag every few iterations.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
