@@ -452,8 +452,11 @@ struct _Solver {
     // stop return at once (the preconditioner and matvec of those only touch
     // scratch vectors).
     void solve_bicgstab(SpMat A, Precon pc, double *x, const double *b, cudaStream_t s) {
-        constexpr int kChunk = 4;
+        // iterations queued between two reads of the device stop flag: the
+        // matvec and preconditioner of an iteration queued after convergence
+        // still run, which costs more than a host read once n is large
         const long long nn = n;
+        const int kChunk = nn >= (1ll << 20) ? 1 : 4;
         // the reference's products (bit-exact) unless the solver runs with FMA
         const int mk = prec == UCFD_PREC_FP64_FMA ? UCFD_PREC_FP64_FMA : UCFD_PREC_FP64;
         const int nb = kfast::gm_blocks(nn);
