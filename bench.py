@@ -82,6 +82,21 @@ def barrier(dist, device=None):
             dist.barrier()
 
 
+def repo_libraries_loaded():
+    """Shared libraries of this repository mapped into the process (from
+    /proc/self/maps): shows which native code an arm ran."""
+    libs = set()
+    try:
+        with open("/proc/self/maps") as f:
+            for line in f:
+                path = line.split()[-1] if len(line.split()) >= 6 else ""
+                if path.startswith(ROOT) and path.endswith(".so"):
+                    libs.add(os.path.relpath(path, ROOT))
+    except OSError:
+        return None
+    return sorted(libs)
+
+
 # ---------------------------------------------------------------------------
 # clocks
 # ---------------------------------------------------------------------------
@@ -239,48 +254,83 @@ def headline_config(args, N, ncolors, ws):
             "l2": "inputs larger than L2 (no flush needed)", "parallelism": f"replicas x{ws}"}
 
 
-def cpu_baseline(case, pairs=1, repeats=1):
-    """One bounded sample: Pack, NS Prepare, `pairs` sweep pairs with
-    SubResidual, Update on the full mesh, with the reference's CPU code
-    (sweeps serial, update/sub-residual OpenMP as in blusgs.c)."""
+# Sweep pairs the headline solve needs per pseudo-time step on this workload:
+# the FP32-sweep + FP64-refinement solve and the plain FP64 solve both reach
+# the 1e-10 relative residual at 40 pairs (the GPU arm reports its own count
+# as pairs_per_step).  The CPU legs compose a step of this many pairs.
+PAIRS_PER_STEP = 40
+
+
+def cpu_impl():
+    """The reference's CPU code for the BLU-SGS step: the reference library
+    compiled from its own sources (oracle/_ref, -O3 -ffast-math as its
+    Makefile.inc) where it was built on this machine, else the oracle's
+    restatement built with the same flags."""
     from oracle import oracle as orc
-    kind = "reference" if orc.ref_available() else "port"
-    threads = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
-    best = float("inf")
-    for _ in range(repeats):
-        t0 = time.perf_counter()
-        if kind == "reference":
-            orc.Ref(fast=True).flowsys_blusgs(case, case["rhs"], case["dt"], case["jmat"], case["vol"], case["upts"],
-                                             nsweeps=pairs)
-        else:
-            orc.Port(fast=True).flowsys_blusgs(case, case["rhs"], case["dt"], case["jmat"], case["vol"],
-                                              case["upts"], nsweeps=pairs)
-        best = min(best, time.perf_counter() - t0)
+    if orc.ref_available():
+        return orc.Ref(fast=True), "reference"
+    return orc.Port(fast=True), "port"
+
+
+def colour_renumbered(case):
+    """The mesh renumbered colour by colour (greedy first-fit in index
+    order, computed by the oracle so that no product library is loaded).  A
+    natural-order sweep of the result is the coloured sweep the GPU runs."""
+    from oracle import oracle as orc
+    from ucfd_sparse_gb300 import meshgen as mg
+    ic, rg, _ = orc.Port(fast=True).greedy_coloring_csr(case["rowptr"], case["colidx"])
+    new = np.empty(case["nlocal"], dtype=np.int64)
+    new[ic] = np.arange(case["nlocal"])
+    return mg.renumber_flowsys(case, new), rg
+
+
+def compose_cpu_step(t_prepare, t_update, t_lower, t_upper_sub, pairs=PAIRS_PER_STEP):
+    """Seconds of one pseudo-time step of `pairs` sweep pairs from the timed
+    pieces: Pack + NSPrepare + Reset, Update, and per pair a lower sweep and
+    an upper sweep + SubResidual (blusgs.c's call sequence)."""
+    return t_prepare + t_update + pairs * (t_lower + t_upper_sub)
+
+
+def cpu_baseline(case, br=None):
+    """A bounded sample of the reference's CPU path on the full mesh (about
+    25 s on 16 Arm cores): Pack + NSPrepare + Reset, one lower sweep, one
+    upper sweep + SubResidual, Update, each timed, composed into a step of
+    PAIRS_PER_STEP pairs.  The reference FlowSys is serial (src/lusgs has
+    no OpenMP), so one core does the work."""
+    if br is None:
+        br, _ = colour_renumbered(case)
+    impl, kind = cpu_impl()
+    ph = impl.blusgs_phases(br, case["rhs"], case["dt"], case["jmat"], case["vol"], case["upts"])
+    tic = time.perf_counter
+    t0 = tic(); ph.pack_prepare(); ph.reset(); t_prep = tic() - t0
+    t0 = tic(); ph.lower(); t_low = tic() - t0
+    t0 = tic(); ph.upper(); ph.sub_residual(); t_up = tic() - t0
+    t0 = tic(); ph.update(); t_upd = tic() - t0
+    ph.close()
+    step = compose_cpu_step(t_prep, t_upd, t_low, t_up)
     N = case["nlocal"]
-    return {"value": N * pairs / best, "unit": UNIT, "cores": threads, "kind": kind,
-            "sample": f"Pack+NSPrepare+{pairs} lower/upper sweep pair(s)+SubResidual+Update on all {N} cells, "
-                      f"FP64, best of {repeats}; sweeps serial as in the reference, {threads} OpenMP threads "
-                      f"available", "seconds": best}
+    return {"value": N * PAIRS_PER_STEP / step, "unit": UNIT, "cores": 1, "kind": kind,
+            "sample": f"FP64 on all {N} cells of the colour-renumbered mesh: Pack+NSPrepare+Reset, one lower "
+                      f"sweep, one upper sweep+SubResidual and Update timed once each and composed into a step "
+                      f"of {PAIRS_PER_STEP} pairs, the GPU arm's unit; serial, as the reference FlowSys",
+            "seconds": {"prepare": t_prep, "lower": t_low, "upper_subresidual": t_up, "update": t_upd,
+                        "composed_step": step}}
 
 
 def lusgs_cpu_baseline(c, iters=1):
     """One bounded sample of the reference's scalar LU-SGS CPU path on the
     same mesh: `iters` pseudo-time iterations of Pack, NS + RANS Prepare,
-    lower and upper sweeps (serial, natural order, as lusgs.c) and Update."""
-    from oracle import oracle as orc
-    kind = "reference" if orc.ref_available() else "port"
-    threads = os.cpu_count() or 1
-    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
-    impl = orc.Ref(fast=True) if kind == "reference" else orc.Port(fast=True)
+    lower and upper sweeps (natural order, as lusgs.c) and Update.  The
+    reference FlowSys is serial (src/lusgs has no OpenMP): one core."""
+    impl, kind = cpu_impl()
     dsrc = np.zeros_like(c["rhs"])
     t0 = time.perf_counter()
     impl.flowsys_lusgs_step(c, c["upts"], c["rhs"], c["dt"], dsrc, c["fspr"], c["tfspr"], rans=True, nsteps=iters)
     sec = time.perf_counter() - t0
     N = c["nlocal"]
-    return {"value": N * iters / sec, "unit": UNIT, "cores": threads, "kind": kind, "seconds": sec,
+    return {"value": N * iters / sec, "unit": UNIT, "cores": 1, "kind": kind, "seconds": sec,
             "sample": f"{iters} iteration(s) of Pack+NS/RANS Prepare+lower/upper sweeps+Update on all {N} cells, "
-                      f"FP64; sweeps serial in natural order as in lusgs.c, {threads} OpenMP threads available"}
+                      f"FP64; serial natural-order sweeps as in lusgs.c"}
 
 
 def krylov_cpu_baseline(s, icolors, tol):
@@ -302,29 +352,75 @@ def krylov_cpu_baseline(s, icolors, tol):
 
 
 def run_reference(args):
+    """The reference's own CPU path (cpu_impl) on the headline workload.
+
+    The unit is the GPU arm's: a pseudo-time step of PAIRS_PER_STEP sweep
+    pairs, cell-updates/s = cells x pairs / step time.  A whole step takes
+    about ten minutes on the host cores, so each timed step is a bounded
+    sample of it: one sweep over all cells, lower sweeps on even steps and
+    upper sweep + SubResidual on odd ones (the serial sweep of the colour-
+    renumbered mesh, as the reference runs it).  Pack + NSPrepare + Reset are
+    timed before the warm-up sweeps and Update after the timed ones; the step
+    time is composed from those and the medians of the sampled sweeps."""
     ws, rank, _ = dist_env()
     dist = dist_init("gloo")
     if rank != 0:
         barrier(dist)
         return
-    from ucfd_sparse_gb300 import coloredlusgs as cl
+    if args.coloring != "index":
+        print(json.dumps({"impl": "reference", "unavailable": "the CPU legs colour in index order only "
+                                                              "(--coloring index)"}))
+        barrier(dist)
+        return
     case = make_case(args.mesh)
     N = case["nlocal"]
-    ncolors = len(cl.greedy_coloring_csr(case["rowptr"], case["colidx"], order=args.coloring)[1])
-    for _ in range(max(args.warmup, 0)):
-        cpu_baseline(case, pairs=args.ref_pairs)
-    times = []
-    for _ in range(args.steps):
-        r = cpu_baseline(case, pairs=args.ref_pairs)
-        times.append(r["seconds"])
-    T = max(statistics.median(times), 1e-12)
-    val = N * args.ref_pairs / T
+    br, rg = colour_renumbered(case)
+    impl, kind = cpu_impl()
+    ph = impl.blusgs_phases(br, case["rhs"], case["dt"], case["jmat"], case["vol"], case["upts"])
+    tic = time.perf_counter
+    t0 = tic()
+    ph.pack_prepare()
+    ph.reset()
+    t_prep = tic() - t0
+    for w in range(args.warmup):
+        (ph.lower if w % 2 == 0 else ph.upper)()
+    lows, ups, samples = [], [], []
+    for k in range(args.steps):
+        t0 = tic()
+        if k % 2 == 0:
+            ph.lower()
+        else:
+            ph.upper()
+            ph.sub_residual()
+        dt_ = tic() - t0
+        samples.append(dt_)
+        (lows if k % 2 == 0 else ups).append(dt_)
+    if not ups:                       # --steps 1: one upper sweep + SubResidual, untimed as a step
+        t0 = tic()
+        ph.upper()
+        ph.sub_residual()
+        ups.append(tic() - t0)
+    t0 = tic()
+    ph.update()
+    t_upd = tic() - t0
+    ph.close()
+    t_low, t_up = statistics.median(lows), statistics.median(ups)
+    step = compose_cpu_step(t_prep, t_upd, t_low, t_up)
+    val = N * PAIRS_PER_STEP / step
+    sample = (f"FP64 on all {N} cells of the colour-renumbered mesh, serial as the reference FlowSys (src/lusgs has "
+              f"no OpenMP); each timed step one sweep (lower on even steps, upper + SubResidual on odd); step of "
+              f"{PAIRS_PER_STEP} pairs composed as Pack+NSPrepare+Reset ({t_prep:.2f} s) + Update ({t_upd:.3f} s) "
+              f"+ {PAIRS_PER_STEP} x (median lower {t_low:.2f} s of {len(lows)} + median upper+SubResidual "
+              f"{t_up:.2f} s of {len(ups)}) = {step:.1f} s")
     out = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": T * 1e3, "higher_is_better": True,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": statistics.mean(samples) * 1e3,
+           "ms_per_step_is": "mean duration of a timed sample (one sweep); the composed step is composed_step_s",
+           "composed_step_s": step, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": headline_config(args, N, ncolors, ws),
-           "cpu_baseline": {"value": val, "unit": UNIT, "cores": r["cores"], "kind": r["kind"], "sample": r["sample"]},
-           "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+           "config": headline_config(args, N, len(rg), ws),
+           "cpu_baseline": {"value": val, "unit": UNIT, "cores": 1, "kind": kind, "sample": sample},
+           "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "libraries_loaded": repo_libraries_loaded()}
     print(json.dumps(out))
     barrier(dist)
 
@@ -419,6 +515,27 @@ def run_gpu(args):
                 "traffic_source": "ncu 96^3 capture, 847 B per cell update, scaled by cells per launch",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s"}
 
+    # ---- error of one step against the FP64 arithmetic of the oracle --------
+    # (UCFD_PREC_FP64 runs the reference's operation order, bit-identical to
+    # the oracle; each step solves the same system, so the per-step
+    # increments dQ = upts_after - upts_before compare directly)
+    def step_increment(P, inner):
+        u0 = P.e["upts"].clone()
+        P.step(args.rtol, args.max_pairs, inner)
+        torch.cuda.synchronize()
+        return P.e["upts"] - u0
+
+    P0 = Problem(case, lc, 0, stream, device)
+    dq0 = step_increment(P0, args.check)
+    del P0
+    torch.cuda.empty_cache()
+    dq0_max = float(dq0.abs().max())
+    err = {"err_vs_fp64": float((step_increment(P32, args.inner) - dq0).abs().max()) / dq0_max,
+           "fp64_fma_err_vs_fp64": float((step_increment(P64, args.check) - dq0).abs().max()) / dq0_max,
+           "definition": "max|dQ - dQ_fp64| / max|dQ_fp64| over all cells and variables, one pseudo-time step "
+                         "solved to rtol, dQ_fp64 from UCFD_PREC_FP64 (the oracle's arithmetic)"}
+    del dq0
+
     # ---- end to end through the C-ABI with pinned host buffers -------------
     Ph = Problem(case, lc, 2, None, device, host_inputs=True)
     if tuned:
@@ -446,7 +563,7 @@ def run_gpu(args):
 
     out = None
     if rank == 0:
-        cpu = cpu_baseline(case, pairs=1) if ws == 1 else None
+        cpu = cpu_baseline(case) if ws == 1 else None
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
@@ -456,6 +573,7 @@ def run_gpu(args):
             "fp64": {"ms_per_step": ms64, "pairs_per_step": statistics.mean(pairs64), "relres": max(rel64),
                      "value": N * statistics.mean(pairs64) / (ms64 * 1e-3)},
             "speedup_fp32_refined_vs_fp64": ms64 / ms32,
+            "err_vs_fp64": err["err_vs_fp64"], "error": err,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": Ph.h2d_bytes(),
@@ -564,6 +682,30 @@ def run_lusgs(args):
             torch.cuda.synchronize()
             res["sweep_ms"] = e0.elapsed_time(e1) / 10
         del S
+    # error of the FP32 loop against the FP64 arithmetic of the oracle
+    # (UCFD_PREC_FP64): args.iters iterations of each from the same state
+    finals = {}
+    for prec in (2, 0):
+        S = FlowSys(N, 6, 5, 3, c["nfaces"], 1, g["rowptr"], g["colidx"], g["slots"], g["sides"], g["face_area"],
+                    g["face_normal"], g["rcp_vol"])
+        S.set_coloring(lc)
+        S.set_precision(prec)
+        S.set_stream(stream.cuda_stream, True)
+        uu = up.clone()
+        S.set_element(0, N, 6, g["cell_ids"], uu, g["rhs"], g["dt"], torch.zeros_like(uu), g["vol"],
+                      torch.zeros_like(uu))
+        S.set_lusgs(g["fspr"], g["tfspr"])
+        if prec == 2 and res.get("launch"):
+            S.set_launch_config(**res["launch"])
+        S.lusgs_pack(0, 1.0, 0.0)
+        S.lusgs_run(args.iters, 1.0, True, 0, None)
+        torch.cuda.synchronize()
+        finals[prec] = uu
+        del S
+    change = float((finals[0] - up).abs().max())
+    err_lusgs = float((finals[2] - finals[0]).abs().max()) / change
+    del finals
+    torch.cuda.empty_cache()
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     peak = float(peaks.get("hbm_gbs", 6800.0))
@@ -592,6 +734,9 @@ def run_lusgs(args):
                         "sweep_ms": res["sweep_ms"], "algorithmic_bytes_per_sweep": sweep_bytes_},
            "loop_frac_of_peak": bytes_iter * args.iters / (best * 1e-3) / 1e9 / peak,
            "resid_fp64": [res[0]["resid_first"], res[0]["resid_last"]],
+           "err_vs_fp64": err_lusgs,
+           "err_definition": f"max|U_fp32 - U_fp64| / max|U_fp64 - U_0| after {args.iters} iterations of the graph "
+                             f"loop from the same state, U_fp64 from UCFD_PREC_FP64 (the oracle's arithmetic)",
            "clocks": res[0]["clocks"], "generation_s": gen_s, "launch": res.get("launch")}
     if args.cpu_iters > 0:
         del g, up
@@ -642,6 +787,7 @@ def run_gmres(args):
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     peak = float(peaks.get("hbm_gbs", 6800.0))
     res = {}
+    xs = {}
     for prec in (1, 2):
         pc = Precon(d["rowptr"], d["colidx"], d["diagslots"], d["values"])
         pc.set_pblusgs(bn, 5, len(rg), icolors, cuda=True)
@@ -667,6 +813,7 @@ def run_gmres(args):
         st, it, r = sv.result()
         res[prec] = dict(s=el, stat=st, restarts=it, resid=r / (tol / 1e-10), arnoldi=sv.arnoldi_steps(),
                          prepare_ms=reprep_ms)
+        xs[prec] = x.clone()
         # preconditioner apply alone
         w = torch.randn(n, dtype=torch.float64, device=dev)
         torch.cuda.synchronize()
@@ -682,6 +829,21 @@ def run_gmres(args):
         res[prec]["precon_GBps"] = pb / (res[prec]["precon_ms"] * 1e-3) / 1e9
         res[prec]["precon_frac"] = res[prec]["precon_GBps"] / peak
         del pc, sv
+    # the solution of the FP64 arithmetic of the oracle (UCFD_PREC_FP64: the
+    # reference's operation order in the matvec and preconditioner), untimed
+    pc = Precon(d["rowptr"], d["colidx"], d["diagslots"], d["values"])
+    pc.set_pblusgs(bn, 5, len(rg), icolors, cuda=True)
+    pc.set_precision(0)
+    pc.prepare()
+    sv = Solver(n, 30, 100, tol, cuda=True)
+    sv.set_precision(0)
+    x0 = torch.zeros(n, dtype=torch.float64, device=dev)
+    sv.solve(pc, A, x0, d["rhs"])
+    x0max = float(x0.abs().max())
+    for prec in (1, 2):
+        res[prec]["err_vs_fp64"] = float((xs[prec] - x0).abs().max()) / x0max
+    del pc, sv, x0, xs
+    torch.cuda.empty_cache()
     # BiCGSTAB (FP64) with the coloured BLU-SGS and the coloured block ILU(0)
     bic = {}
     for pc_kind in ("pblusgs", "pbilu"):
@@ -738,6 +900,9 @@ def run_gmres(args):
            "config": {"workload": f"GMRES(30) + coloured BLU-SGS, Kuhn tets of a {args.mesh}^3 box ({bn} cells, "
                                   f"5x5 BSR, {nnzb} blocks), {len(rg)} colours, tol 1e-10 relative", "cells": bn},
            "fp64": res[1], "mixed": res[2], "speedup_mixed_vs_fp64": res[1]["s"] / res[2]["s"],
+           "err_vs_fp64": res[2]["err_vs_fp64"],
+           "err_definition": "max|x - x_fp64| / max|x_fp64|, x_fp64 the GMRES solution with UCFD_PREC_FP64 "
+                             "(the oracle's arithmetic) to the same tolerance",
            "spmv": {"fp64_ms": sp[False], "fp32_ms": sp[True],
                     "fp64_GBps": b64 / (sp[False] * 1e-3) / 1e9, "fp32_GBps": b32 / (sp[True] * 1e-3) / 1e9,
                     "peak": peak, "fp64_frac": b64 / (sp[False] * 1e-3) / 1e9 / peak,

@@ -154,16 +154,18 @@ UCFD_EXTERN ucfd_status_t UCFDBLUSGS_Residual(FlowSys sys, UCFDReal *relres);
 
 /* The same residual, computed without allocating anything (no counterpart
  * in the reference).  For callers that may not call cudaMalloc while they
- * run -- a pseudo-time loop driven from inside a CUDA stream capture, or a
- * code that gives its whole device memory to its own pool at start-up --
- * yet monitor the residual every iteration.  The reduction partials live
- * in a fixed 64 KiB device array inside the library (held by every GPU
- * that loads it until exit); systems above 8,388,608 cells are rejected
- * with UCFD_ERR_ARGUMENT.  The system must already be packed and prepared
- * (UCFD_ERR_STATE otherwise).  relres may be host or device memory.  The
- * first call on a device looks up the array's address: make it before any
- * stream capture.  All calls share the array, so calls whose kernels
- * overlap on the GPU (unordered streams) race. */
+ * run -- a code that gives its whole device memory to its own pool at
+ * start-up, or whose time-step loop must not stall on an allocation -- yet
+ * monitor the residual every iteration.  The reduction partials live in a
+ * fixed 64 KiB device array inside the library (held by every GPU that
+ * loads it until exit); systems above 8,388,608 cells are rejected with
+ * UCFD_ERR_ARGUMENT.  The system must already be packed and prepared
+ * (UCFD_ERR_STATE otherwise).  relres may be host or device memory; the
+ * call returns once it is written.  It runs on the device holding the
+ * handle's arrays and restores the caller's current device.  The first
+ * call on a device looks up the array's address: make it before any stream
+ * capture.  All calls share the array, so calls whose kernels overlap on
+ * the GPU (unordered streams) race. */
 UCFD_EXTERN ucfd_status_t UCFDBLUSGS_ResidualNoAlloc(FlowSys sys, UCFDReal *relres);
 
 #if defined(__cplusplus)

@@ -25,7 +25,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF = os.path.join(HERE, "_ref")
-REF_SRC = os.environ.get("UCFD_REFERENCE_SRC", "/root/reference")
+# root of a UCFD_SPARSE source tree; the reference libraries are built only
+# where this names one
+REF_SRC = os.environ.get("UCFD_REFERENCE_SRC")
 
 _I, _D, _P = c_int, c_double, c_void_p
 
@@ -35,11 +37,16 @@ def build_port() -> None:
 
 
 def build_ref() -> bool:
-    """Compile the reference sources into oracle/_ref (False if absent)."""
-    if not os.path.isdir(os.path.join(REF_SRC, "src", "lusgs")):
+    """Compile the reference sources into oracle/_ref (False if
+    UCFD_REFERENCE_SRC does not name a source tree)."""
+    if not ref_src_present():
         return False
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"], check=True)
     return True
+
+
+def ref_src_present() -> bool:
+    return bool(REF_SRC) and os.path.isdir(os.path.join(REF_SRC, "src", "lusgs"))
 
 
 def ref_available() -> bool:
@@ -102,12 +109,28 @@ class Port:
             "oracle_ilu_apply": (None, [_I, _P, _P, _P, _P, _P]),
             "oracle_bicgstab": (_I, [_I, _I, _P, _P, _P, _I, _I, _P, _P, _P, _P, _I, _D, _P, _P,
                                      POINTER(c_int), POINTER(c_double), _P]),
+            "oracle_greedy_coloring_csr": (_I, [_I, _P, _P, _P]),
         }
         for n, (r, a) in sig.items():
             f = getattr(L, n)
             f.restype = r
             f.argtypes = a
         self.L = L
+
+    # ---- colouring --------------------------------------------------------
+    def greedy_coloring_csr(self, rowptr, colidx):
+        """Greedy first-fit colouring in index order -> (icolor, ranges,
+        lcolor): cells grouped by colour in ascending index, the end of each
+        colour's range, 1-based colour of each cell."""
+        rp, ci = _i32(rowptr), _i32(colidx)
+        n = rp.shape[0] - 1
+        col = np.empty(n, dtype=np.int32)
+        nc = self.L.oracle_greedy_coloring_csr(n, P(rp), P(ci), P(col))
+        if nc < 0:
+            raise MemoryError("oracle_greedy_coloring_csr: allocation failed")
+        icolor = np.argsort(col, kind="stable").astype(np.int32)
+        ranges = [int(x) for x in np.cumsum(np.bincount(col, minlength=nc))]
+        return icolor, ranges, col + 1
 
     # ---- colored array API ------------------------------------------------
     def legacy_step(self, c: dict, icolor, ranges, lcolor, nsteps: int = 1, rans: bool = False,
@@ -206,6 +229,11 @@ class Port:
             self.L.oracle_blusgs_sub_residual(N, neles, nv, P(ids), P(vol), P(du), P(dup), P(res))
         self.L.oracle_blusgs_update(N, neles, nv, P(ids), P(du), P(upts))
         return upts, du.reshape(N, nv), res.reshape(nv, neles), diag.reshape(N, nfv, nfv)
+
+    def blusgs_phases(self, fs: dict, rhs, dt, jmat, vol, upts, a0=0.0):
+        """The steps of flowsys_blusgs as separate calls (for timing them one
+        by one): see BlusgsPhases."""
+        return _PortBlusgsPhases(self, fs, rhs, dt, jmat, vol, upts, a0)
 
     # ---- Krylov -------------------------------------------------------------
     def bsr_spmv(self, s: dict, x, alpha=1.0, beta=0.0, y=None):
@@ -410,6 +438,11 @@ class Ref:
         self.lus.UCFDFlowSysDestroy(byref(h))
         return upts, res
 
+    def blusgs_phases(self, fs, rhs, dt, jmat, vol, upts, a0=0.0):
+        """The reference's own FlowSys BLU-SGS calls one by one: see
+        BlusgsPhases."""
+        return _RefBlusgsPhases(self, fs, rhs, dt, jmat, vol, upts, a0)
+
     def bsr_spmv(self, s, x, alpha=1.0, beta=0.0, y=None):
         h = c_void_p()
         rp, ci, v = _i32(s["rowptr"]), _i32(s["colidx"]), _f64(s["values"])
@@ -503,6 +536,108 @@ class Ref:
         self.kry.UCFDPreconDestroy(byref(pc_h))
         self.kry.UCFDMatDestroy(byref(A))
         return x, st.value, it.value, res.value, hist
+
+
+# ---------------------------------------------------------------------------
+# one BLU-SGS pseudo-time step, call by call
+# ---------------------------------------------------------------------------
+class BlusgsPhases:
+    """One FlowSys BLU-SGS step split into its calls, as a CFD code makes
+    them (blusgs.c:17-57 pack, 200-270 prepare, 431-440 reset, 273-373
+    sweeps, 161-197 sub-residual, 126-155 update): ``pack_prepare()``,
+    ``reset()``, then ``lower()`` / ``upper()`` / ``sub_residual()`` per
+    sweep pair, then ``update()``.  ``upts`` is updated in a copy
+    (``self.upts``); ``self.res`` holds the last sub-residual."""
+
+    def close(self):
+        pass
+
+
+class _PortBlusgsPhases(BlusgsPhases):
+    def __init__(self, port, fs, rhs, dt, jmat, vol, upts, a0):
+        L = port.L
+        self.L = L
+        N, nv, nfv, nF = fs["nlocal"], fs["nvars"], fs["nfvars"], fs["nfaces"]
+        self.N, self.nv, self.nfv, self.nF, self.a0 = N, nv, nfv, nF, a0
+        self.neles = dt.shape[0]
+        self.ids = _i32(fs["cell_ids"])
+        self.rp, self.ci, self.sl = _i32(fs["rowptr"]), _i32(fs["colidx"]), _i32(fs["slots"])
+        self.sd = np.ascontiguousarray(fs["sides"], dtype=np.int8)
+        self.fa, self.rv = _f64(fs["face_area"]), _f64(fs["rcp_vol"])
+        self.rhs, self.dt, self.jmat, self.vol = _f64(rhs), _f64(dt), _f64(jmat), _f64(vol)
+        self.upts = _f64(upts).copy()
+        self.rrhs = np.zeros(N * nv)
+        self.diag = np.zeros(N * nfv * nfv)
+        self.du = np.zeros(N * nv)
+        self.dup = np.zeros(N * nv)
+        self.res = np.zeros((nv, self.neles))
+
+    def pack_prepare(self):
+        L = self.L
+        L.oracle_blusgs_pack(self.N, self.neles, self.nv, self.nfv, self.a0, P(self.ids), P(self.rhs), P(self.dt),
+                             P(self.rrhs), P(self.diag))
+        L.oracle_blusgs_prepare(self.N, self.nfv, self.nF, P(self.rp), P(self.sl), P(self.sd), P(self.fa),
+                                P(self.rv), P(self.diag), P(self.jmat))
+
+    def reset(self):
+        self.du[:] = 0.0
+        self.dup[:] = 0.0
+
+    def _g(self):
+        return (P(self.rp), P(self.ci), P(self.sd), P(self.sl), P(self.fa), P(self.rv), P(self.rrhs), P(self.diag),
+                P(self.jmat), P(self.du))
+
+    def lower(self):
+        self.L.oracle_blusgs_lower(0, self.nfv, self.N, self.nv, self.nF, *self._g())
+
+    def upper(self):
+        self.L.oracle_blusgs_upper(0, self.nfv, self.N, self.nv, self.nF, *self._g())
+
+    def sub_residual(self):
+        self.L.oracle_blusgs_sub_residual(self.N, self.neles, self.nv, P(self.ids), P(self.vol), P(self.du),
+                                          P(self.dup), P(self.res))
+
+    def update(self):
+        self.L.oracle_blusgs_update(self.N, self.neles, self.nv, P(self.ids), P(self.du), P(self.upts))
+
+
+class _RefBlusgsPhases(BlusgsPhases):
+    def __init__(self, ref, fs, rhs, dt, jmat, vol, upts, a0):
+        self.lus = ref.lus
+        self.h, self.keep = ref._sys(fs)
+        self.a0 = a0
+        self.upts = _f64(upts).copy()
+        self.rhs, self.dt, self.jmat, self.vol = _f64(rhs), _f64(dt), _f64(jmat), _f64(vol)
+        self.ids = _i32(fs["cell_ids"])
+        self.res = np.zeros_like(self.upts)
+        self.dsrc = np.zeros_like(self.upts)
+        self.lus.UCFDFlowSysSetBLUSGS(byref(self.h), P(self.jmat), None)
+        self.lus.UCFDFlowSysSetElement(byref(self.h), 0, self.dt.shape[0], 6, P(self.ids), P(self.upts),
+                                       P(self.rhs), P(self.dt), P(self.dsrc), P(self.vol), P(self.res))
+
+    def pack_prepare(self):
+        self.lus.UCFDBLUSGS_Pack(self.h, 0, self.a0)
+        self.lus.UCFDBLUSGS_NSPrepare(self.h)
+
+    def reset(self):
+        self.lus.UCFDBLUSGS_Reset(self.h)
+
+    def lower(self):
+        self.lus.UCFDBLUSGS_NSLowerSweep(self.h)
+
+    def upper(self):
+        self.lus.UCFDBLUSGS_NSUpperSweep(self.h)
+
+    def sub_residual(self):
+        self.lus.UCFDBLUSGS_SubResidual(self.h, 0)
+
+    def update(self):
+        self.lus.UCFDBLUSGS_Update(self.h, 0)
+
+    def close(self):
+        if self.h:
+            self.lus.UCFDFlowSysDestroy(byref(self.h))
+            self.h = c_void_p()
 
 
 # ---------------------------------------------------------------------------

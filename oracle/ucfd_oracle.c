@@ -1053,3 +1053,71 @@ done:
     free(r); free(rt); free(p); free(pt); free(v); free(s); free(sh); free(t);
     return stat;
 }
+
+/* ========================================================================
+ * Greedy first-fit colouring of a CSR graph, cells visited in index order.
+ * The reference has no general colouring (its examples use the checkerboard
+ * of examples/utils/pbutils.py:39-56); this is the colouring the GB300
+ * library defines for jittered / permuted meshes, restated here so that the
+ * CPU legs can colour a mesh without the product library.  A cell takes the
+ * smallest colour that no already coloured neighbour holds, an edge counting
+ * in both directions (the graph is used as if symmetric; negative and
+ * self entries are ignored).  color[] gets
+ * 0-based colours; returns the number of colours (-1 on allocation failure).
+ * ====================================================================== */
+int oracle_greedy_coloring_csr(oint n, const oint *rowptr, const oint *colidx, oint *color)
+{
+    const oint nnz = rowptr[n];
+    oint *trp = (oint *)calloc((size_t)n + 1, sizeof(oint));
+    oint *tci = (oint *)malloc(sizeof(oint) * (size_t)(nnz > 0 ? nnz : 1));
+    oint maxdeg = 0;
+    if (!trp || !tci) {
+        free(trp); free(tci);
+        return -1;
+    }
+    /* transpose: the cells that list i as a neighbour */
+    for (oint i = 0; i < n; ++i)
+        for (oint p = rowptr[i]; p < rowptr[i + 1]; ++p)
+            if (colidx[p] >= 0 && colidx[p] != i) trp[colidx[p] + 1]++;
+    for (oint i = 0; i < n; ++i) trp[i + 1] += trp[i];
+    {
+        oint *fill = (oint *)malloc(sizeof(oint) * (size_t)(n > 0 ? n : 1));
+        if (!fill) {
+            free(trp); free(tci);
+            return -1;
+        }
+        memcpy(fill, trp, sizeof(oint) * (size_t)n);
+        for (oint i = 0; i < n; ++i)
+            for (oint p = rowptr[i]; p < rowptr[i + 1]; ++p)
+                if (colidx[p] >= 0 && colidx[p] != i) tci[fill[colidx[p]]++] = i;
+        free(fill);
+    }
+    for (oint i = 0; i < n; ++i) {
+        oint d = (rowptr[i + 1] - rowptr[i]) + (trp[i + 1] - trp[i]);
+        if (d > maxdeg) maxdeg = d;
+    }
+    oint *mark = (oint *)malloc(sizeof(oint) * (size_t)(maxdeg + 2));
+    if (!mark) {
+        free(trp); free(tci);
+        return -1;
+    }
+    for (oint c = 0; c < maxdeg + 2; ++c) mark[c] = -1;
+    oint nc = 0;
+    for (oint i = 0; i < n; ++i) color[i] = -1;
+    for (oint i = 0; i < n; ++i) {
+        for (oint p = rowptr[i]; p < rowptr[i + 1]; ++p) {
+            const oint j = colidx[p];
+            if (j >= 0 && j != i && color[j] >= 0) mark[color[j]] = i;
+        }
+        for (oint p = trp[i]; p < trp[i + 1]; ++p) {
+            const oint j = tci[p];
+            if (color[j] >= 0) mark[color[j]] = i;
+        }
+        oint c = 0;
+        while (mark[c] == i) ++c;
+        color[i] = c;
+        if (c + 1 > nc) nc = c + 1;
+    }
+    free(mark); free(trp); free(tci);
+    return nc;
+}

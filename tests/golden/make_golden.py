@@ -1,7 +1,8 @@
 """Generate the golden vectors of tests/golden/ from the reference itself.
 
-Run here, where the reference source tree exists:
-    python tests/golden/make_golden.py [reference_root]
+Run where a UCFD_SPARSE source tree exists:
+    python tests/golden/make_golden.py <reference_root>
+(or with UCFD_REFERENCE_SRC set to that root)
 
 * box connectivity and the checkerboard come from importing the reference
   example module examples/utils/pbutils.py;
@@ -116,4 +117,8 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("UCFD_REFERENCE_SRC")
+    if not root:
+        sys.exit("usage: python tests/golden/make_golden.py <root of the UCFD_SPARSE source tree> "
+                 "(or set UCFD_REFERENCE_SRC)")
+    main(root)

@@ -167,3 +167,25 @@ def test_bsr_case_is_diagonally_dominant():
     np.add.at(absrow, rows, np.abs(v).sum(axis=2))
     d = np.abs(v[s["diagslots"]][:, np.arange(blk), np.arange(blk)])
     assert np.all(d > absrow - d)
+
+
+def test_oracle_colouring_equals_native(ucfd, port):
+    """The oracle's greedy colouring (used by the CPU legs, which must not
+    load the product library) equals UCFDGreedyColoringCSR: on a permuted
+    hex mesh, and on a random graph with one-directional edges, self entries
+    and negative (boundary) entries."""
+    from ucfd_sparse_gb300 import coloredlusgs as cl
+    from ucfd_sparse_gb300 import meshgen as mg
+    b = mg.blusgs_case(8, seed=2)
+    rng = np.random.default_rng(7)
+    n = 3000
+    deg = rng.integers(0, 7, n)
+    rp = np.concatenate([[0], np.cumsum(deg)]).astype(np.int32)
+    ci = rng.integers(-1, n, int(rp[-1])).astype(np.int32)
+    ci[::17] = np.repeat(np.arange(n), deg)[::17]          # some self entries
+    for rowptr, colidx in ((b["rowptr"], b["colidx"]), (rp, ci)):
+        ic, rg, lc = cl.greedy_coloring_csr(rowptr, colidx)
+        ic2, rg2, lc2 = port.greedy_coloring_csr(rowptr, colidx)
+        np.testing.assert_array_equal(ic, ic2)
+        np.testing.assert_array_equal(lc, lc2)
+        assert rg == rg2

@@ -1,0 +1,23 @@
+"""The benchmark's reference arm (CPU): it runs the reference's CPU path
+alone -- no library of this repository's product is loaded -- and reports
+the GPU arm's metric, unit and workload description."""
+import json
+import os
+import subprocess
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_reference_arm_loads_no_product_library():
+    r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--mesh", "8",
+                        "--steps", "3", "--warmup", "3"], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stderr
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "cell-updates/s" and line["higher_is_better"]
+    assert line["config"]["cells"] == 512 and line["config"]["colors"] >= 2
+    libs = line["libraries_loaded"]
+    assert libs is not None and not any("libucfd_gb300" in p for p in libs), libs
+    assert any(p.startswith("oracle/") for p in libs), libs
+    assert line["cpu_baseline"]["kind"] in ("reference", "port") and line["cpu_baseline"]["cores"] == 1
+    assert line["value"] > 0 and line["e2e"]["value"] == line["value"]

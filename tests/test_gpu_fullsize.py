@@ -1,7 +1,24 @@
-"""Size-independent properties at the full workload sizes (GPU).
+"""The full workload sizes (GPU): parity with the oracle and
+size-independent properties.
 
-The oracle finishes only small cases; at full size the checks are
-properties that hold whatever the size:
+Parity: the CUDA path in its FP64 mode (UCFD_PREC_FP64, the reference's
+operation order) against the oracle's CPU restatement on the same seeded
+inputs, bit for bit, on the benchmark meshes:
+
+* C2  128^3 jittered, permuted hex (2,097,152 cells), BLU-SGS 5x5: Pack,
+  NSPrepare, Reset, one lower + upper sweep pair, SubResidual, Update in
+  greedy colour order, against the reference call sequence on the colour-
+  renumbered mesh (blusgs.c:17-57, 126-155, 161-197, 200-270, 273-373);
+* C3  Kuhn tets of a 96^3 box (5,308,416 cells), BSR 5x5: one matvec
+  (sparsemat.c:57-101) and one coloured BLU-SGS preconditioner apply
+  (precon/blusgs.c:7-100 on the colour-ordered matrix);
+* C5  256^3 jittered, permuted hex (16,777,216 cells), scalar LU-SGS NS +
+  1-equation RANS: one pseudo-time iteration (lusgs.c:8-321) in colour
+  order; the FP32 path's error against it is bounded as well.
+The oracle's sweeps are serial, as the reference's: about a minute of CPU for
+C5 and half a minute for C2.
+
+Properties that hold whatever the size:
 
 * C2  128^3 hex (2,097,152 cells), BLU-SGS: FP32 sweeps + FP64 refinement
   and plain FP64 sweeps both reach a 1e-10 relative residual, confirmed by
@@ -23,9 +40,58 @@ pytestmark = pytest.mark.gpu
 
 DEV = torch.device("cuda", 0)
 
+# FP32 sweeps against the FP64 arithmetic, one C5 iteration:
+# max|dU_fp32 - dU_fp64| <= C5_FP32_BOUND * max|dU_fp64|
+C5_FP32_BOUND = 1e-3
+
 
 def T(a):
     return torch.from_numpy(np.ascontiguousarray(a)).to(DEV)
+
+
+def renumber_by_colour(case):
+    """Greedy colouring of a FlowSys mesh and the mesh renumbered colour by
+    colour (on which the oracle's natural-order sweeps are the coloured
+    sweeps) -> (renumbered case, lcolor, colour range ends)."""
+    from ucfd_sparse_gb300 import coloredlusgs as cl
+    from ucfd_sparse_gb300 import meshgen as mg
+    ic, rg, lc = cl.greedy_coloring_csr(case["rowptr"], case["colidx"])
+    new = np.empty(case["nlocal"], dtype=np.int64)
+    new[ic] = np.arange(case["nlocal"])
+    return mg.renumber_flowsys(case, new), lc, rg
+
+
+# the meshes take a minute each to generate: once per module
+@pytest.fixture(scope="module")
+def c2():
+    from ucfd_sparse_gb300 import meshgen as mg
+    case = mg.blusgs_case(128, seed=0)
+    assert case["nlocal"] == 2097152
+    br, lc, rg = renumber_by_colour(case)
+    return case, br, lc, rg
+
+
+@pytest.fixture(scope="module")
+def c3():
+    """The C3 system renumbered colour by colour and its colour offsets."""
+    from ucfd_sparse_gb300 import coloredlusgs as cl
+    from ucfd_sparse_gb300 import meshgen as mg
+    s0 = mg.bsr_case(96, seed=0)
+    assert s0["bn"] == 5308416
+    tab = np.where(s0["nei"] >= 0, s0["nei"], np.arange(s0["bn"])[None, :]).astype(np.int32)
+    ic, rg, lc = cl.greedy_coloring(tab)
+    new = np.empty(s0["bn"], dtype=np.int64)
+    new[ic] = np.arange(s0["bn"])
+    return mg.renumber_bsr(s0, new), rg
+
+
+@pytest.fixture(scope="module")
+def c5():
+    from ucfd_sparse_gb300 import meshgen as mg
+    c = mg.lusgs_flowsys_case(256, nvars=6, seed=0, rhs_scale=1e-3)
+    assert c["nlocal"] == 16777216
+    br, lc, rg = renumber_by_colour(c)
+    return c, br, lc, rg
 
 
 def blusgs_system(case, lc, prec):
@@ -56,12 +122,8 @@ def noalloc_relres(S):
     return r.value
 
 
-def test_c2_blusgs_full_size(ucfd):
-    from ucfd_sparse_gb300 import coloredlusgs as cl
-    from ucfd_sparse_gb300 import meshgen as mg
-    case = mg.blusgs_case(128, seed=0)
-    assert case["nlocal"] == 2097152
-    ic, rg, lc = cl.greedy_coloring_csr(case["rowptr"], case["colidx"])
+def test_c2_blusgs_full_size(c2, ucfd):
+    case, _, lc, _ = c2
     sols = {}
     for prec in (2, 1):
         S, e = blusgs_system(case, lc, prec)
@@ -96,18 +158,9 @@ def test_c2_sweep_variants_full_size(ucfd):
         np.testing.assert_array_equal(o, outs[0])
 
 
-def test_c3_gmres_full_size(ucfd):
-    from ucfd_sparse_gb300 import coloredlusgs as cl
-    from ucfd_sparse_gb300 import meshgen as mg
+def test_c3_gmres_full_size(c3, ucfd):
     from ucfd_sparse_gb300.krylov import Precon, Solver, SpMat
-    s0 = mg.bsr_case(96, seed=0)
-    assert s0["bn"] == 5308416
-    tab = np.where(s0["nei"] >= 0, s0["nei"], np.arange(s0["bn"])[None, :]).astype(np.int32)
-    ic, rg, lc = cl.greedy_coloring(tab)
-    new = np.empty(s0["bn"], dtype=np.int64)
-    new[ic] = np.arange(s0["bn"])
-    s = mg.renumber_bsr(s0, new)
-    del s0
+    s, rg = c3
     bn = s["bn"]
     n = bn * 5
     d = {k: T(s[k]) for k in ("rowptr", "colidx", "values", "diagslots", "rhs")}
@@ -158,14 +211,10 @@ def test_c4_adjoint_full_size(ucfd):
     assert abs(adj - fd) <= 1e-6 * max(abs(fd), 1e-30), (adj, fd)
 
 
-def test_c5_lusgs_loop_full_size(ucfd):
-    from ucfd_sparse_gb300 import coloredlusgs as cl
-    from ucfd_sparse_gb300 import meshgen as mg
+def test_c5_lusgs_loop_full_size(c5, ucfd):
     from ucfd_sparse_gb300.flowsys import FlowSys
-    c = mg.lusgs_flowsys_case(256, nvars=6, seed=0, rhs_scale=1e-3)
+    c, _, lc, _ = c5
     N = c["nlocal"]
-    assert N == 16777216
-    ic, rg, lc = cl.greedy_coloring_csr(c["rowptr"], c["colidx"])
     g = {k: T(c[k]) for k in ("rowptr", "colidx", "slots", "sides", "face_area", "face_normal", "rcp_vol", "fspr",
                               "tfspr", "dt", "rhs", "cell_ids", "vol")}
     out = {}
@@ -188,3 +237,105 @@ def test_c5_lusgs_loop_full_size(ucfd):
     np.testing.assert_array_equal(out[0][0], out[1][0])
     np.testing.assert_array_equal(out[0][1], out[1][1])
     assert np.all(np.isfinite(out[0][1])) and out[0][1][0] > 0
+
+
+# ---------------------------------------------------------------------------
+# parity with the oracle at full size
+# ---------------------------------------------------------------------------
+def flowsys(case, nvars, lc, prec):
+    from ucfd_sparse_gb300.flowsys import FlowSys
+    m = {k: T(case[k]) for k in ("rowptr", "colidx", "slots", "sides", "face_area", "face_normal", "rcp_vol")}
+    S = FlowSys(case["nlocal"], nvars, 5, 3, case["nfaces"], 1, m["rowptr"], m["colidx"], m["slots"], m["sides"],
+                m["face_area"], m["face_normal"], m["rcp_vol"])
+    S.set_coloring(lc)
+    S.set_precision(prec)
+    return S
+
+
+def test_c2_blusgs_fp64_bitexact_full_size(c2, port, ucfd):
+    case, br, lc, rg = c2
+    assert len(rg) == 7
+    S = flowsys(case, 5, lc, 0)
+    e = {k: T(case[k]) for k in ("rhs", "dt", "cell_ids", "vol", "jmat")}
+    e["upts"] = T(np.array(case["upts"]))
+    e["res"] = torch.zeros_like(e["rhs"])
+    S.set_element(0, case["neles"], 6, e["cell_ids"], e["upts"], e["rhs"], e["dt"], torch.zeros_like(e["rhs"]),
+                  e["vol"], e["res"])
+    S.set_blusgs(e["jmat"])
+    S.blusgs_pack(0, 0.0)
+    S.blusgs_ns_prepare()
+    S.blusgs_reset()
+    S.blusgs_ns_lower()
+    S.blusgs_ns_upper()
+    S.blusgs_sub_residual(0)
+    S.blusgs_update(0)
+    got_up, got_res = e["upts"].cpu().numpy(), e["res"].cpu().numpy()
+    S.destroy()
+    del S, e
+    torch.cuda.empty_cache()
+    up, _, res, _ = port.flowsys_blusgs(br, case["rhs"], case["dt"], case["jmat"], case["vol"], case["upts"],
+                                        nsweeps=1)
+    np.testing.assert_array_equal(got_up, up)
+    np.testing.assert_array_equal(got_res, res)
+    assert np.abs(up - case["upts"]).max() > 0
+
+
+def test_c3_spmv_and_coloured_blusgs_fp64_bitexact_full_size(c3, port, ucfd):
+    from ucfd_sparse_gb300.krylov import Precon, SpMat
+    s, rg = c3
+    bn = s["bn"]
+    icolors = np.array([0] + rg, dtype=np.int32)
+    rng = np.random.default_rng(21)
+    x = rng.standard_normal(bn * 5)
+    b = rng.standard_normal(bn * 5)
+    d = {k: T(s[k]) for k in ("rowptr", "colidx", "values", "diagslots")}
+    A = SpMat(bn, 5, d["rowptr"], d["colidx"], d["values"], cuda=True)
+    y = torch.zeros(bn * 5, dtype=torch.float64, device=DEV)
+    A.mult(1.0, T(x), 0.0, y)
+    got_y = y.cpu().numpy()
+    pc = Precon(d["rowptr"], d["colidx"], d["diagslots"], d["values"])
+    pc.set_pblusgs(bn, 5, len(rg), icolors, cuda=True)
+    pc.set_precision(0)
+    pc.prepare()
+    xb = T(b)
+    pc.apply(xb)
+    got_pc = xb.cpu().numpy()
+    del A, pc, d, y, xb
+    torch.cuda.empty_cache()
+    np.testing.assert_array_equal(got_y, port.bsr_spmv(s, x))
+    np.testing.assert_array_equal(got_pc, port.precon_apply(s, b, icolors=icolors))
+
+
+def test_c5_lusgs_iteration_full_size(c5, port, ucfd):
+    """One NS + RANS iteration, FP64 bit for bit; FP32 within C5_FP32_BOUND."""
+    c, br, lc, rg = c5
+    N = c["nlocal"]
+    g = {k: T(c[k]) for k in ("fspr", "tfspr", "dt", "rhs", "cell_ids", "vol")}
+    got = {}
+    for prec in (0, 2):
+        S = flowsys(c, 6, lc, prec)
+        up = T(c["upts"])
+        S.set_element(0, N, 6, g["cell_ids"], up, g["rhs"], g["dt"], torch.zeros_like(up), g["vol"],
+                      torch.zeros_like(up))
+        S.set_lusgs(g["fspr"], g["tfspr"])
+        S.lusgs_pack(0, 1.0, 0.0)
+        S.lusgs_ns_prepare(1.0)
+        S.lusgs_ns_lower(1.0)
+        S.lusgs_ns_upper(1.0)
+        S.lusgs_rans_prepare(1.0)
+        S.lusgs_rans_lower(1.0)
+        S.lusgs_rans_upper(1.0)
+        S.lusgs_update(0)
+        got[prec] = up.cpu().numpy()
+        S.destroy()
+        del S, up
+        torch.cuda.empty_cache()
+    del g
+    torch.cuda.empty_cache()
+    ref = port.flowsys_lusgs_step(br, c["upts"], c["rhs"], c["dt"], np.zeros_like(c["rhs"]), c["fspr"],
+                                  c["tfspr"], rans=True, nsteps=1)[0]
+    np.testing.assert_array_equal(got[0], ref)
+    d64 = ref - c["upts"]
+    err = np.abs((got[2] - c["upts"]) - d64).max() / np.abs(d64).max()
+    print(f"C5 FP32 iteration: max|dU32 - dU64| / max|dU64| = {err:.3e}")
+    assert err <= C5_FP32_BOUND, err

@@ -103,6 +103,27 @@ def test_pblusgs_equals_natural_on_colour_ordered_matrix(port):
     np.testing.assert_array_equal(a, c)
 
 
+def test_blusgs_phases_equal_whole_step(port):
+    """The call-by-call BLU-SGS driver the CPU timing legs use performs the
+    same step as flowsys_blusgs (and, where the reference was compiled here,
+    as the reference's own calls)."""
+    b = cases.blusgs_case(m=6, seed=4)
+    whole = port.flowsys_blusgs(b, b["rhs"], b["dt"], b["jmat"], b["vol"], b["upts"], nsweeps=3)
+    impls = [port] + ([orc.Ref()] if orc.ref_available() else [])
+    for impl in impls:
+        ph = impl.blusgs_phases(b, b["rhs"], b["dt"], b["jmat"], b["vol"], b["upts"])
+        ph.pack_prepare()
+        ph.reset()
+        for _ in range(3):
+            ph.lower()
+            ph.upper()
+            ph.sub_residual()
+        ph.update()
+        np.testing.assert_array_equal(ph.upts, whole[0])
+        np.testing.assert_array_equal(ph.res, whole[2])
+        ph.close()
+
+
 @pytest.mark.skipif(not orc.ref_available(), reason="reference source tree not present on this machine")
 def test_port_vs_compiled_reference_extra(port):
     ref = orc.Ref()

@@ -1,8 +1,8 @@
 """The allocation-free residual entry point (UCFDBLUSGS_ResidualNoAlloc).
 
-Callers that cannot allocate device memory while they run -- a pseudo-time
-loop driven from inside a CUDA stream capture, or a code whose memory is all
-handed to its own pool at start-up -- use this variant to monitor the block
+Callers that cannot allocate device memory while they run -- a code whose
+device memory is all handed to its own pool at start-up, or whose time-step
+loop must not stall on cudaMalloc -- use this variant to monitor the block
 LU-SGS residual.  It must agree with UCFDBLUSGS_Residual (same per-cell
 arithmetic, different summation order across cells) on consecutive calls,
 since every call reuses the same fixed device scratch array.  This file is
@@ -78,3 +78,46 @@ def test_noalloc_residual_requires_prepared_system(ucfd):
     with pytest.raises(lib.UCFDError) as ex:
         _noalloc(S, h)
     assert ex.value.status == 8 and "prepared" in str(ex.value)
+
+
+def test_noalloc_residual_rejects_systems_above_its_limit(ucfd):
+    """8,388,610 cells, two more than the fixed scratch array covers: cells
+    2k and 2k+1 share face k, so the system is small in memory (about 8 GB on
+    the device) yet valid; the allocation-free call refuses it with
+    UCFD_ERR_ARGUMENT while UCFDBLUSGS_Residual still computes it."""
+    from ucfd_sparse_gb300 import lib
+    from ucfd_sparse_gb300.flowsys import FlowSys
+    N = 8388610
+    nF = N // 2
+    dev = torch.device("cuda:0")
+    i = torch.arange(N, dtype=torch.int32, device=dev)
+    rowptr = torch.arange(N + 1, dtype=torch.int32, device=dev)
+    colidx = torch.bitwise_xor(i, 1)
+    slots = torch.div(i, 2, rounding_mode="floor")
+    sides = torch.where(i % 2 == 0, 1, -1).to(torch.int8)
+    area = torch.ones(nF, dtype=torch.float64, device=dev)
+    normal = torch.zeros(3, nF, dtype=torch.float64, device=dev)
+    normal[0] = 1.0
+    rv = torch.ones(N, dtype=torch.float64, device=dev)
+    S = FlowSys(N, 5, 5, 3, nF, 1, rowptr, colidx, slots, sides, area, normal, rv)
+    jmat = torch.zeros(2, 5, 5, nF, dtype=torch.float64, device=dev)
+    for r in range(5):
+        jmat[0, r, r] = 1.0
+        jmat[1, r, r] = -1.0
+    rhs = torch.randn(5, N, dtype=torch.float64, device=dev, generator=torch.Generator(dev).manual_seed(3))
+    upts = torch.zeros_like(rhs)
+    S.set_element(0, N, 1, i.clone(), upts, rhs, torch.ones(N, dtype=torch.float64, device=dev),
+                  torch.zeros_like(rhs), torch.ones(N, dtype=torch.float64, device=dev), torch.zeros_like(rhs))
+    S.set_blusgs(jmat)
+    S.blusgs_pack(0, 0.0)
+    S.blusgs_ns_prepare()
+    S.blusgs_reset()
+    assert abs(S.blusgs_residual() - 1.0) <= 1e-12  # du = 0: the residual is rhs itself
+    h = ctypes.c_double(-1.0)
+    with pytest.raises(lib.UCFDError) as ex:
+        _noalloc(S, h)
+    assert ex.value.status == 2 and "8388608" in str(ex.value)
+    assert h.value == -1.0
+    S.destroy()
+    del jmat
+    torch.cuda.empty_cache()

@@ -1,13 +1,13 @@
 // noalloc.cu -- UCFDBLUSGS_ResidualNoAlloc: the FP64 residual norm of a
 // prepared block LU-SGS system computed without any allocation.
 //
-// Who needs it: a CFD code that drives its pseudo-time loop from inside a
-// CUDA stream capture (cudaMalloc is not allowed while a stream is being
-// captured), or one that hands its whole device-memory budget to its own
-// pool allocator at start-up and forbids allocations afterwards, still has
-// to monitor the linear residual every iteration.  UCFDBLUSGS_Residual
-// grows private reduction buffers on first use; this variant keeps its
-// partial sums in a fixed file-scope device array instead.
+// Who needs it: a CFD code that hands its whole device-memory budget to its
+// own pool allocator at start-up and forbids allocations afterwards, or one
+// whose time-step loop must not stall on cudaMalloc (which can synchronise
+// the device), still has to monitor the linear residual every iteration.
+// UCFDBLUSGS_Residual grows private reduction buffers on first use; this
+// variant keeps its partial sums in a fixed file-scope device array instead
+// and calls no cudaMalloc, cudaFree or allocating library routine.
 //
 // Limits and sharing rules:
 //  * the scratch array holds 2 * kMaxBlocks partial sums plus 2 totals
@@ -20,11 +20,17 @@
 //    slot a call reads is written by that same call first, so nothing has to
 //    start at zero -- but two calls whose kernels overlap on the GPU (e.g.
 //    issued on different streams without ordering) race on it;
-//  * the first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress) and caches it; make that first call before any
-//    stream capture begins.
+//  * the call runs on the device that holds the handle's arrays: it makes
+//    that device current for its duration and restores the caller's device
+//    before returning;
+//  * the first call on a device does the set-up: with that device current it
+//    looks up the array's device address (cudaGetSymbolAddress) and caches
+//    it, so make that first call before any stream capture begins;
+//  * like UCFDBLUSGS_Residual the call returns only after the result has
+//    been written (it synchronises the handle's stream).
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 
 #include "../../include/ucfdlusgs.h"
@@ -43,7 +49,23 @@ constexpr int kMaxDevices = 64;
 // 2 partial sums per block (r.r, rhs.rhs) followed by the 2 totals.
 static __device__ __align__(256) double g_resid_scratch[2 * kMaxBlocks + 2];
 
-double *g_scratch_addr[kMaxDevices] = {nullptr};
+// device address of g_resid_scratch per device, filled on a device's first
+// call; concurrent first calls store the same value
+std::atomic<double *> g_scratch_addr[kMaxDevices];
+
+// Makes `dev` current for the scope of a call and restores the caller's
+// device afterwards (also when the call fails).
+struct DeviceScope {
+    int prev = -1;
+    explicit DeviceScope(int dev) {
+        UCFD_CUDA(cudaGetDevice(&prev));
+        if (prev != dev) UCFD_CUDA(cudaSetDevice(dev));
+        else prev = -1;
+    }
+    ~DeviceScope() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
 
 __device__ inline double warp_block_sum(double v, double *sh) {
 #pragma unroll
@@ -161,16 +183,20 @@ extern "C" ucfd_status_t UCFDBLUSGS_ResidualNoAlloc(FlowSys sys, UCFDReal *relre
     UCFD_REQUIRE(v.N <= kMaxCells,
                  "UCFDBLUSGS_ResidualNoAlloc: %lld cells exceed the fixed scratch capacity of %lld cells "
                  "(use UCFDBLUSGS_Residual)", v.N, kMaxCells);
-    int dev = 0;
-    UCFD_CUDA(cudaGetDevice(&dev));
-    UCFD_REQUIRE(dev >= 0 && dev < kMaxDevices, "device index %d out of range", dev);
-    if (!g_scratch_addr[dev]) {
+    // the device that holds the handle's prepared arrays
+    cudaPointerAttributes pa{};
+    UCFD_CUDA(cudaPointerGetAttributes(&pa, v.D));
+    const int dev = pa.device;
+    UCFD_REQUIRE(pa.type == cudaMemoryTypeDevice && dev >= 0 && dev < kMaxDevices,
+                 "UCFDBLUSGS_ResidualNoAlloc: the handle's arrays are not on a CUDA device below %d", kMaxDevices);
+    DeviceScope on(dev);
+    if (!g_scratch_addr[dev].load(std::memory_order_acquire)) {
         // set-up, once per device, with that device current
         void *p = nullptr;
         UCFD_CUDA(cudaGetSymbolAddress(&p, g_resid_scratch));
-        g_scratch_addr[dev] = (double *)p;
+        g_scratch_addr[dev].store((double *)p, std::memory_order_release);
     }
-    double *scratch = g_scratch_addr[dev];
+    double *scratch = g_scratch_addr[dev].load(std::memory_order_acquire);
     cudaStream_t s = (cudaStream_t)v.stream;
     const int nb = (int)((v.N + kCellsPerBlock - 1) / kCellsPerBlock);
     if (v.x64) launch<double>(v, v.x64, scratch, nb, s);
