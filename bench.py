@@ -157,13 +157,14 @@ def make_case(m: int, seed: int = 0):
 
 def sweep_bytes(rowptr: np.ndarray, elt: int, B: int = 5, lu_elt: int | None = None) -> int:
     """Algorithmic bytes of one lower (or upper) BLU-SGS sweep over all
-    cells: per cell-face its neighbour index (4), face area (elt) and block
-    (B*B*elt); per cell rcp_vol, the LU block, rhs, and du read (as the
-    neighbours' data, once) and written."""
+    cells as the FP32 / FMA-mode kernels run it: per cell-face its neighbour
+    index (4) and block (B*B*elt, the face factor folded in at Prepare); per
+    cell the LU block, rhs, and du read (as the neighbours' data, once) and
+    written."""
     lu_elt = elt if lu_elt is None else lu_elt
     nnz = int(rowptr[-1])
     N = rowptr.shape[0] - 1
-    return nnz * (4 + elt + B * B * elt) + N * (elt + B * B * lu_elt + 3 * B * elt)
+    return nnz * (4 + B * B * elt) + N * (B * B * lu_elt + 3 * B * elt)
 
 
 class Problem:
@@ -493,12 +494,25 @@ def run_gpu(args):
     ev1.record(stream)
     torch.cuda.synchronize()
     sweep_ms = ev0.elapsed_time(ev1) / (2 * nk)
+    # the FP64 (fused multiply-add) sweep the same way
+    P64.S.blusgs_pack(0, 0.0)
+    P64.S.blusgs_ns_prepare()
+    P64.S.blusgs_reset()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    for _ in range(nk):
+        P64.S.blusgs_ns_lower()
+        P64.S.blusgs_ns_upper()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    sweep64_ms = ev0.elapsed_time(ev1) / (2 * nk)
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except OSError:
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
+    bytes_sweep64 = sweep_bytes(case["rowptr"], 8, 5, 8)
     bytes_sweep = sweep_bytes(case["rowptr"], 4, 5, 4)
     achieved = bytes_sweep / (sweep_ms * 1e-3) / 1e9
     launch_bytes = bytes_sweep / nlev
@@ -551,6 +565,27 @@ def run_gpu(args):
         pe.append(Ph.step(args.rtol, args.max_pairs, args.inner, calls)[0])
     torch.cuda.synchronize()
     e2e_s = reduce_max((time.perf_counter() - t0) / args.steps, dist, device)
+    # the same steps again with the library's host<->device copies timed by
+    # CUDA events (each timed copy waits for itself, so these steps are not
+    # the ones above): where the time of the host-input calls goes
+    from ucfd_sparse_gb300 import lib as _lib
+    xfer_calls = {}
+    _lib.transfer_timing(True)
+    t1 = time.perf_counter()
+    for _ in range(args.steps):
+        Ph.step(args.rtol, args.max_pairs, args.inner, xfer_calls)
+    torch.cuda.synchronize()
+    xfer_s = (time.perf_counter() - t1) / args.steps
+    xfer = _lib.transfer_stats()
+    _lib.transfer_timing(False)
+    xfer_out = {"ms_per_step": xfer_s * 1e3,
+                "h2d_ms_per_step": xfer["h2d_ms"] / args.steps,
+                "h2d_bytes_per_step": xfer["h2d_bytes"] / args.steps,
+                "h2d_GBps": xfer["h2d_bytes"] / max(xfer["h2d_ms"], 1e-9) / 1e6,
+                "d2h_ms_per_step": xfer["d2h_ms"] / args.steps,
+                "d2h_bytes_per_step": xfer["d2h_bytes"] / args.steps,
+                "ms_per_call": {k: v * 1e3 / args.steps for k, v in xfer_calls.items()},
+                "how": "CUDA events around every host<->device copy the library makes, same steps repeated"}
     # the same pinned jmat copied alone (torch copy, one transfer): the host link's rate for it
     jdev = torch.empty(Ph.e["jmat"].shape, dtype=Ph.e["jmat"].dtype, device=device)
     torch.cuda.synchronize()
@@ -571,7 +606,10 @@ def run_gpu(args):
             "config": headline_config(args, N, len(rg), ws),
             "pairs_per_step": pairs_mean, "relres": max(rel32),
             "fp64": {"ms_per_step": ms64, "pairs_per_step": statistics.mean(pairs64), "relres": max(rel64),
-                     "value": N * statistics.mean(pairs64) / (ms64 * 1e-3)},
+                     "value": N * statistics.mean(pairs64) / (ms64 * 1e-3),
+                     "sweep_ms": sweep64_ms, "sweep_GBps": bytes_sweep64 / (sweep64_ms * 1e-3) / 1e9,
+                     "sweep_frac": bytes_sweep64 / (sweep64_ms * 1e-3) / 1e9 / peak,
+                     "sweep_kernel": "fs_blusgs_sweep_kernel<double,5,6,true> (FP64 with fused multiply-adds)"},
             "speedup_fp32_refined_vs_fp64": ms64 / ms32,
             "err_vs_fp64": err["err_vs_fp64"], "error": err,
             "roofline": roofline,
@@ -579,7 +617,7 @@ def run_gpu(args):
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": Ph.h2d_bytes(),
                     "d2h_bytes_per_step": Ph.d2h_bytes(), "ms_per_step": e2e_s * 1e3,
                     "ms_per_call": {k: v * 1e3 / args.steps for k, v in calls.items()},
-                    "jmat_copy_GBps": jmat_gbps},
+                    "jmat_copy_GBps": jmat_gbps, "copies_timed": xfer_out},
             "gpu_launches": launches_per_step(nlev, int(round(pairs_mean)), args.inner, True) * args.steps,
             "clocks": clocks,
             "launch": tuned or "defaults (--no-autotune)",
@@ -670,17 +708,32 @@ def run_lusgs(args):
         S.lusgs_pack(0, 1.0, 0.0)
         S.lusgs_run(args.iters, 1.0, True, mode, hist)
         res[mode] = dict(ms=ms, clocks=clk.summary(), resid_first=float(hist[0]), resid_last=float(hist[-1]))
-        # scalar sweep kernel alone (per-level launches): NS lower sweep
+        # scalar sweep kernel alone (per-level launches): NS lower sweep, the
+        # tuned launch and every variant at 256 threads
         if mode == 0:
             S.lusgs_ns_prepare(1.0)
-            torch.cuda.synchronize()
-            e0, e1 = _events(stream)
-            e0.record(stream)
-            for _ in range(10):
+
+            def lower_ms():
                 S.lusgs_ns_lower(1.0)
-            e1.record(stream)
-            torch.cuda.synchronize()
-            res["sweep_ms"] = e0.elapsed_time(e1) / 10
+                torch.cuda.synchronize()
+                e0, e1 = _events(stream)
+                e0.record(stream)
+                for _ in range(10):
+                    S.lusgs_ns_lower(1.0)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                return e0.elapsed_time(e1) / 10
+
+            res["sweep_ms"] = lower_ms()
+            res["sweep_launch"] = S.launch_config()
+            cand = {}
+            for var in (0, 1, 2, 3, 5):
+                S.set_launch_config(threads_per_block=256, sweep_variant=var)
+                cand[f"v{var}/b256"] = lower_ms()
+            for tpb in (64, 128):
+                S.set_launch_config(threads_per_block=tpb, sweep_variant=5)
+                cand[f"v5/b{tpb}"] = lower_ms()
+            res["sweep_candidates_ms"] = cand
         del S
     # error of the FP32 loop against the FP64 arithmetic of the oracle
     # (UCFD_PREC_FP64): args.iters iterations of each from the same state
@@ -699,6 +752,7 @@ def run_lusgs(args):
             S.set_launch_config(**res["launch"])
         S.lusgs_pack(0, 1.0, 0.0)
         S.lusgs_run(args.iters, 1.0, True, 0, None)
+        S.lusgs_update(0)                           # the device-resident state back to uu
         torch.cuda.synchronize()
         finals[prec] = uu
         del S
@@ -728,7 +782,13 @@ def run_lusgs(args):
            "persistent": {"ms": res[1]["ms"], "cell_updates_per_s": N * args.iters / (res[1]["ms"] * 1e-3),
                           "GBps": bytes_iter * args.iters / (res[1]["ms"] * 1e-3) / 1e9},
            "bytes_per_cell_iteration": bytes_iter / N,
-           "roofline": {"bound": "hbm", "kernel": "scalar_sweep_kernel<float,6,5,3,false>",
+           "roofline": {"bound": "hbm",
+                        "kernel": ("scalar_sweep_faces_kernel<float,6,5,3,false>"
+                                   if res["sweep_launch"]["sweep_variant"] == 5 else
+                                   "scalar_sweep_pair_kernel<float,6,5,3,false>"
+                                   if res["sweep_launch"]["sweep_variant"] in (3, 4) else
+                                   "scalar_sweep_kernel<float,6,5,3,false>"),
+                        "launch": res["sweep_launch"], "candidates_ms": res["sweep_candidates_ms"],
                         "achieved": sweep_bytes_ / (res["sweep_ms"] * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                         "frac": sweep_bytes_ / (res["sweep_ms"] * 1e-3) / 1e9 / peak,
                         "sweep_ms": res["sweep_ms"], "algorithmic_bytes_per_sweep": sweep_bytes_},

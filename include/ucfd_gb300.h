@@ -73,6 +73,20 @@ UCFD_EXTERN const char *UCFDGetLastError(void);
  * process-wide runtime values here). */
 UCFD_EXTERN ucfd_status_t UCFDSetConstants(UCFDReal gamma, UCFDReal pmin, UCFDReal betast);
 
+/* Host<->device copies of caller arrays made by the library (host-pointer
+ * arguments are staged to the GPU and results copied back), timed with CUDA
+ * events on the copying stream while timing is on.  No counterpart in the
+ * reference.  UCFDSetTransferTiming(1) clears the counters and starts
+ * timing (each timed copy then waits for its own completion);
+ * UCFDSetTransferTiming(0) stops it.  Counters are process-wide. */
+typedef struct {
+    double h2d_ms, h2d_bytes;  /* host -> device: summed copy time, bytes */
+    double d2h_ms, d2h_bytes;  /* device -> host */
+    long long h2d_copies, d2h_copies;
+} UCFDTransferStats;
+UCFD_EXTERN ucfd_status_t UCFDSetTransferTiming(int on);
+UCFD_EXTERN ucfd_status_t UCFDGetTransferStats(UCFDTransferStats *stats);
+
 /* Library version string and the device it runs on (diagnostics). */
 UCFD_EXTERN const char *UCFDVersion(void);
 UCFD_EXTERN ucfd_status_t UCFDDeviceInfo(char *name, size_t len, int *sm_count);

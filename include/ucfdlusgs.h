@@ -109,8 +109,11 @@ typedef struct {
                               by bulk copies (2 / 1 buffers per warp; ELL width 6 or 4),
                               4 = 0 launched as a programmatic dependent of the previous
                               colour (its start overlaps the previous colour's tail);
+                              5 = 0 for the block sweep;
                               scalar sweeps: 0 default build, 1 / 2 capped at 80 / 64
-                              registers (more resident warps) */
+                              registers (more resident warps), 3 / 4 two threads per
+                              cell, 5 one thread per active face (per-level launches;
+                              the persistent kernel keeps one thread per cell) */
     int run_mode;          /* UCFDLUSGS_Run with mode -1: 0 CUDA graph, 1 persistent kernel */
     double ms;             /* Autotune: time of the best candidate (one sweep pair, or one
                               Run iteration for scalar LU-SGS); 0 when set by hand */

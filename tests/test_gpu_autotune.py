@@ -85,16 +85,16 @@ def test_blusgs_autotune_keeps_golden(golden, ucfd):
 
 @pytest.mark.parametrize("prec", [0, 2])
 def test_scalar_sweep_variants_identical(prec, golden, ucfd):
-    """The five scalar sweep builds (one thread per cell with 3 register
-    budgets, two threads per cell with 2) give the same result; in FP64 it
-    is the golden oracle result bit for bit."""
+    """The six scalar sweep builds (one thread per cell with 3 register
+    budgets, two threads per cell with 2, one thread per active face) give
+    the same result; in FP64 it is the golden oracle result bit for bit."""
     from tests.test_gpu_lusgs import flowsys_step
     meta, arr = golden
     name = "fs9"
     kw = cases.FLOWSYS[name]
     fs, inp = cases.flowsys_case(**kw)
     outs = []
-    for var in range(5):
+    for var in range(6):
         S, e = make_flowsys(fs, inp, prec=prec, on_device=True)
         S.set_launch_config(threads_per_block=128, sweep_variant=var)
         flowsys_step(S, kw, kw["nsteps"])

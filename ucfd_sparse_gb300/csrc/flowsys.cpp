@@ -37,6 +37,7 @@ struct Work {
     DevBuf<S> u, du, diag, base, lamN, lamT, rhs0;  // scalar LU-SGS
     DevBuf<S> rhs, bdu, dup, J, LU, tJ, tLU;        // block LU-SGS
     DevBuf<S> r, delta;                    // refinement
+    DevBuf<S> fl_geo[2];                   // face lists (lower, upper): normal + fa * rv per entry
 };
 
 }  // namespace
@@ -85,6 +86,9 @@ struct _FlowSys {
     int run_rans = -1;
     double run_kappa = 0;
     bool run_state = false;  // set by UCFDLUSGS_Run, cleared by Pack
+    // scalar sweep variant 5: per sweep direction (lower, upper) the active
+    // faces cell by cell -- offsets [N + 1], neighbour and ELL slot per entry
+    DevBuf<int> fl_off[2], fl_nb[2], fl_q[2];
     // persistent sweeps: level offsets on the device, barrier {count, gen}, timeout flag
     DevBuf<int> d_lev_off, d_err;
     DevBuf<unsigned> d_bar;
@@ -230,6 +234,57 @@ constexpr long long kBarrierMaxSpin = 1ll << 24;
 // poll may suspend for a while): far beyond a copy's microseconds.
 constexpr long long kBulkMaxSpin = 1ll << 20;
 
+// Scalar sweep variant 5 (one thread per active face): the face lists of
+// both sweep directions, built on the host from the level schedule at first
+// use (never inside a stream capture: run_graph_build calls this first),
+// and their geometry in the working precision.
+template <typename S>
+void ensure_face_lists(FlowSys s) {
+    Work<S> &w = work<S>(s);
+    if (w.fl_geo[0].p && w.fl_geo[1].p) return;
+    cudaStream_t st = s->stream();
+    const long long N = s->N;
+    const int P = s->P;
+    UCFD_REQUIRE((long long)P * N < (1ll << 31), "face-list sweep: %lld cell-faces exceed int32", (long long)P * N);
+    if (!s->fl_nb[0].p || !s->fl_nb[1].p) {
+        std::vector<int> nei((size_t)P * N);
+        UCFD_CUDA(cudaMemcpyAsync(nei.data(), s->d_nei.p, nei.size() * sizeof(int), cudaMemcpyDeviceToHost, st));
+        UCFD_CUDA(cudaStreamSynchronize(st));
+        std::vector<int> lev((size_t)N);
+        for (int l = 0; l < s->sch.nlev; ++l)
+            for (int k = s->sch.lev_off[l]; k < s->sch.lev_off[l + 1]; ++k) lev[k] = l;
+        for (int dir = 0; dir < 2; ++dir) {
+            std::vector<int> off((size_t)N + 1), nb, q;
+            nb.reserve((size_t)P * N / 2 + 1);
+            q.reserve((size_t)P * N / 2 + 1);
+            for (long long k = 0; k < N; ++k) {
+                off[k] = (int)nb.size();
+                for (int p = 0; p < P; ++p) {
+                    const int g = nei[(size_t)p * N + k];
+                    if (g < 0) continue;
+                    // active: the neighbour's level comes earlier in this sweep
+                    if (dir == 0 ? lev[g] < lev[k] : lev[g] > lev[k]) {
+                        nb.push_back(g);
+                        q.push_back((int)(p * N + k));
+                    }
+                }
+            }
+            off[N] = (int)nb.size();
+            s->fl_off[dir].upload(off.data(), off.size(), st);
+            s->fl_nb[dir].upload(nb.data(), nb.size(), st);
+            s->fl_q[dir].upload(q.data(), q.size(), st);
+        }
+    }
+    for (int dir = 0; dir < 2; ++dir) {
+        const long long E = (long long)s->fl_nb[dir].n;
+        w.fl_geo[dir].ensure((size_t)4 * (E > 0 ? E : 1));
+        kfast::face_list_geo<S>(E, N, s->ndims, s->fl_q[dir].p, w.nrm.p, geo_fa<S>(s), geo_rv<S>(s),
+                                w.fl_geo[dir].p, st);
+    }
+    UCFD_CHECK_LAUNCH();
+    UCFD_CUDA(cudaStreamSynchronize(st));
+}
+
 template <typename S, bool EX>
 void lusgs_sweep(FlowSys s, bool rans, bool upper, double kappa, bool persistent = false) {
     Work<S> &w = work<S>(s);
@@ -258,6 +313,16 @@ void lusgs_sweep(FlowSys s, bool rans, bool upper, double kappa, bool persistent
     // 256 per SM; 3 / 4 = two threads per cell, default / 64-register build
     a.regcap = (s->variant == 1) ? 3 : (s->variant == 2 || s->variant == 4) ? 4 : 0;
     a.pair = (s->variant == 3 || s->variant == 4) ? 1 : 0;
+    // 5: one thread per active face, from the face lists
+    a.facelist = (s->variant == 5 && !persistent) ? 1 : 0;
+    if (a.facelist) {
+        ensure_face_lists<S>(s);
+        const int dir = upper ? 1 : 0;
+        a.fl_off = s->fl_off[dir].p;
+        a.fl_nb = s->fl_nb[dir].p;
+        a.fl_q = s->fl_q[dir].p;
+        a.fl_geo = w.fl_geo[dir].p;
+    }
     const int L = s->sch.nlev;
     if (persistent) {
         // one cooperative launch per sweep, bounded grid barrier between levels
@@ -367,12 +432,14 @@ void blusgs_residual(FlowSys s, const Sx *x, R *r_out, double *rnorm, double *bn
     s->red.ensure(2);
     const double *J64 = s->prec == UCFD_PREC_FP32 ? s->J64.p : s->w64.J.p;
     const double *rhs64 = s->prec == UCFD_PREC_FP32 ? s->rhs64.p : s->w64.rhs.p;
+    // the FMA mode's blocks already carry the face factor (nullptr face areas)
+    const double *fa = s->prec == UCFD_PREC_FP64_FMA ? nullptr : s->fa64.p;
     int nb = 0;
     if constexpr (EX)
-        kexact::fs_blusgs_residual<Sx, R>(s->nfvars, s->N, s->P, 0, s->nvars, s->d_nei.p, s->fa64.p, s->rv64.p,
+        kexact::fs_blusgs_residual<Sx, R>(s->nfvars, s->N, s->P, 0, s->nvars, s->d_nei.p, fa, s->rv64.p,
                                           J64, s->D.p, rhs64, x, r_out, s->part.p, nbmax, &nb, s->stream());
     else
-        kfast::fs_blusgs_residual<Sx, R>(s->nfvars, s->N, s->P, 0, s->nvars, s->d_nei.p, s->fa64.p, s->rv64.p,
+        kfast::fs_blusgs_residual<Sx, R>(s->nfvars, s->N, s->P, 0, s->nvars, s->d_nei.p, fa, s->rv64.p,
                                          J64, s->D.p, rhs64, x, r_out, s->part.p, nbmax, &nb, s->stream());
     kfast::pair_reduce(nb, s->part.p, s->red.p, s->stream());
     double *h = s->h_red.ensure(2);
@@ -437,6 +504,7 @@ void run_graph_build(FlowSys s, bool rans, double kappa) {
     if (s->run_exec && s->run_rans == (int)rans && s->run_kappa == kappa) return;
     run_graph_drop(s);
     cudaStream_t st = s->stream();
+    if (s->variant == 5) ensure_face_lists<S>(s);  // host work: before the capture
     UCFD_CUDA(cudaStreamSynchronize(st));
     cudaGraph_t g;
     UCFD_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -644,9 +712,9 @@ ucfd_status_t UCFDFlowSysSetLaunchConfig(FlowSys s, const UCFDLaunchConfig *cfg)
     const int b = cfg->threads_per_block;
     UCFD_REQUIRE(b == 0 || (b % 32 == 0 && b >= 32 && b <= 256),
                  "threads_per_block must be 0 or a multiple of 32 up to 256 (got %d)", b);
-    UCFD_REQUIRE(cfg->sweep_variant >= 0 && cfg->sweep_variant <= 4, "sweep_variant must be 0..4");
+    UCFD_REQUIRE(cfg->sweep_variant >= 0 && cfg->sweep_variant <= 5, "sweep_variant must be 0..5");
     UCFD_REQUIRE(cfg->run_mode == 0 || cfg->run_mode == 1, "run_mode must be 0 or 1");
-    if (b != s->block) run_graph_drop(s);
+    if (b != s->block || cfg->sweep_variant != s->variant) run_graph_drop(s);
     s->block = b;
     s->variant = cfg->sweep_variant;
     s->run_mode = cfg->run_mode;
@@ -739,8 +807,9 @@ ucfd_status_t UCFDFlowSysAutotune(FlowSys s, int reps, UCFDLaunchConfig *best) {
             }
             run_gather_lambda<S>(s, false, 1);
             // variant 0: unconstrained registers; 1 / 2: at most 80 / 64 registers;
-            // 3 / 4: two threads per cell (the persistent kernel stays one per cell)
-            for (int v = 0; v <= 4; ++v) {
+            // 3 / 4: two threads per cell; 5: one thread per active face (the
+            // persistent kernel stays one per cell)
+            for (int v = 0; v <= 5; ++v) {
                 s->variant = v;
                 for (int b : kTuneBlocks) {
                     s->block = b;
@@ -848,7 +917,7 @@ ucfd_status_t UCFDLUSGS_Update(FlowSys s, UCFDInt eidx) {
         KCALL(EX, fs_lusgs_update<S>, e.neles, s->nvars, s->N, ids, s->d_iperm.p, s->run_state ? w.u.p : w.du.p,
               up, s->run_state ? 1 : 0, st);
     });
-    if (!dev) UCFD_CUDA(cudaMemcpyAsync(e.uptsb, up, nv * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (!dev) copy_d2h(e.uptsb, up, nv * sizeof(double), st);
     finish(s, !dev);
     UCFD_API_END
 }
@@ -1087,7 +1156,7 @@ ucfd_status_t UCFDBLUSGS_SubResidual(FlowSys s, UCFDInt eidx) {
         UCFD_REQUIRE(w.bdu.p, "SubResidual before Pack");
         KCALL(EX, fs_blusgs_subres<S>, e.neles, s->nvars, s->N, ids, s->d_iperm.p, vol, w.bdu.p, w.dup.p, res, st);
     });
-    if (!dev) UCFD_CUDA(cudaMemcpyAsync(e.resid_out, res, nv * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (!dev) copy_d2h(e.resid_out, res, nv * sizeof(double), st);
     finish(s, !dev);
     UCFD_API_END
 }
@@ -1112,7 +1181,7 @@ ucfd_status_t UCFDBLUSGS_Update(FlowSys s, UCFDInt eidx) {
             KCALL(EX, fs_blusgs_update<S>, e.neles, s->nvars, s->N, ids, s->d_iperm.p, w.bdu.p, up, st);
         });
     }
-    if (!dev) UCFD_CUDA(cudaMemcpyAsync(e.uptsb, up, nv * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (!dev) copy_d2h(e.uptsb, up, nv * sizeof(double), st);
     finish(s, !dev);
     UCFD_API_END
 }
@@ -1214,7 +1283,7 @@ bool ucfd::flowsys_block_view(FlowSys s, BlockSystemView &v) {
     t.P = s->P;
     t.B = s->nfvars;
     t.nei = s->d_nei.p;
-    t.fa = s->fa64.p;
+    t.fa = s->prec == UCFD_PREC_FP64_FMA ? nullptr : s->fa64.p;  // FMA mode: J64 carries fa * rv
     t.rv = s->rv64.p;
     t.D = s->D.p;
     if (s->prec == UCFD_PREC_FP32) {

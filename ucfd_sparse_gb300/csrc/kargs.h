@@ -57,6 +57,15 @@ struct ScalarSweepArgs {
     int regcap;            // 0, or 3 / 4: the kernel built for that many blocks of 256 threads per SM
                            // (at most 80 / 64 registers)
     int pair;              // 1: two threads per cell (faces 0-2 / 3-5; ELL width <= 6, per-level launches)
+    // one thread per active face (per-level launches): the faces of this
+    // sweep direction whose neighbour lies in an earlier level, cell by cell
+    // in face order
+    int facelist;          // 1: use the list
+    int cpb;               // cells per block (0: a third of the block's threads)
+    const int *fl_off;     // [ld + 1] first list entry of each cell
+    const int *fl_nb;      // [E] neighbour cell of each entry
+    const int *fl_q;       // [E] ELL slot f * ld + cell of each entry (spectral radius)
+    const T *fl_geo;       // [E][4] outward normal (zero-padded to 3 components) and fa * rv
 };
 
 // One colour of a transposed (adjoint) colored LU-SGS sweep.

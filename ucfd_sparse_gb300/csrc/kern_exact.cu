@@ -2,6 +2,7 @@
 // contraction, so each cell's arithmetic is the reference's operation by
 // operation (IEEE-rounded division and multiply/add, same order).
 #define UCFD_KNS kexact
+#define UCFD_KEXACT 1
 #include "launchers.cuh"
 
 namespace kexact {

@@ -6,6 +6,8 @@
 namespace kfast {
 #define UCFD_INST_T(T)                                                                                          \
     template void scalar_sweep<T>(const ::ucfd::ScalarSweepArgs<T> &, int, int, int, int, int, cudaStream_t);  \
+    template void face_list_geo<T>(long long, long long, int, const int *, const T *, const T *, const T *,    \
+                                   T *, cudaStream_t);                                                         \
     template void scalar_sweep_persistent<T>(const ::ucfd::ScalarSweepArgs<T> &, int, int, int, int,           \
                                              const int *, int, unsigned *, int *, long long, cudaStream_t);    \
     template void legacy_pre<T>(int, int, T, const T *, const T *, T *, const T *, cudaStream_t);              \

@@ -18,12 +18,13 @@ namespace UCFD_KNS {
 
 // ludcmp: src/lusgs/inverse.h:13-45 (Doolittle, no pivoting, row by row).
 // RCP: multiply by the reciprocal of each pivot (B - 1 divisions instead of
-// B(B-1)/2 + B - 1) -- used where the FP64 factors are then rounded to FP32
-// for the sweeps: x * (1/p) differs from x / p by at most a rounding at the
-// 1e-16 level, far below the FP32 rounding that follows.  The FP64 modes
-// keep the reference's divisions.
-template <typename T, int B, bool RCP = false>
+// B(B-1)/2 + B - 1) -- used in the fast build: x * (1/p) differs from x / p
+// by at most a rounding at the 1e-16 level.  RSTORE (with RCP): the
+// diagonal then holds the reciprocal pivots 1/p instead of p, for
+// lusub_dev<..., true>.  The exact build keeps the reference's divisions.
+template <typename T, int B, bool RCP = false, bool RSTORE = false>
 __device__ __forceinline__ void ludcmp_dev(T *A) {
+    static_assert(RCP || !RSTORE, "reciprocal pivots are stored by the RCP form");
     if constexpr (B == 1) {
         A[0] = T(1) / A[0];
     } else if constexpr (RCP) {
@@ -46,7 +47,12 @@ __device__ __forceinline__ void ludcmp_dev(T *A) {
                     A[nr + col] -= v;
                 }
             }
-            if (row + 1 < B) ip[row] = T(1) / A[(B + 1) * row];  // the row's pivot is final now
+            // the row's pivot is final now (pivots are read only through ip)
+            if (row + 1 < B || RSTORE) ip[row] = T(1) / A[(B + 1) * row];
+        }
+        if constexpr (RSTORE) {
+#pragma unroll
+            for (int row = 0; row < B; ++row) A[(B + 1) * row] = ip[row];
         }
     } else {
 #pragma unroll
@@ -71,7 +77,9 @@ __device__ __forceinline__ void ludcmp_dev(T *A) {
 }
 
 // lusub: src/lusgs/inverse.h:51-80 (unit-lower forward, upper backward).
-template <typename T, int B>
+// RCP: the diagonal holds reciprocal pivots (ludcmp_dev RSTORE): multiply.
+// (B == 1 stores the reciprocal in both forms, inverse.h:16.)
+template <typename T, int B, bool RCP = false>
 __device__ __forceinline__ void lusub_dev(const T *LU, T *b) {
     if constexpr (B == 1) {
         b[0] *= LU[0];
@@ -83,13 +91,15 @@ __device__ __forceinline__ void lusub_dev(const T *LU, T *b) {
             for (int col = 0; col < row; ++col) v += LU[row * B + col] * b[col];
             b[row] -= v;
         }
-        b[B - 1] /= LU[B * B - 1];
+        if constexpr (RCP) b[B - 1] *= LU[B * B - 1];
+        else b[B - 1] /= LU[B * B - 1];
 #pragma unroll
         for (int row = B - 2; row > -1; --row) {
             T v = T(0);
 #pragma unroll
             for (int col = row + 1; col < B; ++col) v += LU[row * B + col] * b[col];
-            b[row] = (b[row] - v) / LU[row * B + row];
+            if constexpr (RCP) b[row] = (b[row] - v) * LU[row * B + row];
+            else b[row] = (b[row] - v) / LU[row * B + row];
         }
     }
 }
@@ -201,7 +211,10 @@ __device__ __forceinline__ double xor_sign(double x, unsigned hi_mask) {
 }
 
 // pre_blusgs: blusgs.c:200-246, plus the gather of each cell-face's
-// off-diagonal block (the half the sweeps use) into the ELL layout.
+// off-diagonal block (the half the sweeps use) into the ELL layout.  The
+// fast build stores the sweep blocks J_s times the face factor fv and
+// reciprocal pivots (kFold); J64, the FP64 copy the FP32 mode's residual
+// reads, always holds the unscaled blocks.
 // The block starts from dd[k] I when dd is given (NS pack), else from D.
 // jt holds the face-major records written by jmat_face_major_kernel.
 // The side's sign goes into the face factor once per face: the diagonal
@@ -251,7 +264,7 @@ __global__ void fs_blusgs_prepare_kernel(long long N, int P, const int *nei, con
                 dm[c + r * B] += (pos ? h0 : h1) * fvs;    // == (pos ? h0 : -h1) * fv
                 const double jv = xor_sign(pos ? h1 : h0, neg);  // == pos ? h1 : -h0
                 const long long o = jbase + ((long long)(p * B2 + r * B + c) << 5);
-                J_s[o] = (S)jv;
+                J_s[o] = (S)(kFold ? jv * fv : jv);
                 if (J64) J64[o] = jv;
             }
         }
@@ -259,7 +272,7 @@ __global__ void fs_blusgs_prepare_kernel(long long N, int P, const int *nei, con
     const long long dbase = ::ucfd::tile_index(k, 0, B2);
 #pragma unroll
     for (int e = 0; e < B2; ++e) D[dbase + (e << 5)] = dm[e];
-    ludcmp_dev<double, B, std::is_same<S, float>::value>(dm);
+    ludcmp_dev<double, B, kFold, kFold>(dm);
 #pragma unroll
     for (int e = 0; e < B2; ++e) {
         if (LU64) LU64[dbase + (e << 5)] = dm[e];
@@ -308,14 +321,14 @@ __global__ void __launch_bounds__(256) fs_blusgs_sweep_kernel(int t0, int t1, lo
     S b[B];
 #pragma unroll
     for (int r = 0; r < B; ++r) b[r] = __ldcs(rhs + (var0 + r) * N + k);
-    const S rvk = rv[k];
+    const S rvk = kFold ? S(1) : rv[k];
     if constexpr (PW > 0) {
         int nb[PW];
         S fv[PW];
 #pragma unroll
         for (int p = 0; p < PW; ++p) {
             nb[p] = __ldcs(nei + p * N + k);
-            fv[p] = __ldcs(fa + p * N + k) * rvk;
+            if constexpr (!kFold) fv[p] = __ldcs(fa + p * N + k) * rvk;
         }
         if constexpr (DEP) asm volatile("griddepcontrol.wait;" ::: "memory");
         S x[PW][B];
@@ -334,10 +347,16 @@ __global__ void __launch_bounds__(256) fs_blusgs_sweep_kernel(int t0, int t1, lo
             if (nb[p] >= 0) {
 #pragma unroll
                 for (int r = 0; r < B; ++r) {
-                    S val = S(0);
+                    if constexpr (kFold) {
+                        // straight into b: one fused multiply-add per block entry
 #pragma unroll
-                    for (int c = 0; c < B; ++c) val += jv[r * B + c] * x[p][c];
-                    b[r] -= val * fv[p];
+                        for (int c = 0; c < B; ++c) b[r] -= jv[r * B + c] * x[p][c];
+                    } else {
+                        S val = S(0);
+#pragma unroll
+                        for (int c = 0; c < B; ++c) val += jv[r * B + c] * x[p][c];
+                        b[r] -= val * fv[p];
+                    }
                 }
             }
         }
@@ -345,17 +364,22 @@ __global__ void __launch_bounds__(256) fs_blusgs_sweep_kernel(int t0, int t1, lo
         for (int p = 0; p < P; ++p) {
             const int nb = __ldcs(nei + p * N + k);
             if (nb < 0) break;
-            const S fv = __ldcs(fa + p * N + k) * rvk;
+            const S fv = kFold ? S(1) : __ldcs(fa + p * N + k) * rvk;
             S x[B];
 #pragma unroll
             for (int c = 0; c < B; ++c) x[c] = du[(var0 + c) * N + nb];
             const S *Jp = Jk + ((long long)p * B2 << 5);
 #pragma unroll
             for (int r = 0; r < B; ++r) {
-                S val = S(0);
+                if constexpr (kFold) {
 #pragma unroll
-                for (int c = 0; c < B; ++c) val += __ldcs(Jp + ((r * B + c) << 5)) * x[c];
-                b[r] -= val * fv;
+                    for (int c = 0; c < B; ++c) b[r] -= __ldcs(Jp + ((r * B + c) << 5)) * x[c];
+                } else {
+                    S val = S(0);
+#pragma unroll
+                    for (int c = 0; c < B; ++c) val += __ldcs(Jp + ((r * B + c) << 5)) * x[c];
+                    b[r] -= val * fv;
+                }
             }
         }
     }
@@ -363,7 +387,7 @@ __global__ void __launch_bounds__(256) fs_blusgs_sweep_kernel(int t0, int t1, lo
     const S *LUk = LU + ::ucfd::tile_index(k, 0, B2);
 #pragma unroll
     for (int e = 0; e < B2; ++e) lu[e] = __ldcs(LUk + (e << 5));
-    lusub_dev<S, B>(lu, b);
+    lusub_dev<S, B, kFold>(lu, b);
 #pragma unroll
     for (int r = 0; r < B; ++r) du[(var0 + r) * N + k] = b[r];
 }
@@ -391,11 +415,11 @@ __global__ void __launch_bounds__(128) fs_blusgs_sweep_small_kernel(int t0, int 
     int nb[PW];
 #pragma unroll
     for (int r = 0; r < B; ++r) b[r] = __ldcs(rhs + (var0 + r) * N + k);
-    const float rvk = rv[k];
+    const float rvk = kFold ? 1.f : rv[k];
 #pragma unroll
     for (int p = 0; p < PW; ++p) {
         nb[p] = __ldcs(nei + p * N + k);
-        fv[p] = __ldcs(fa + p * N + k) * rvk;
+        if constexpr (!kFold) fv[p] = __ldcs(fa + p * N + k) * rvk;
 #pragma unroll
         for (int e = 0; e < B2; ++e) jv[p][e] = __ldcs(Jk + ((p * B2 + e) << 5));
     }
@@ -414,14 +438,19 @@ __global__ void __launch_bounds__(128) fs_blusgs_sweep_small_kernel(int t0, int 
         if (nb[p] >= 0) {
 #pragma unroll
             for (int r = 0; r < B; ++r) {
-                float val = 0.f;
+                if constexpr (kFold) {
 #pragma unroll
-                for (int c = 0; c < B; ++c) val += jv[p][r * B + c] * x[p][c];
-                b[r] -= val * fv[p];
+                    for (int c = 0; c < B; ++c) b[r] -= jv[p][r * B + c] * x[p][c];
+                } else {
+                    float val = 0.f;
+#pragma unroll
+                    for (int c = 0; c < B; ++c) val += jv[p][r * B + c] * x[p][c];
+                    b[r] -= val * fv[p];
+                }
             }
         }
     }
-    lusub_dev<float, B>(lu, b);
+    lusub_dev<float, B, kFold>(lu, b);
 #pragma unroll
     for (int r = 0; r < B; ++r) du[(var0 + r) * N + k] = b[r];
 }
@@ -486,13 +515,13 @@ __global__ void __launch_bounds__(NST == 2 ? 128 : 256)
         float b[B];
 #pragma unroll
         for (int r = 0; r < B; ++r) b[r] = rhs[(var0 + r) * N + kk];
-        const float rvk = rv[kk];
+        const float rvk = kFold ? 1.f : rv[kk];
         int nb[PW];
         float fv[PW];
 #pragma unroll
         for (int p = 0; p < PW; ++p) {
             nb[p] = act ? __ldg(nei + p * N + kk) : -1;
-            fv[p] = __ldg(fa + p * N + kk) * rvk;
+            if constexpr (!kFold) fv[p] = __ldg(fa + p * N + kk) * rvk;
         }
         float x[PW][B];
 #pragma unroll
@@ -515,17 +544,22 @@ __global__ void __launch_bounds__(NST == 2 ? 128 : 256)
             if (nb[p] >= 0) {
 #pragma unroll
                 for (int r = 0; r < B; ++r) {
-                    float val = 0.f;
+                    if constexpr (kFold) {
 #pragma unroll
-                    for (int c = 0; c < B; ++c) val += sJ[(p * B2 + r * B + c) << 5] * x[p][c];
-                    b[r] -= val * fv[p];
+                        for (int c = 0; c < B; ++c) b[r] -= sJ[(p * B2 + r * B + c) << 5] * x[p][c];
+                    } else {
+                        float val = 0.f;
+#pragma unroll
+                        for (int c = 0; c < B; ++c) val += sJ[(p * B2 + r * B + c) << 5] * x[p][c];
+                        b[r] -= val * fv[p];
+                    }
                 }
             }
         }
         float lu[B2];
 #pragma unroll
         for (int e = 0; e < B2; ++e) lu[e] = sJ[JT + (e << 5)];
-        lusub_dev<float, B>(lu, b);
+        lusub_dev<float, B, kFold>(lu, b);
         if (act) {
 #pragma unroll
             for (int r = 0; r < B; ++r) du[(var0 + r) * N + k] = b[r];
@@ -536,6 +570,8 @@ __global__ void __launch_bounds__(NST == 2 ? 128 : 256)
 }
 
 // FP64 residual of the packed system: r = rhs - D x - sum_f J x_nb fv.
+// fa == nullptr: J64 holds the blocks already multiplied by fv (the FP64
+// fused multiply-add mode's sweep blocks), so r = rhs - D x - sum_f J x_nb.
 // Writes r (as R) when r_out != nullptr and accumulates per-block partial
 // sums of r^2 and rhs^2 into part[2*blockIdx.x + {0,1}].
 template <typename Sx, typename R, int B>
@@ -583,14 +619,15 @@ __global__ void fs_blusgs_residual_kernel(long long N, int P, int var0, int nvar
             for (int q = 0; q < PU; ++q) {
                 if (nbv[q] < 0) continue;
                 const int p = p0 + q;
-                const double fv = fa[p * N + k] * rv[k];
+                const double fv = fa ? fa[p * N + k] * rv[k] : 1.0;
 #pragma unroll
                 for (int r = 0; r < B; ++r) {
                     double val = 0.0;
 #pragma unroll
                     for (int c = 0; c < B; ++c)
                         val += J64[::ucfd::tile_index(k, (long long)p * B2 + r * B + c, (long long)P * B2)] * xn[q][c];
-                    res[r] -= val * fv;
+                    if (fa) res[r] -= val * fv;
+                    else res[r] -= val;
                 }
             }
         }

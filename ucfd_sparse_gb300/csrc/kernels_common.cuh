@@ -11,9 +11,23 @@
 #error "UCFD_KNS (kernel namespace) must be defined by the including translation unit"
 #endif
 
+#ifndef UCFD_KEXACT
+#define UCFD_KEXACT 0
+#endif
+
 namespace UCFD_KNS {
 
 constexpr int kBlock = 256;
+
+// Block LU-SGS storage of the two builds.  The exact build keeps the
+// reference's arithmetic: off-diagonal blocks J as given, each face's
+// product multiplied by fv = face_area * rcp_vol, LU pivots divided by.
+// The fast build (FP32 sweeps and the FP64 fused multiply-add mode) folds fv
+// into the stored sweep blocks (J fv, formed once per Prepare in FP64) and
+// stores reciprocal pivots in the LU diagonal, so a sweep does no division
+// and no per-face scaling, and reads no face areas; its block products go
+// straight into the right-hand side (one fused multiply-add per entry).
+constexpr bool kFold = !UCFD_KEXACT;
 
 __host__ __device__ inline unsigned grid_for(long long n, int block = kBlock) {
     long long g = (n + block - 1) / block;

@@ -69,6 +69,60 @@ __device__ __forceinline__ void rans_flux(const T *u, const T *nf, T *f) {
     for (int i = 0; i < NT; ++i) f[i] = u[NFV + i] * contrav;
 }
 
+// F(u + dn; n) - F(u; n) of ns_flux in difference form, for FP32: the
+// reference subtracts two whole fluxes (lusgs.c:143-155), which in single
+// precision cancels most of the digits when |dn| << |u| (an increment of
+// 1e-6 on a state of order 1 is below half an FP32 ulp of the energy).
+// With c = m.n / rho, ke = |m|^2 / (2 rho), p = (gamma - 1)(E - ke) and the
+// primed values at u + dn, the same difference is, exactly in real numbers,
+//   dc  = (dm.n - c drho) / rho',  dke = (m.dm + |dm|^2 / 2 - ke drho) / rho',
+//   dp  = (gamma - 1)(dE - dke),
+//   dF0 = dm.n,  dFi = dm_i c' + m_i dc + n_i dp,  dF4 = (dE + dp) c' + (E + p) dc,
+// each term formed from the increments themselves.  Where the pressure floor
+// acts on either state (p or p' below pmin, flux.c:51-56) the two fluxes
+// are subtracted as the reference does.
+template <int NFV, int NDIMS>
+__device__ __forceinline__ void ns_flux_diff(float gamma, float pmin, const float *u, const float *dn,
+                                             const float *nf, float *dfl) {
+    const float rho = u[0], drho = dn[0], rho1 = rho + drho;
+    const float E = u[NFV - 1], dE = dn[NFV - 1];
+    float mn = 0.f, dmn = 0.f, m2 = 0.f, mdm = 0.f, dm2 = 0.f;
+#pragma unroll
+    for (int i = 0; i < NDIMS; ++i) {
+        const float m = u[i + 1], dm = dn[i + 1];
+        mn += m * nf[i];
+        dmn += dm * nf[i];
+        m2 += m * m;
+        mdm += m * dm;
+        dm2 += dm * dm;
+    }
+    const float ir = __fdividef(1.f, rho), ir1 = __fdividef(1.f, rho1);
+    const float c = mn * ir;
+    const float dc = (dmn - c * drho) * ir1;
+    const float c1 = c + dc;
+    const float ke = 0.5f * m2 * ir;
+    const float dke = (mdm + 0.5f * dm2 - ke * drho) * ir1;
+    const float p = (gamma - 1.f) * (E - ke);
+    const float dp = (gamma - 1.f) * (dE - dke);
+    if (p < pmin || p + dp < pmin) {
+        float uu[NFV], u1[NFV], f0[NFV], f1[NFV];
+#pragma unroll
+        for (int v = 0; v < NFV; ++v) {
+            uu[v] = u[v];
+            u1[v] = u[v] + dn[v];
+        }
+        ns_flux<float, NFV, NDIMS>(gamma, pmin, uu, nf, f0);
+        ns_flux<float, NFV, NDIMS>(gamma, pmin, u1, nf, f1);
+#pragma unroll
+        for (int v = 0; v < NFV; ++v) dfl[v] = f1[v] - f0[v];
+        return;
+    }
+    dfl[0] = dmn;
+#pragma unroll
+    for (int i = 0; i < NDIMS; ++i) dfl[i + 1] = dn[i + 1] * c1 + u[i + 1] * dc + nf[i] * dp;
+    dfl[NFV - 1] = (dE + dp) * c1 + (E + p) * dc;
+}
+
 template <typename T>
 using ScalarSweepArgs = ::ucfd::ScalarSweepArgs<T>;
 
@@ -174,6 +228,60 @@ __device__ __forceinline__ unsigned active_faces(const ScalarSweepArgs<T> &a, in
     return m;
 }
 
+// One active face's term ((F(u+dn) - F(u)) - kappa lam dn) * fvk of
+// lusgs.c:143-205 (fvk = face area * rcp_vol), u the neighbour's state (only
+// the variables the flux reads need be set; the pressure floor may rewrite
+// u's energy), dn the neighbour's increment.  FP64 follows the reference's
+// operations (du += u before either flux); FP32 forms the flux difference in
+// difference form.  Every sweep kernel forms its terms here.
+template <typename T, int NV, int NFV, int NDIMS, bool RANS>
+__device__ __forceinline__ void face_term(const ScalarSweepArgs<T> &a, T *u, const T *dn, const T *nf, T fvk, T kl,
+                                          T *term) {
+    constexpr int NV0 = RANS ? NFV : 0;
+    constexpr int DNV = RANS ? NV - NFV : NFV;
+    T dfl[DNV];
+    if constexpr (sizeof(T) == 4) {
+        if constexpr (RANS) {
+            // only the turbulence variables move: dF_j = dn_j * m.n / rho
+            T mn = T(0);
+#pragma unroll
+            for (int d = 0; d < NDIMS; ++d) mn += u[d + 1] * nf[d];
+            const T c = div_sweep(mn, u[0]);
+#pragma unroll
+            for (int j = 0; j < DNV; ++j) dfl[j] = dn[j] * c;
+        } else {
+            ns_flux_diff<NFV, NDIMS>(a.gamma, a.pmin, u, dn, nf, dfl);
+        }
+    } else {
+        T du[NV], f0v[DNV], f1v[DNV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) du[v] = T(0);
+#pragma unroll
+        for (int j = 0; j < DNV; ++j) du[j + NV0] = dn[j];
+        // diff_flux: lusgs.c:143-155 (du += u before either flux)
+#pragma unroll
+        for (int v = 0; v < NV; ++v) du[v] += u[v];
+        if constexpr (RANS) {
+            rans_flux<T, NFV, NDIMS, NV - NFV>(u, nf, f0v);
+            rans_flux<T, NFV, NDIMS, NV - NFV>(du, nf, f1v);
+        } else {
+            ns_flux<T, NFV, NDIMS>(a.gamma, a.pmin, u, nf, f0v);
+            ns_flux<T, NFV, NDIMS>(a.gamma, a.pmin, du, nf, f1v);
+        }
+#pragma unroll
+        for (int j = 0; j < DNV; ++j) dfl[j] = f1v[j] - f0v[j];
+    }
+    const T klk = a.kappa * kl;
+#pragma unroll
+    for (int j = 0; j < DNV; ++j) term[j] = mul_rn(dfl[j] - klk * dn[j], fvk);
+}
+
+// Whether a flux of this kind reads state variable v of the neighbour.
+template <typename T, int NV, int NFV, int NDIMS, bool RANS>
+__device__ __forceinline__ constexpr bool flux_reads(int v) {
+    return RANS ? (v <= NDIMS || (v >= NFV && sizeof(T) == 8)) : (v < NFV);
+}
+
 // Terms of the next (up to) KB active faces of a cell, taken from the mask
 // m of its slots f0 + q (neighbours nb[q], NB slots) lowest slot first, so
 // the k-th term is that of the k-th active face in face order; the faces
@@ -214,8 +322,7 @@ __device__ __forceinline__ int face_terms(const ScalarSweepArgs<T> &a, int i, T 
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
             // only the variables the flux reads are loaded
-            const bool need = RANS ? (v <= NDIMS || v >= NFV) : (v < NFV);
-            uu[k][v] = need ? __ldg(a.u + v * ld + g) : T(0);
+            uu[k][v] = flux_reads<T, NV, NFV, NDIMS, RANS>(v) ? __ldg(a.u + v * ld + g) : T(0);
         }
 #pragma unroll
         for (int j = 0; j < DNV; ++j)
@@ -231,30 +338,13 @@ __device__ __forceinline__ int face_terms(const ScalarSweepArgs<T> &a, int i, T 
     for (int k = 0; k < KB; ++k) {
         if (!on[k]) continue;
         ++n;
-        T *u = uu[k];
-        T du[NV], f0v[DNV], f1v[DNV];
-#pragma unroll
-        for (int v = 0; v < NV; ++v) du[v] = T(0);
-#pragma unroll
-        for (int j = 0; j < DNV; ++j) du[j + NV0] = dn[k][j];
         const T fvk = a.rv ? fv[k] * rvi : fv[k];
-        // diff_flux: lusgs.c:143-155 (du += u before either flux)
-#pragma unroll
-        for (int v = 0; v < NV; ++v) du[v] += u[v];
-        if constexpr (RANS) {
-            rans_flux<T, NFV, NDIMS, NV - NFV>(u, nf[k], f0v);
-            rans_flux<T, NFV, NDIMS, NV - NFV>(du, nf[k], f1v);
-        } else {
-            ns_flux<T, NFV, NDIMS>(a.gamma, a.pmin, u, nf[k], f0v);
-            ns_flux<T, NFV, NDIMS>(a.gamma, a.pmin, du, nf[k], f1v);
-        }
-        const T klk = a.kappa * kl[k];
+        T term[DNV];
+        face_term<T, NV, NFV, NDIMS, RANS>(a, uu[k], dn[k], nf[k], fvk, kl[k], term);
 #pragma unroll
         for (int j = 0; j < DNV; ++j) {
-            const T dfj = f1v[j] - f0v[j];
-            const T term = mul_rn(dfj - klk * dn[k][j], fvk);
-            if constexpr (ACC) df[j] += term;
-            else c[k][j] = term;
+            if constexpr (ACC) df[j] += term[j];
+            else c[k][j] = term[j];
         }
     }
     return n;
@@ -315,6 +405,88 @@ __device__ __forceinline__ void scalar_sweep_cell(const ScalarSweepArgs<T> &a, i
     }
 #pragma unroll
     for (int k = 0; k < DNV; ++k) a.own_out[(k + NV0) * ld + i] = sweep_result(a.upper != 0, own[k], df[k], dg[k]);
+}
+
+// One level of the sweep with one thread per active face.  A block owns
+// a.cpb consecutive cells of the level; their active faces are consecutive
+// entries of the face list.  Every thread forms the terms of the entries
+// e0 + tid, e0 + tid + blockDim, ... (neighbour gathers and two flux
+// evaluations each, all independent), parks them in shared memory, and
+// after the barrier the first a.cpb threads add their cell's terms in face
+// order and write the cell: the terms and their order are those of
+// scalar_sweep_cell.  Each thread holds one face's data instead of a whole
+// cell's, so many more warps fit to cover the gathers' latency, and no lane
+// idles on a face that is active for a neighbouring cell only.
+template <typename T, int NV, int NFV, int NDIMS, bool RANS>
+__global__ void __launch_bounds__(256) scalar_sweep_faces_kernel(ScalarSweepArgs<T> a) {
+    constexpr int NV0 = RANS ? NFV : 0;
+    constexpr int DNV = RANS ? NV - NFV : NFV;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *terms = reinterpret_cast<T *>(smem_raw);
+    const long long ld = a.ld;
+    const int c0 = a.t0 + blockIdx.x * a.cpb;
+    const int c1 = min(a.t1, c0 + a.cpb);
+    const int e0 = __ldg(a.fl_off + c0), e1 = __ldg(a.fl_off + c1);
+    const int k = c0 + (int)threadIdx.x;
+    const bool owner = (int)threadIdx.x < a.cpb && k < c1;
+    T own[DNV], dg[DNV];
+    int f0 = 0, f1 = 0;
+    if (owner) {
+#pragma unroll
+        for (int j = 0; j < DNV; ++j) {
+            own[j] = a.own_in[(j + NV0) * ld + k];
+            dg[j] = a.diag[(j + NV0) * a.diag_vs + k];
+        }
+        f0 = __ldg(a.fl_off + k);
+        f1 = __ldg(a.fl_off + k + 1);
+    }
+    for (int e = e0 + (int)threadIdx.x; e < e1; e += blockDim.x) {
+        const int g = __ldcs(a.fl_nb + e);
+        T geo[4];
+        if constexpr (sizeof(T) == 4) {
+            const float4 v = __ldcs(reinterpret_cast<const float4 *>(a.fl_geo) + e);
+            geo[0] = v.x, geo[1] = v.y, geo[2] = v.z, geo[3] = v.w;
+        } else {
+            const double2 v0 = __ldcs(reinterpret_cast<const double2 *>(a.fl_geo) + 2 * (long long)e);
+            const double2 v1 = __ldcs(reinterpret_cast<const double2 *>(a.fl_geo) + 2 * (long long)e + 1);
+            geo[0] = v0.x, geo[1] = v0.y, geo[2] = v1.x, geo[3] = v1.y;
+        }
+        const T kl = __ldg(a.lam + __ldcs(a.fl_q + e));
+        T u[NV], dn[DNV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) u[v] = flux_reads<T, NV, NFV, NDIMS, RANS>(v) ? __ldg(a.u + v * ld + g) : T(0);
+#pragma unroll
+        for (int j = 0; j < DNV; ++j) dn[j] = a.nbsrc[(j + NV0) * ld + g];
+        T term[DNV];
+        face_term<T, NV, NFV, NDIMS, RANS>(a, u, dn, geo, geo[3], kl, term);
+#pragma unroll
+        for (int j = 0; j < DNV; ++j) terms[(e - e0) * DNV + j] = term[j];
+    }
+    __syncthreads();
+    if (!owner) return;
+    T df[DNV];
+#pragma unroll
+    for (int j = 0; j < DNV; ++j) df[j] = T(0);
+    for (int e = f0; e < f1; ++e)
+#pragma unroll
+        for (int j = 0; j < DNV; ++j) df[j] += terms[(e - e0) * DNV + j];
+#pragma unroll
+    for (int j = 0; j < DNV; ++j) a.own_out[(j + NV0) * ld + k] = sweep_result(a.upper != 0, own[j], df[j], dg[j]);
+}
+
+// Face list geometry: per entry the outward normal of its ELL slot q
+// (nrm [nface][ndims][ld], zero-padded to 3 components) and fa * rv, the
+// same product the per-cell kernels form.
+template <typename T>
+__global__ void face_list_geo_kernel(long long E, long long ld, int ndims, const int *q, const T *nrm, const T *fa,
+                                     const T *rv, T *geo) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < E;
+         e += (long long)gridDim.x * blockDim.x) {
+        const long long qq = q[e];
+        const long long p = qq / ld, k = qq - p * ld;
+        for (int d = 0; d < 3; ++d) geo[4 * e + d] = d < ndims ? nrm[(p * ndims + d) * ld + k] : T(0);
+        geo[4 * e + 3] = rv ? fa[qq] * rv[k] : fa[qq];
+    }
 }
 
 // Two threads per cell (ELL width <= 6, level-major or coloured): the even

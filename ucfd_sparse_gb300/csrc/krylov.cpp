@@ -321,7 +321,7 @@ struct _Precon {
         }
         if (kind != 0) {
             factorize(vd, s);
-            if (!vdev) UCFD_CUDA(cudaMemcpyAsync(values, vd, nv * sizeof(double), cudaMemcpyDeviceToHost, s));
+            if (!vdev) copy_d2h(values, vd, nv * sizeof(double), s);
         }
         L.gather(vd, !fp32, fp32, s);
         U.gather(vd, !fp32, fp32, s);
@@ -664,7 +664,7 @@ static ucfd_status_t mat_mult(UCFDReal alpha, SpMat mat, UCFDReal *x, UCFDReal b
     double *yd = ydev ? y : const_cast<double *>(device_view<double>(y, n, mat->sy, s));
     mat->mult(alpha, xd, beta, yd, fp32 ? UCFD_PREC_FP32 : UCFD_PREC_FP64, s);
     UCFD_CHECK_LAUNCH();
-    if (!ydev) UCFD_CUDA(cudaMemcpyAsync(y, yd, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (!ydev) copy_d2h(y, yd, n * sizeof(double), s);
     UCFD_CUDA(cudaStreamSynchronize(s));
     UCFD_API_END
 }
@@ -797,7 +797,7 @@ ucfd_status_t UCFDPreconApply(Precon pc, UCFDReal *b) {
     double *bd = dev ? b : const_cast<double *>(device_view<double>(b, n, pc->stage_b, s));
     pc->apply(bd, s);
     UCFD_CHECK_LAUNCH();
-    if (!dev) UCFD_CUDA(cudaMemcpyAsync(b, bd, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (!dev) copy_d2h(b, bd, n * sizeof(double), s);
     UCFD_CUDA(cudaStreamSynchronize(s));
     UCFD_API_END
 }
@@ -891,7 +891,7 @@ ucfd_status_t UCFDSolve(Solver solver, Precon pc, SpMat A, UCFDReal *x, UCFDReal
     double *xd = xdev ? x : const_cast<double *>(device_view<double>(x, n, solver->sx, s));
     const double *bd = device_view<double>(b, n, solver->sb, s);
     solver->solve(A, pc, xd, bd, s);
-    if (!xdev) UCFD_CUDA(cudaMemcpyAsync(x, xd, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (!xdev) copy_d2h(x, xd, n * sizeof(double), s);
     UCFD_CUDA(cudaStreamSynchronize(s));
     UCFD_API_END
 }

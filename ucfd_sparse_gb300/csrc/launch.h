@@ -23,6 +23,9 @@
                                  int rans, const int *lev_off, int nlev, unsigned *bar, int *err,  \
                                  long long max_spin, cudaStream_t s);                              \
     template <typename T>                                                                          \
+    void face_list_geo(long long E, long long ld, int ndims, const int *q, const T *nrm,           \
+                       const T *fa, const T *rv, T *geo, cudaStream_t s);                          \
+    template <typename T>                                                                          \
     void legacy_pre(int neles, int nface, T factor, const T *fnorm_vol, const T *dt, T *diag,      \
                     const T *fspr, cudaStream_t s);                                                \
     template <typename T>                                                                          \

@@ -45,10 +45,28 @@ void adj_lower(const ::ucfd::AdjArgs &a, int nfv, int ndims, T gamma, T pmin, T 
 }
 
 // ---- scalar LU-SGS ---------------------------------------------------------
+template <typename T>
+void face_list_geo(long long E, long long ld, int ndims, const int *q, const T *nrm, const T *fa, const T *rv,
+                   T *geo, cudaStream_t s) {
+    if (E <= 0) return;
+    const long long g = (E + kBlock - 1) / kBlock;
+    face_list_geo_kernel<T><<<(unsigned)(g < 65535 * 16 ? g : 65535 * 16), kBlock, 0, s>>>(E, ld, ndims, q, nrm, fa,
+                                                                                          rv, geo);
+}
+
 template <typename T, int NV, int NFV, int NDIMS, bool RANS>
 static void sweep_go(const ::ucfd::ScalarSweepArgs<T> &a, int block, cudaStream_t s) {
     const long long n = a.t1 - a.t0;
     if (n <= 0) return;
+    if (a.facelist) {
+        constexpr int DNV = RANS ? NV - NFV : NFV;
+        ::ucfd::ScalarSweepArgs<T> b = a;
+        if (b.cpb <= 0 || b.cpb > block) b.cpb = block / 3 > 0 ? block / 3 : 1;
+        const size_t smem = (size_t)b.cpb * (a.nface > 0 ? a.nface : 1) * DNV * sizeof(T);
+        if (smem > 48 * 1024) ::ucfd::fail(UCFD_ERR_UNSUPPORTED, "face-list sweep: %zu bytes of shared memory", smem);
+        scalar_sweep_faces_kernel<T, NV, NFV, NDIMS, RANS><<<grid_for(n, b.cpb), block, smem, s>>>(b);
+        return;
+    }
     if (a.pair && a.nface <= 6) {
         if (a.regcap == 4)
             scalar_sweep_pair_kernel<T, NV, NFV, NDIMS, RANS, 4><<<grid_for(2 * n, block), block, 0, s>>>(a);

@@ -68,7 +68,7 @@ Arr<T> stage(T *p, size_t count, DevBuf<T> &buf, cudaStream_t s) {
 template <typename T>
 void writeback(const Arr<T> &a, cudaStream_t s) {
     if (a.host && a.count)
-        UCFD_CUDA(cudaMemcpyAsync(a.user, a.dev, a.count * sizeof(T), cudaMemcpyDeviceToHost, s));
+        copy_d2h(a.user, a.dev, a.count * sizeof(T), s);
 }
 
 void done(cudaStream_t s) {

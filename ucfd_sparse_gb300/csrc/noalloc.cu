@@ -83,7 +83,8 @@ __device__ inline double warp_block_sum(double v, double *sh) {
 }
 
 // Grid-stride variant of the FP64 residual kernel: per cell
-// r = rhs - D x - sum_f J x_nb fv (same per-cell arithmetic), per block the
+// r = rhs - D x - sum_f J x_nb fv (same per-cell arithmetic; fa == nullptr:
+// the blocks already carry fv), per block the
 // partial sums of r^2 and rhs^2 go to scratch[2 b], scratch[2 b + 1].
 template <typename Sx, int B>
 __global__ void __launch_bounds__(kThreads) residual_noalloc_kernel(long long N, int P, const int *nei,
@@ -110,7 +111,7 @@ __global__ void __launch_bounds__(kThreads) residual_noalloc_kernel(long long N,
         for (int p = 0; p < P; ++p) {
             const int nb = nei[p * N + k];
             if (nb < 0) break;
-            const double fv = fa[p * N + k] * rv[k];
+            const double fv = fa ? fa[p * N + k] * rv[k] : 1.0;
             double xn[B];
 #pragma unroll
             for (int c = 0; c < B; ++c) xn[c] = (double)x[c * N + nb];
@@ -120,7 +121,8 @@ __global__ void __launch_bounds__(kThreads) residual_noalloc_kernel(long long N,
 #pragma unroll
                 for (int c = 0; c < B; ++c)
                     val += J64[::ucfd::tile_index(k, (long long)p * B2 + r * B + c, (long long)P * B2)] * xn[c];
-                res[r] -= val * fv;
+                if (fa) res[r] -= val * fv;
+                else res[r] -= val;
             }
         }
 #pragma unroll

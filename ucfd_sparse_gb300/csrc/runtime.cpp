@@ -29,6 +29,53 @@ void fail(ucfd_status_t st, const char *fmt, ...) {
     throw Error{st};
 }
 
+// ---- timed host<->device copies (UCFDSetTransferTiming) ------------------
+namespace {
+std::mutex g_xfer_mu;
+bool g_xfer_on = false;
+UCFDTransferStats g_xfer{};
+
+void timed_copy(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind, cudaStream_t s) {
+    bool on;
+    {
+        std::lock_guard<std::mutex> lk(g_xfer_mu);
+        on = g_xfer_on;
+    }
+    if (!on) {
+        UCFD_CUDA(cudaMemcpyAsync(dst, src, bytes, kind, s));
+        return;
+    }
+    thread_local cudaEvent_t ev[2] = {nullptr, nullptr};
+    if (!ev[0]) {
+        UCFD_CUDA(cudaEventCreate(&ev[0]));
+        UCFD_CUDA(cudaEventCreate(&ev[1]));
+    }
+    UCFD_CUDA(cudaEventRecord(ev[0], s));
+    UCFD_CUDA(cudaMemcpyAsync(dst, src, bytes, kind, s));
+    UCFD_CUDA(cudaEventRecord(ev[1], s));
+    UCFD_CUDA(cudaEventSynchronize(ev[1]));
+    float ms = 0.f;
+    UCFD_CUDA(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+    std::lock_guard<std::mutex> lk(g_xfer_mu);
+    if (kind == cudaMemcpyHostToDevice) {
+        g_xfer.h2d_ms += ms;
+        g_xfer.h2d_bytes += (double)bytes;
+        g_xfer.h2d_copies++;
+    } else {
+        g_xfer.d2h_ms += ms;
+        g_xfer.d2h_bytes += (double)bytes;
+        g_xfer.d2h_copies++;
+    }
+}
+}  // namespace
+
+void copy_h2d(void *dst, const void *src, size_t bytes, cudaStream_t s) {
+    timed_copy(dst, src, bytes, cudaMemcpyHostToDevice, s);
+}
+void copy_d2h(void *dst, const void *src, size_t bytes, cudaStream_t s) {
+    timed_copy(dst, src, bytes, cudaMemcpyDeviceToHost, s);
+}
+
 static std::once_flag g_dev_once;
 static int g_sm_count = 0;
 static cudaError_t g_dev_err = cudaSuccess;
@@ -78,6 +125,22 @@ ucfd_status_t UCFDSetConstants(UCFDReal gamma, UCFDReal pmin, UCFDReal betast) {
     ucfd::constants().gamma = gamma;
     ucfd::constants().pmin = pmin;
     ucfd::constants().betast = betast;
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDSetTransferTiming(int on) {
+    UCFD_API_BEGIN
+    std::lock_guard<std::mutex> lk(ucfd::g_xfer_mu);
+    if (on) ucfd::g_xfer = UCFDTransferStats{};
+    ucfd::g_xfer_on = on != 0;
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDGetTransferStats(UCFDTransferStats *stats) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(stats, "UCFDGetTransferStats: null argument");
+    std::lock_guard<std::mutex> lk(ucfd::g_xfer_mu);
+    *stats = ucfd::g_xfer;
     UCFD_API_END
 }
 

@@ -50,6 +50,11 @@ inline void cuda_check(cudaError_t e, const char *what, const char *file, int li
 
 // ---- device buffers ---------------------------------------------------------
 // Owning, growable device allocation.  Never shrinks; realloc discards data.
+// Host -> device / device -> host copy of `bytes` on stream s
+// (cudaMemcpyAsync), counted and, while UCFDSetTransferTiming is on, timed.
+void copy_h2d(void *dst, const void *src, size_t bytes, cudaStream_t s);
+void copy_d2h(void *dst, const void *src, size_t bytes, cudaStream_t s);
+
 template <typename T>
 struct DevBuf {
     T *p = nullptr;
@@ -92,7 +97,7 @@ struct DevBuf {
     }
     void upload(const T *host, size_t count, cudaStream_t s) {
         ensure(count);
-        if (count) UCFD_CUDA(cudaMemcpyAsync(p, host, count * sizeof(T), cudaMemcpyHostToDevice, s));
+        if (count) copy_h2d(p, host, count * sizeof(T), s);
     }
     void zero(size_t count, cudaStream_t s) {
         ensure(count);

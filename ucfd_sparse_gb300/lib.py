@@ -21,6 +21,27 @@ LIB_PATH = os.path.join(HERE, "lib", "libucfd_gb300.so")
 _I, _D, _P = c_int, c_double, c_void_p
 
 
+class TransferStats(ctypes.Structure):
+    """``UCFDTransferStats`` of ucfd_gb300.h."""
+
+    _fields_ = [("h2d_ms", c_double), ("h2d_bytes", c_double), ("d2h_ms", c_double), ("d2h_bytes", c_double),
+                ("h2d_copies", ctypes.c_longlong), ("d2h_copies", ctypes.c_longlong)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def transfer_timing(on: bool) -> None:
+    """Start (clearing the counters) or stop timing the library's host<->device copies."""
+    call("UCFDSetTransferTiming", 1 if on else 0)
+
+
+def transfer_stats() -> dict:
+    st = TransferStats()
+    call("UCFDGetTransferStats", ctypes.addressof(st))
+    return st.as_dict()
+
+
 class LaunchConfig(ctypes.Structure):
     """``UCFDLaunchConfig`` of ucfdlusgs.h."""
 
@@ -39,6 +60,8 @@ SIGNATURES = {
     "UCFDVersion": (c_char_p, []),
     "UCFDDeviceInfo": (_I, [c_char_p, c_size_t, POINTER(c_int)]),
     "UCFDSelfTestTimeouts": (_I, [POINTER(c_int), POINTER(c_int)]),
+    "UCFDSetTransferTiming": (_I, [_I]),
+    "UCFDGetTransferStats": (_I, [_P]),
     # ucfdmesh.h
     "UCFDMakeNeiEle": (_I, [_I, _I, _I, _P]),
     "UCFDMakeColoring": (_I, [_I, _I, _I, _P]),
