@@ -1198,7 +1198,9 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mesh", type=int, default=128)
+    ap.add_argument("--mesh", type=int, default=None,
+                    help="box size (default per workload: blusgs/kernels 128, lusgs 256, gmres 96, colored 32, "
+                         "adjoint 64)")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--rtol", type=float, default=1e-10)
     ap.add_argument("--inner", type=int, default=20, help="FP32 sweep pairs per FP64 refinement step")
@@ -1223,6 +1225,8 @@ def main(argv=None):
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3
+    if args.mesh is None:
+        args.mesh = {"lusgs": 256, "gmres": 96, "colored": 32, "adjoint": 64}.get(args.workload, 128)
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "lusgs":

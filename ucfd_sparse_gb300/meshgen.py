@@ -407,14 +407,15 @@ def kuhn_tet_adjacency(m: int):
             nodes[:, t, k] = (hx + off[0]) + nn * ((hy + off[1]) + nn * (hz + off[2]))
     nodes = nodes.reshape(-1, 4)
     ncell = nodes.shape[0]
-    keys = np.empty((ncell, 4), dtype=np.int64)
+    # each tet face as its sorted node triple, cell-major (tet, face k);
+    # faces shared by two tets are equal triples, adjacent once sorted
+    tris = np.empty((ncell, 4, 3), dtype=np.int64)
     for k in range(4):
-        tri = np.sort(np.delete(nodes, k, axis=1), axis=1)
-        keys[:, k] = (tri[:, 0] << 42) | (tri[:, 1] << 21) | tri[:, 2]
-    flat = keys.ravel()
-    order = np.argsort(flat, kind='stable')
-    sk = flat[order]
-    same = sk[1:] == sk[:-1]
+        tris[:, k] = np.sort(np.delete(nodes, k, axis=1), axis=1)
+    tris = tris.reshape(-1, 3)
+    order = np.lexsort((tris[:, 2], tris[:, 1], tris[:, 0]))
+    st = tris[order]
+    same = np.all(st[1:] == st[:-1], axis=1)
     i0 = order[:-1][same]
     i1 = order[1:][same]
     nei = -np.ones(ncell * 4, dtype=np.int64)
