@@ -206,20 +206,29 @@ class Problem:
         cfg.pop("source", None)
         return cfg
 
-    def step(self, rtol, max_pairs, inner, calls=None):
+    def step(self, rtol, max_pairs, inner, calls=None, copies=None):
         """One pseudo-time step; with `calls` (a dict) the host wall time of
         each C-ABI call is added to it (the calls on host inputs are
-        synchronous, so this is each call's whole cost)."""
+        synchronous, so this is each call's whole cost); with `copies` (a
+        dict, transfer timing on) each call's timed host<->device copy
+        milliseconds."""
+        from ucfd_sparse_gb300 import lib as _lib
         S = self.S
         steps = (("pack", lambda: S.blusgs_pack(0, 0.0)), ("prepare", S.blusgs_ns_prepare),
                  ("reset", S.blusgs_reset), ("solve", lambda: S.blusgs_solve(rtol, max_pairs, inner)),
                  ("update", lambda: S.blusgs_update(0)))
         out = None
         for name, f in steps:
+            x0 = _lib.transfer_stats() if copies is not None else None
             t = time.perf_counter()
             r = f()
             if calls is not None:
                 calls[name] = calls.get(name, 0.0) + time.perf_counter() - t
+            if copies is not None:
+                x1 = _lib.transfer_stats()
+                c = copies.setdefault(name, {"h2d_ms": 0.0, "h2d_bytes": 0.0, "d2h_ms": 0.0, "d2h_bytes": 0.0})
+                for k in c:
+                    c[k] += x1[k] - x0[k]
             if name == "solve":
                 out = r
         return out
@@ -566,26 +575,37 @@ def run_gpu(args):
     torch.cuda.synchronize()
     e2e_s = reduce_max((time.perf_counter() - t0) / args.steps, dist, device)
     # the same steps again with the library's host<->device copies timed by
-    # CUDA events (each timed copy waits for itself, so these steps are not
-    # the ones above): where the time of the host-input calls goes
+    # CUDA events (each timed copy waits for itself), then once more untimed:
+    # where the time of the host-input calls goes, and whether the host link
+    # changed speed meanwhile
     from ucfd_sparse_gb300 import lib as _lib
-    xfer_calls = {}
+    xfer_calls, xfer_copies = {}, {}
     _lib.transfer_timing(True)
     t1 = time.perf_counter()
     for _ in range(args.steps):
-        Ph.step(args.rtol, args.max_pairs, args.inner, xfer_calls)
+        Ph.step(args.rtol, args.max_pairs, args.inner, xfer_calls, xfer_copies)
     torch.cuda.synchronize()
     xfer_s = (time.perf_counter() - t1) / args.steps
     xfer = _lib.transfer_stats()
     _lib.transfer_timing(False)
-    xfer_out = {"ms_per_step": xfer_s * 1e3,
-                "h2d_ms_per_step": xfer["h2d_ms"] / args.steps,
-                "h2d_bytes_per_step": xfer["h2d_bytes"] / args.steps,
+    t2 = time.perf_counter()
+    for _ in range(args.steps):
+        Ph.step(args.rtol, args.max_pairs, args.inner)
+    torch.cuda.synchronize()
+    again_s = (time.perf_counter() - t2) / args.steps
+    K = args.steps
+    xfer_out = {"ms_per_step": xfer_s * 1e3, "untimed_again_ms_per_step": again_s * 1e3,
+                "h2d_ms_per_step": xfer["h2d_ms"] / K,
+                "h2d_bytes_per_step": xfer["h2d_bytes"] / K,
                 "h2d_GBps": xfer["h2d_bytes"] / max(xfer["h2d_ms"], 1e-9) / 1e6,
-                "d2h_ms_per_step": xfer["d2h_ms"] / args.steps,
-                "d2h_bytes_per_step": xfer["d2h_bytes"] / args.steps,
-                "ms_per_call": {k: v * 1e3 / args.steps for k, v in xfer_calls.items()},
-                "how": "CUDA events around every host<->device copy the library makes, same steps repeated"}
+                "d2h_ms_per_step": xfer["d2h_ms"] / K,
+                "d2h_bytes_per_step": xfer["d2h_bytes"] / K,
+                "ms_per_call": {k: v * 1e3 / K for k, v in xfer_calls.items()},
+                "copies_per_call": {k: {"h2d_ms": v["h2d_ms"] / K, "h2d_MB": v["h2d_bytes"] / K / 1e6,
+                                        "d2h_ms": v["d2h_ms"] / K, "d2h_MB": v["d2h_bytes"] / K / 1e6}
+                                    for k, v in xfer_copies.items()},
+                "how": "CUDA events around every host<->device copy the library makes, the same steps repeated; "
+                       "then the steps once more without timing"}
     # the same pinned jmat copied alone (torch copy, one transfer): the host link's rate for it
     jdev = torch.empty(Ph.e["jmat"].shape, dtype=Ph.e["jmat"].dtype, device=device)
     torch.cuda.synchronize()
@@ -690,7 +710,10 @@ def run_lusgs(args):
                       torch.zeros_like(uu))
         S.set_lusgs(g["fspr"], g["tfspr"])
         S.lusgs_pack(0, 1.0, 0.0)
-        if not args.no_autotune:
+        if args.sweep_variant is not None:
+            S.set_launch_config(threads_per_block=256, sweep_variant=args.sweep_variant, run_mode=mode)
+            res.setdefault("launch", S.launch_config())
+        elif not args.no_autotune:
             tuned = S.autotune(reps=2, cache=args.autotune_cache)  # block size x register build (state restored)
             tuned.pop("source", None)
             res.setdefault("launch", tuned)
@@ -942,20 +965,49 @@ def run_gmres(args):
                             prepare_ms=reprep_ms)
         del pc, sv, pvals
         torch.cuda.empty_cache()
-    # SpMV kernel alone (FP64 and FP32 values)
+    # SpMV kernel alone: FP64 in the reference's order, FP64 with fused
+    # multiply-adds, FP32 values; beside them the reference's own GPU kernel
+    # (_SpMV_CUDABSR<5>, cusparsemat.cu:74-139) compiled from its source
+    from ucfd_sparse_gb300.lib import PREC_FP32, PREC_FP64, PREC_FP64_FMA
     x = torch.randn(n, dtype=torch.float64, device=dev)
     y = torch.zeros(n, dtype=torch.float64, device=dev)
     sp = {}
-    for fp32 in (False, True):
-        A.mult(1.0, x, 0.0, y, fp32=fp32)
+    for prec in (PREC_FP64, PREC_FP64_FMA, PREC_FP32):
+        A.mult(1.0, x, 0.0, y, precision=prec)
         torch.cuda.synchronize()
         t = time.perf_counter()
         for _ in range(20):
-            A.mult(1.0, x, 0.0, y, fp32=fp32)
+            A.mult(1.0, x, 0.0, y, precision=prec)
         torch.cuda.synchronize()
-        sp[fp32] = (time.perf_counter() - t) / 20 * 1e3
+        sp[prec] = (time.perf_counter() - t) / 20 * 1e3
+    sp[False], sp[True] = sp[PREC_FP64], sp[PREC_FP32]
     b64 = nnzb * (4 + 25 * 8) + bn * (40 + 40)
     b32 = nnzb * (4 + 25 * 4) + bn * (40 + 40)
+    ref_spmv = None
+    from oracle import oracle as orc
+    if orc.ref_cuda_available():
+        R = orc.RefCudaBSR(5)
+        cs = torch.cuda.current_stream(dev)
+        yr = torch.zeros_like(y)
+        launch = lambda: R.spmv(1.0, bn, d["rowptr"].data_ptr(), d["colidx"].data_ptr(), d["values"].data_ptr(),
+                                x.data_ptr(), 0.0, yr.data_ptr(), cs.cuda_stream)
+        launch()
+        torch.cuda.synchronize()
+        e0, e1 = _events(cs)
+        e0.record(cs)
+        for _ in range(20):
+            launch()
+        e1.record(cs)
+        torch.cuda.synchronize()
+        ref_ms = e0.elapsed_time(e1) / 20
+        A.mult(1.0, x, 0.0, y, precision=PREC_FP64_FMA)
+        agree = float((yr - y).abs().max() / y.abs().max())
+        R.close()
+        ref_spmv = {"kernel": "_SpMV_CUDABSR<5> of cusparsemat.cu, built from the reference source for sm_103a "
+                              "(oracle/Makefile), launched as its SpMV_CUDABSR (128 threads, one per block row)",
+                    "ms": ref_ms, "GBps": b64 / (ref_ms * 1e-3) / 1e9, "frac": b64 / (ref_ms * 1e-3) / 1e9 / peak,
+                    "speedup_of_fp64_fma": ref_ms / sp[PREC_FP64_FMA], "speedup_of_fp64": ref_ms / sp[PREC_FP64],
+                    "max_rel_diff_vs_fp64_fma": agree}
     out = {"workload": "gmres", "unit": "s to 1e-10",
            "config": {"workload": f"GMRES(30) + coloured BLU-SGS, Kuhn tets of a {args.mesh}^3 box ({bn} cells, "
                                   f"5x5 BSR, {nnzb} blocks), {len(rg)} colours, tol 1e-10 relative", "cells": bn},
@@ -963,10 +1015,13 @@ def run_gmres(args):
            "err_vs_fp64": res[2]["err_vs_fp64"],
            "err_definition": "max|x - x_fp64| / max|x_fp64|, x_fp64 the GMRES solution with UCFD_PREC_FP64 "
                              "(the oracle's arithmetic) to the same tolerance",
-           "spmv": {"fp64_ms": sp[False], "fp32_ms": sp[True],
+           "spmv": {"fp64_ms": sp[False], "fp32_ms": sp[True], "fp64_fma_ms": sp[PREC_FP64_FMA],
                     "fp64_GBps": b64 / (sp[False] * 1e-3) / 1e9, "fp32_GBps": b32 / (sp[True] * 1e-3) / 1e9,
+                    "fp64_fma_GBps": b64 / (sp[PREC_FP64_FMA] * 1e-3) / 1e9,
                     "peak": peak, "fp64_frac": b64 / (sp[False] * 1e-3) / 1e9 / peak,
-                    "fp32_frac": b32 / (sp[True] * 1e-3) / 1e9 / peak},
+                    "fp64_fma_frac": b64 / (sp[PREC_FP64_FMA] * 1e-3) / 1e9 / peak,
+                    "fp32_frac": b32 / (sp[True] * 1e-3) / 1e9 / peak,
+                    "reference_gpu_kernel": ref_spmv},
            "bicgstab_fp64": bic,
            "generation_s": gen_s}
     del A, d, x, y
@@ -1132,9 +1187,15 @@ def run_kernels(args):
     ic, rg, lc = cl.greedy_coloring_csr(case["rowptr"], case["colidx"], order=args.coloring)
     device = torch.device("cuda", 0)
     stream = torch.cuda.Stream(device=device)
-    P = Problem(case, lc, 2, stream, device)
+    prec = 1 if args.fp64 else 2
+    P = Problem(case, lc, prec, stream, device)
     S = P.S
     tuned = P.tune(cache=args.autotune_cache) if not args.no_autotune else None
+    if args.sweep_variant is not None:
+        S.blusgs_pack(0, 0.0)
+        S.blusgs_ns_prepare()
+        S.set_launch_config(threads_per_block=256, sweep_variant=args.sweep_variant)
+        tuned = S.launch_config()
     S.blusgs_reset()
 
     def timed(fn, reps):
@@ -1159,9 +1220,15 @@ def run_kernels(args):
 
     reps = max(args.steps, 3)
     prep_ms = timed(prep, reps)
-    # every launch candidate of the sweep, then the tuned one
+    # every launch candidate of the sweep (unless one variant was asked
+    # for), then the chosen one
     candidates = {}
-    for tpb, var in ((64, 0), (128, 0), (256, 0), (64, 1), (256, 1), (0, 2), (0, 3), (64, 4), (128, 4), (256, 4)):
+    cand_list = ((64, 0), (128, 0), (256, 0), (64, 1), (256, 1), (0, 2), (0, 3), (64, 4), (128, 4), (256, 4))
+    if args.sweep_variant is not None:
+        cand_list = ()
+    for tpb, var in cand_list:
+        if prec != 2 and var in (2, 3):
+            continue                      # bulk-copy kernels are FP32-only
         S.set_launch_config(threads_per_block=tpb, sweep_variant=var)
         candidates[f"v{var}/b{tpb}"] = timed(pair, max(10, 2 * reps))
     if tuned:
@@ -1174,13 +1241,15 @@ def run_kernels(args):
     peak = float(peaks.get("hbm_gbs", 6800.0))
     nnz = int(case["rowptr"][-1])
     nF = int(case["nfaces"])
-    sw = 2 * sweep_bytes(case["rowptr"], 4, 5, 4)
+    elt = 8 if prec != 2 else 4
+    sw = 2 * sweep_bytes(case["rowptr"], elt, 5, elt)
     # Prepare: jmat read twice (transpose in, face records out) + written once,
     # face records read per cell-face, J32/J64/D/LU32 written, ELL index arrays
     prep_b = nF * 400 * 3 + nnz * (400 + 100 + 200 + 4 + 4 + 1 + 8) + N * (200 + 100 + 8 + 8)
     res_b = nnz * (4 + 8 + 200) + N * (8 + 200 + 40 + 40 + 20)
     out = {"workload": "kernels", "unit": "ms", "config": {
-        "workload": f"BLU-SGS 5x5 FP32 pieces, {args.mesh}^3 jittered permuted hex ({N} cells, {nF} faces), "
+        "workload": f"BLU-SGS 5x5 {'FP64 (FMA)' if prec != 2 else 'FP32'} pieces, {args.mesh}^3 jittered permuted "
+                    f"hex ({N} cells, {nF} faces), "
                     f"{len(rg)} colours", "cells": N, "colors": len(rg)},
         "launch": tuned,
         "prepare": {"ms": prep_ms, "GBps": prep_b / (prep_ms * 1e-3) / 1e9, "bytes": prep_b},
@@ -1208,6 +1277,10 @@ def main(argv=None):
     ap.add_argument("--max-pairs", type=int, default=400)
     ap.add_argument("--ref-pairs", type=int, default=1)
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")
+    ap.add_argument("--sweep-variant", type=int, default=None,
+                    help="lusgs / kernels workloads: this sweep variant at 256 threads instead of the autotuned "
+                         "launch (a profiler then sees one known kernel)")
+    ap.add_argument("--fp64", action="store_true", help="kernels workload: the FP64 (fused multiply-add) system")
     ap.add_argument("--autotune-cache", default=None,
                     help="JSON file of launch choices: reused when it holds one for the system, else written "
                          "(a profiled run can then repeat the choices of an unprofiled one)")
@@ -1227,6 +1300,8 @@ def main(argv=None):
         args.warmup = 3
     if args.mesh is None:
         args.mesh = {"lusgs": 256, "gmres": 96, "colored": 32, "adjoint": 64}.get(args.workload, 128)
+    if args.sweep_variant is not None:
+        args.no_autotune = True
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "lusgs":

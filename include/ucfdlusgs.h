@@ -140,7 +140,10 @@ UCFD_EXTERN ucfd_status_t UCFDFlowSysSetStream(FlowSys sys, void *cuda_stream, i
  * of the launch configuration (UCFDFlowSysAutotune).  Requires a prior Pack of
  * every element.  resid (optional, [niter]) receives sqrt(sum du^2)
  * accumulated in FP64 after each iteration.  Update() afterwards writes
- * the final state back to the element arrays. */
+ * the final state back to the element arrays.  With UCFD_PREC_FP32 the
+ * sweeps read an FP32 copy of the state while u += du accumulates into an
+ * FP64 master copy (made at Pack), so increments below the state's FP32
+ * rounding unit are not lost; Update() writes that master back. */
 UCFD_EXTERN ucfd_status_t UCFDLUSGS_Run(FlowSys sys, UCFDInt niter, UCFDReal kappa, int rans,
                                         int mode, UCFDReal *resid);
 

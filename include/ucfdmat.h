@@ -53,6 +53,11 @@ UCFD_EXTERN ucfd_status_t UCFDMatGetType(SpMat mat, const char **type_name);
  * on first use), FP64 vectors and FP64 accumulation. */
 UCFD_EXTERN ucfd_status_t UCFDMatMultFP32(UCFDReal alpha, SpMat mat, UCFDReal *x,
                                           UCFDReal beta, UCFDReal *y);
+/* The product in a chosen arithmetic: UCFD_PREC_FP64 (= UCFDMatMult, the
+ * reference's operation order), UCFD_PREC_FP64_FMA (fused multiply-adds, as
+ * the solvers' FMA mode uses it) or UCFD_PREC_FP32 (= UCFDMatMultFP32). */
+UCFD_EXTERN ucfd_status_t UCFDMatMultPrecision(UCFDReal alpha, SpMat mat, UCFDReal *x,
+                                               UCFDReal beta, UCFDReal *y, int precision);
 
 #if defined(__cplusplus)
 }

@@ -539,6 +539,66 @@ class Ref:
 
 
 # ---------------------------------------------------------------------------
+# the reference's own GPU BSR matvec (oracle/_ref/cusparsemat.cubin)
+# ---------------------------------------------------------------------------
+REF_CUBIN = os.path.join(REF, "cusparsemat.cubin")
+
+
+def ref_cuda_available() -> bool:
+    return os.path.exists(REF_CUBIN)
+
+
+class RefCudaBSR:
+    """_SpMV_CUDABSR<blk> of src/krylov/matrix/cusparsemat.cu:74-115,
+    compiled from the reference source for sm_103a by oracle/Makefile, loaded
+    with the CUDA driver API and launched as SpMV_CUDABSR does
+    (cusparsemat.cu:118-139: (bn + TPB - 1) / TPB blocks of TPB = 128
+    threads, config.h:62-64).  Arguments are device pointers (integers);
+    the caller's CUDA context must be current (any torch CUDA call makes
+    it so)."""
+
+    TPB = 128
+
+    def __init__(self, blk: int = 5):
+        self.cu = ctypes.CDLL("libcuda.so.1")
+        cu = self.cu
+        for n in ("cuModuleLoad", "cuModuleGetFunction", "cuLaunchKernel", "cuCtxGetCurrent", "cuModuleUnload"):
+            getattr(cu, n).restype = c_int
+        ctx = c_void_p()
+        self._check(cu.cuCtxGetCurrent(byref(ctx)), "cuCtxGetCurrent")
+        if not ctx.value:
+            raise RuntimeError("no current CUDA context (initialise CUDA first, e.g. with torch)")
+        self.mod = c_void_p()
+        self._check(cu.cuModuleLoad(byref(self.mod), REF_CUBIN.encode()), "cuModuleLoad")
+        self.fn = c_void_p()
+        # the entry name nvcc gives the template instance (printed by ptxas -v)
+        name = f"_Z13_SpMV_CUDABSRILi{blk}EEvdiPKiS1_PKdS3_dPd".encode()
+        self._check(cu.cuModuleGetFunction(byref(self.fn), self.mod, name), "cuModuleGetFunction")
+
+    @staticmethod
+    def _check(rc, what):
+        if rc != 0:
+            raise RuntimeError(f"{what} failed with CUresult {rc}")
+
+    def spmv(self, alpha, bn, rowptr, colidx, values, x, beta, y, stream=0):
+        """y = alpha A x + beta y (all pointers device addresses)."""
+        a, b = c_double(alpha), c_double(beta)
+        n = c_int(bn)
+        ptrs = [c_void_p(rowptr), c_void_p(colidx), c_void_p(values), c_void_p(x)]
+        yp = c_void_p(y)
+        params = (c_void_p * 8)(ctypes.addressof(a), ctypes.addressof(n), *[ctypes.addressof(q) for q in ptrs],
+                                ctypes.addressof(b), ctypes.addressof(yp))
+        grid = (bn + self.TPB - 1) // self.TPB
+        self._check(self.cu.cuLaunchKernel(self.fn, grid, 1, 1, self.TPB, 1, 1, 0, c_void_p(stream), params, None),
+                    "cuLaunchKernel")
+
+    def close(self):
+        if self.mod:
+            self.cu.cuModuleUnload(self.mod)
+            self.mod = c_void_p()
+
+
+# ---------------------------------------------------------------------------
 # one BLU-SGS pseudo-time step, call by call
 # ---------------------------------------------------------------------------
 class BlusgsPhases:

@@ -434,3 +434,36 @@ def test_precon_without_off_diagonal_blocks(bn, kind, port, ucfd):
         sv.solve(pc2, A, xs, np.ascontiguousarray(b))
         assert sv.result()[0] == 0
         assert np.linalg.norm(port.bsr_spmv(s, xs) - b) <= 1e-10 * np.linalg.norm(b)
+
+
+@pytest.mark.skipif(not __import__("oracle.oracle", fromlist=["x"]).ref_cuda_available(),
+                    reason="the reference's GPU matvec was not compiled (oracle/_ref/cusparsemat.cubin)")
+def test_reference_gpu_matvec_agrees(port, ucfd):
+    """The reference's own _SpMV_CUDABSR<5> (cusparsemat.cu:74-139, built from
+    its source), which the bench times beside this library's matvec, gives
+    the oracle's product up to the rounding of fused multiply-adds, as does
+    this library's FMA-mode product."""
+    import torch
+
+    from oracle.oracle import RefCudaBSR
+    from ucfd_sparse_gb300.krylov import SpMat
+    from ucfd_sparse_gb300.lib import PREC_FP64_FMA
+    s = cases.bsr_case(mesh=6, seed=7)
+    bn = s["bn"]
+    x = cases.spmv_x(s)
+    d = {k: dev(s[k]) for k in ("rowptr", "colidx", "values")}
+    xd = dev(x)
+    torch.cuda.synchronize()
+    R = RefCudaBSR(5)
+    yr = torch.zeros(bn * 5, dtype=torch.float64, device="cuda")
+    R.spmv(1.0, bn, d["rowptr"].data_ptr(), d["colidx"].data_ptr(), d["values"].data_ptr(), xd.data_ptr(), 0.0,
+           yr.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    R.close()
+    A = SpMat(bn, 5, d["rowptr"], d["colidx"], d["values"], cuda=True)
+    y = torch.zeros(bn * 5, dtype=torch.float64, device="cuda")
+    A.mult(1.0, xd, 0.0, y, precision=PREC_FP64_FMA)
+    ref = port.bsr_spmv(s, x)
+    scale = np.abs(ref).max()
+    assert np.abs(yr.cpu().numpy() - ref).max() <= 1e-13 * scale
+    assert np.abs(y.cpu().numpy() - ref).max() <= 1e-13 * scale

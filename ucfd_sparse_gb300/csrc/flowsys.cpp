@@ -38,6 +38,7 @@ struct Work {
     DevBuf<S> rhs, bdu, dup, J, LU, tJ, tLU;        // block LU-SGS
     DevBuf<S> r, delta;                    // refinement
     DevBuf<S> fl_geo[2];                   // face lists (lower, upper): normal + fa * rv per entry
+    DevBuf<double> u64;                    // FP32 mode: FP64 master of the packed state (UCFDLUSGS_Run)
 };
 
 }  // namespace
@@ -468,9 +469,13 @@ void lusgs_iteration(FlowSys s, bool rans, double kappa, double *resid_slot, boo
         lusgs_sweep<S, EX>(s, true, false, kappa, persistent);
         lusgs_sweep<S, EX>(s, true, true, kappa, persistent);
     }
-    // u += du over the swept variables, ||du|| in FP64
+    // u += du over the swept variables, ||du|| in FP64; FP32 mode adds into
+    // the FP64 master state and rounds the working copy from it
     const int v1 = rans ? s->nvars : s->nfvars;
-    kfast::axpy_norm<S>((long long)v1 * s->N, w.du.p, w.u.p, s->part.p, resid_slot, st);
+    if constexpr (std::is_same<S, float>::value)
+        kfast::axpy_master((long long)v1 * s->N, w.du.p, w.u64.p, w.u.p, s->part.p, resid_slot, st);
+    else
+        kfast::axpy_norm<S>((long long)v1 * s->N, w.du.p, w.u.p, s->part.p, resid_slot, st);
 }
 
 void run_graph_drop(FlowSys s) {
@@ -793,11 +798,16 @@ ucfd_status_t UCFDFlowSysAutotune(FlowSys s, int reps, UCFDLaunchConfig *best) {
             UCFD_REQUIRE(w.u.p, "Autotune before Pack");
             // the loop writes u, du, diag and the spectral radii: keep them
             DevBuf<S> su, sdu, sdiag, slam;
+            DevBuf<double> su64;
             const size_t nl = (size_t)s->P * s->N;
             const bool had_lam = w.lamN.p != nullptr;
             su.ensure(n);
             sdu.ensure(n);
             sdiag.ensure(n);
+            if (w.u64.p) {
+                su64.ensure(n);
+                UCFD_CUDA(cudaMemcpyAsync(su64.p, w.u64.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+            }
             UCFD_CUDA(cudaMemcpyAsync(su.p, w.u.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
             UCFD_CUDA(cudaMemcpyAsync(sdu.p, w.du.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
             UCFD_CUDA(cudaMemcpyAsync(sdiag.p, w.diag.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
@@ -828,6 +838,7 @@ ucfd_status_t UCFDFlowSysAutotune(FlowSys s, int reps, UCFDLaunchConfig *best) {
                 consider(pms, 256, v, 1);
             }
             UCFD_CUDA(cudaMemcpyAsync(w.u.p, su.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
+            if (w.u64.p) UCFD_CUDA(cudaMemcpyAsync(w.u64.p, su64.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
             UCFD_CUDA(cudaMemcpyAsync(w.du.p, sdu.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
             UCFD_CUDA(cudaMemcpyAsync(w.diag.p, sdiag.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
             if (had_lam) UCFD_CUDA(cudaMemcpyAsync(w.lamN.p, slam.p, nl * sizeof(S), cudaMemcpyDeviceToDevice, st));
@@ -890,6 +901,10 @@ ucfd_status_t UCFDLUSGS_Pack(FlowSys s, UCFDInt eidx, UCFDReal turb_factor, UCFD
         Work<S> &w = work<S>(s);
         KCALL(EX, fs_lusgs_pack<S>, e.neles, s->nvars, s->nfvars, s->N, turb_factor, a0, ids, s->d_iperm.p, up, rh,
               dt, ds, w.u.p, w.du.p, w.diag.p, st);
+        if constexpr (std::is_same<S, float>::value) {
+            w.u64.ensure((size_t)s->nvars * s->N);
+            kfast::state64_pack(e.neles, s->nvars, s->N, ids, s->d_iperm.p, up, w.u64.p, st);
+        }
         const size_t n = (size_t)s->nvars * s->N;
         UCFD_CUDA(cudaMemcpyAsync(w.base.p, w.diag.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
         UCFD_CUDA(cudaMemcpyAsync(w.rhs0.p, w.du.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
@@ -914,8 +929,12 @@ ucfd_status_t UCFDLUSGS_Update(FlowSys s, UCFDInt eidx) {
         Work<S> &w = work<S>(s);
         UCFD_REQUIRE(w.du.p, "Update before Pack");
         // after UCFDLUSGS_Run the device-resident state itself is written back
-        KCALL(EX, fs_lusgs_update<S>, e.neles, s->nvars, s->N, ids, s->d_iperm.p, s->run_state ? w.u.p : w.du.p,
-              up, s->run_state ? 1 : 0, st);
+        // (FP32 mode: its FP64 master)
+        if (std::is_same<S, float>::value && s->run_state)
+            kfast::fs_lusgs_update<double>(e.neles, s->nvars, s->N, ids, s->d_iperm.p, w.u64.p, up, 1, st);
+        else
+            KCALL(EX, fs_lusgs_update<S>, e.neles, s->nvars, s->N, ids, s->d_iperm.p, s->run_state ? w.u.p : w.du.p,
+                  up, s->run_state ? 1 : 0, st);
     });
     if (!dev) copy_d2h(e.uptsb, up, nv * sizeof(double), st);
     finish(s, !dev);

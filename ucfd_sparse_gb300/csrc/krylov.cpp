@@ -653,7 +653,7 @@ ucfd_status_t UCFDMatGetType(SpMat mat, const char **type_name) {
     UCFD_API_END
 }
 
-static ucfd_status_t mat_mult(UCFDReal alpha, SpMat mat, UCFDReal *x, UCFDReal beta, UCFDReal *y, bool fp32) {
+static ucfd_status_t mat_mult(UCFDReal alpha, SpMat mat, UCFDReal *x, UCFDReal beta, UCFDReal *y, int prec) {
     UCFD_API_BEGIN
     UCFD_REQUIRE(mat && mat->type_name && mat->ready, "Matrix type must be set");
     UCFD_REQUIRE(x && y, "null vector");
@@ -662,7 +662,7 @@ static ucfd_status_t mat_mult(UCFDReal alpha, SpMat mat, UCFDReal *x, UCFDReal b
     const double *xd = device_view<double>(x, n, mat->sx, s);
     const bool ydev = is_device_ptr(y);
     double *yd = ydev ? y : const_cast<double *>(device_view<double>(y, n, mat->sy, s));
-    mat->mult(alpha, xd, beta, yd, fp32 ? UCFD_PREC_FP32 : UCFD_PREC_FP64, s);
+    mat->mult(alpha, xd, beta, yd, prec, s);
     UCFD_CHECK_LAUNCH();
     if (!ydev) copy_d2h(y, yd, n * sizeof(double), s);
     UCFD_CUDA(cudaStreamSynchronize(s));
@@ -670,10 +670,18 @@ static ucfd_status_t mat_mult(UCFDReal alpha, SpMat mat, UCFDReal *x, UCFDReal b
 }
 
 ucfd_status_t UCFDMatMult(UCFDReal alpha, SpMat mat, UCFDReal *x, UCFDReal beta, UCFDReal *y) {
-    return mat_mult(alpha, mat, x, beta, y, false);
+    return mat_mult(alpha, mat, x, beta, y, UCFD_PREC_FP64);
 }
 ucfd_status_t UCFDMatMultFP32(UCFDReal alpha, SpMat mat, UCFDReal *x, UCFDReal beta, UCFDReal *y) {
-    return mat_mult(alpha, mat, x, beta, y, true);
+    return mat_mult(alpha, mat, x, beta, y, UCFD_PREC_FP32);
+}
+ucfd_status_t UCFDMatMultPrecision(UCFDReal alpha, SpMat mat, UCFDReal *x, UCFDReal beta, UCFDReal *y,
+                                   int precision) {
+    if (precision != UCFD_PREC_FP64 && precision != UCFD_PREC_FP64_FMA && precision != UCFD_PREC_FP32) {
+        ucfd::set_error("UCFDMatMultPrecision: unknown precision %d", precision);
+        return UCFD_ERR_ARGUMENT;
+    }
+    return mat_mult(alpha, mat, x, beta, y, precision);
 }
 
 // ---- Precon ------------------------------------------------------------------

@@ -105,6 +105,10 @@
     void axpy_into(long long n, const Ts *x, double *y, cudaStream_t s);                           \
     template <typename S>                                                                          \
     void axpy_norm(long long n, const S *x, S *y, double *part, double *out, cudaStream_t s);      \
+    void axpy_master(long long n, const float *x, double *y64, float *y, double *part, double *out,  \
+                     cudaStream_t s);                                                              \
+    void state64_pack(int neles, int nvars, long long N, const int *cell_ids, const int *iperm,    \
+                      const double *upts, double *u64, cudaStream_t s);                            \
     /* ---- adjoint of the colored LU-SGS step ---- */                                            \
     template <typename T>                                                                          \
     void adj_upper(const ::ucfd::AdjArgs &a, int nfv, int ndims, T gamma, T pmin, const T *fnv,    \

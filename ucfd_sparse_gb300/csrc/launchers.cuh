@@ -655,6 +655,45 @@ void axpy_norm(long long n, const S *x, S *y, double *part, double *out, cudaStr
     sqrt_sum_kernel<<<1, 1024, 0, s>>>(nb, part, out);
 }
 
+// The FP32 pseudo-time update with an FP64 master state: y64 += x,
+// y = (float)y64, out = ||x||_2 accumulated in FP64.  An increment far
+// below the state's FP32 rounding unit is kept in y64 instead of being
+// rounded away at every iteration.
+__global__ void axpy_master_kernel(long long n, const float *x, double *y64, float *y, double *part) {
+    double t = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double xv = (double)x[i];
+        const double v = y64[i] + xv;
+        y64[i] = v;
+        y[i] = (float)v;
+        t += xv * xv;
+    }
+    t = block_sum(t);
+    if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+void axpy_master(long long n, const float *x, double *y64, float *y, double *part, double *out, cudaStream_t s) {
+    const int nb = gm_blocks(n);
+    axpy_master_kernel<<<nb, kBlock, 0, s>>>(n, x, y64, y, part);
+    sqrt_sum_kernel<<<1, 1024, 0, s>>>(nb, part, out);
+}
+
+// The FP64 master copy of the packed state (lusgs_pack's state, lusgs.c:8-37,
+// without rounding): u64[k + v N] = upts[idx + v neles], k = iperm[cell_ids[idx]].
+__global__ void state64_pack_kernel(int neles, int nvars, long long N, const int *cell_ids, const int *iperm,
+                                    const double *upts, double *u64) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= neles) return;
+    const long long k = iperm[cell_ids[idx]];
+    for (int v = 0; v < nvars; ++v) u64[k + v * N] = upts[idx + (long long)v * neles];
+}
+
+void state64_pack(int neles, int nvars, long long N, const int *cell_ids, const int *iperm, const double *upts,
+                  double *u64, cudaStream_t s) {
+    if (neles <= 0) return;
+    state64_pack_kernel<<<grid_for(neles), kBlock, 0, s>>>(neles, nvars, N, cell_ids, iperm, upts, u64);
+}
+
 __global__ void __launch_bounds__(256) norm_finalize_kernel(int nblocks, const double *part, double *out) {
     const double t = block_sum_partials(part, nblocks, kMaxK);
     if (threadIdx.x == 0) *out = sqrt(t);

@@ -20,8 +20,13 @@ class SpMat:
         call("UCFDMatCreateCUDABSR" if cuda else "UCFDMatCreateBSR", byref(self._h), bn, blk, ptr(rowptr),
              ptr(colidx), ptr(values))
 
-    def mult(self, alpha, x, beta, y, fp32=False):
-        call("UCFDMatMultFP32" if fp32 else "UCFDMatMult", alpha, self._h, ptr(x), beta, ptr(y))
+    def mult(self, alpha, x, beta, y, fp32=False, precision=None):
+        """y = alpha A x + beta y; precision (PREC_*) picks the arithmetic
+        (default FP64 in the reference's order, or FP32 values with fp32)."""
+        if precision is not None:
+            call("UCFDMatMultPrecision", alpha, self._h, ptr(x), beta, ptr(y), precision)
+        else:
+            call("UCFDMatMultFP32" if fp32 else "UCFDMatMult", alpha, self._h, ptr(x), beta, ptr(y))
 
     def update_values(self):
         call("UCFDMatUpdateValues", self._h)

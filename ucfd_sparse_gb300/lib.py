@@ -139,6 +139,7 @@ SIGNATURES = {
     "UCFDMatDestroy": (_I, [POINTER(c_void_p)]),
     "UCFDMatMult": (_I, [_D, _P, _P, _D, _P]),
     "UCFDMatMultFP32": (_I, [_D, _P, _P, _D, _P]),
+    "UCFDMatMultPrecision": (_I, [_D, _P, _P, _D, _P, _I]),
     "UCFDMatCreateCSR": (_I, [POINTER(c_void_p), _I, _P, _P, _P]),
     "UCFDMatCreateBSR": (_I, [POINTER(c_void_p), _I, _I, _P, _P, _P]),
     "UCFDMatCreateCUDACSR": (_I, [POINTER(c_void_p), _I, _P, _P, _P]),
