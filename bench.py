@@ -155,16 +155,15 @@ def make_case(m: int, seed: int = 0):
     return mg.blusgs_case(m, seed=seed)
 
 
-def sweep_bytes(rowptr: np.ndarray, elt: int, B: int = 5, lu_elt: int | None = None) -> int:
+def sweep_bytes(rowptr: np.ndarray, elt: int, B: int = 5) -> int:
     """Algorithmic bytes of one lower (or upper) BLU-SGS sweep over all
     cells as the FP32 / FMA-mode kernels run it: per cell-face its neighbour
-    index (4) and block (B*B*elt, the face factor folded in at Prepare); per
-    cell the LU block, rhs, and du read (as the neighbours' data, once) and
-    written."""
-    lu_elt = elt if lu_elt is None else lu_elt
+    index (4) and block (B*B*elt: M = D^-1 J fv, formed at Prepare); per
+    cell its right-hand side (D^-1 rhs) and du read (as the neighbours'
+    data, once) and written."""
     nnz = int(rowptr[-1])
     N = rowptr.shape[0] - 1
-    return nnz * (4 + B * B * elt) + N * (B * B * lu_elt + 3 * B * elt)
+    return nnz * (4 + B * B * elt) + N * (3 * B * elt)
 
 
 class Problem:
@@ -521,8 +520,8 @@ def run_gpu(args):
     except OSError:
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    bytes_sweep64 = sweep_bytes(case["rowptr"], 8, 5, 8)
-    bytes_sweep = sweep_bytes(case["rowptr"], 4, 5, 4)
+    bytes_sweep64 = sweep_bytes(case["rowptr"], 8, 5)
+    bytes_sweep = sweep_bytes(case["rowptr"], 4, 5)
     achieved = bytes_sweep / (sweep_ms * 1e-3) / 1e9
     launch_bytes = bytes_sweep / nlev
     cfg32 = P32.S.launch_config()
@@ -912,6 +911,27 @@ def run_gmres(args):
         res[prec]["precon_GBps"] = pb / (res[prec]["precon_ms"] * 1e-3) / 1e9
         res[prec]["precon_frac"] = res[prec]["precon_GBps"] / peak
         del pc, sv
+    # FP64 (FMA) GMRES ending a cycle once its residual estimate is low enough
+    # (UCFDSolverSetCycleExit) instead of the reference's full 30-step cycle
+    pc = Precon(d["rowptr"], d["colidx"], d["diagslots"], d["values"])
+    pc.set_pblusgs(bn, 5, len(rg), icolors, cuda=True)
+    pc.set_precision(1)
+    pc.prepare()
+    sv = Solver(n, 30, 100, tol, cuda=True)
+    sv.set_precision(1)
+    sv.set_cycle_exit(True)
+    x = torch.zeros(n, dtype=torch.float64, device=dev)
+    sv.solve(pc, A, x, d["rhs"])  # warm-up
+    x.zero_()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    sv.solve(pc, A, x, d["rhs"])
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t
+    st, it, r = sv.result()
+    res["fp64_cycle_exit"] = dict(s=el, stat=st, restarts=it, resid=r / (tol / 1e-10), arnoldi=sv.arnoldi_steps())
+    xs["fp64_cycle_exit"] = x.clone()
+    del pc, sv
     # the solution of the FP64 arithmetic of the oracle (UCFD_PREC_FP64: the
     # reference's operation order in the matvec and preconditioner), untimed
     pc = Precon(d["rowptr"], d["colidx"], d["diagslots"], d["values"])
@@ -923,8 +943,8 @@ def run_gmres(args):
     x0 = torch.zeros(n, dtype=torch.float64, device=dev)
     sv.solve(pc, A, x0, d["rhs"])
     x0max = float(x0.abs().max())
-    for prec in (1, 2):
-        res[prec]["err_vs_fp64"] = float((xs[prec] - x0).abs().max()) / x0max
+    for key in (1, 2, "fp64_cycle_exit"):
+        res[key]["err_vs_fp64"] = float((xs[key] - x0).abs().max()) / x0max
     del pc, sv, x0, xs
     torch.cuda.empty_cache()
     # BiCGSTAB (FP64) with the coloured BLU-SGS and the coloured block ILU(0)
@@ -1012,6 +1032,8 @@ def run_gmres(args):
            "config": {"workload": f"GMRES(30) + coloured BLU-SGS, Kuhn tets of a {args.mesh}^3 box ({bn} cells, "
                                   f"5x5 BSR, {nnzb} blocks), {len(rg)} colours, tol 1e-10 relative", "cells": bn},
            "fp64": res[1], "mixed": res[2], "speedup_mixed_vs_fp64": res[1]["s"] / res[2]["s"],
+           "fp64_cycle_exit": res["fp64_cycle_exit"],
+           "speedup_mixed_vs_fp64_cycle_exit": res["fp64_cycle_exit"]["s"] / res[2]["s"],
            "err_vs_fp64": res[2]["err_vs_fp64"],
            "err_definition": "max|x - x_fp64| / max|x_fp64|, x_fp64 the GMRES solution with UCFD_PREC_FP64 "
                              "(the oracle's arithmetic) to the same tolerance",
@@ -1242,10 +1264,13 @@ def run_kernels(args):
     nnz = int(case["rowptr"][-1])
     nF = int(case["nfaces"])
     elt = 8 if prec != 2 else 4
-    sw = 2 * sweep_bytes(case["rowptr"], elt, 5, elt)
+    sw = 2 * sweep_bytes(case["rowptr"], elt, 5)
     # Prepare: jmat read twice (transpose in, face records out) + written once,
-    # face records read per cell-face, J32/J64/D/LU32 written, ELL index arrays
-    prep_b = nF * 400 * 3 + nnz * (400 + 100 + 200 + 4 + 4 + 1 + 8) + N * (200 + 100 + 8 + 8)
+    # face records read per cell-face, the sweep blocks written, read back and
+    # rewritten as D^-1 J fv, J64 (FP32 mode) / D / LU written, ELL index arrays
+    jb = 25 * elt
+    prep_b = (nF * 400 * 3 + nnz * (400 + 3 * jb + (200 if prec == 2 else 0) + 4 + 4 + 1 + 8)
+              + N * (200 + 25 * elt + 8 + 8))
     res_b = nnz * (4 + 8 + 200) + N * (8 + 200 + 40 + 40 + 20)
     out = {"workload": "kernels", "unit": "ms", "config": {
         "workload": f"BLU-SGS 5x5 {'FP64 (FMA)' if prec != 2 else 'FP32'} pieces, {args.mesh}^3 jittered permuted "

@@ -62,6 +62,13 @@ UCFD_EXTERN ucfd_status_t UCFDSolverCreateBICGSTAB(Solver *solver, UCFDInt n, UC
 UCFD_EXTERN ucfd_status_t UCFDSolverSetPrecision(Solver solver, int precision);
 /* Happy-breakdown tolerance (default 1e-12, solver.c:11). */
 UCFD_EXTERN ucfd_status_t UCFDSolverSetHappyTol(Solver solver, UCFDReal haptol);
+/* GMRES in the FP64 modes: with on != 0 a restart cycle also ends once its
+ * residual estimate has fallen by the factor the true residual still needs
+ * to reach tol (with a margin of 10), instead of always building m Krylov
+ * vectors; the restart then checks the true residual as usual.  Default
+ * off: the reference's iteration (gmres.c:62-125).  The mixed-precision
+ * mode always ends a cycle at the FP32 operator's accuracy. */
+UCFD_EXTERN ucfd_status_t UCFDSolverSetCycleExit(Solver solver, int on);
 /* Total Arnoldi steps of the last solve. */
 UCFD_EXTERN ucfd_status_t UCFDSolverGetArnoldiSteps(Solver solver, UCFDInt *steps);
 

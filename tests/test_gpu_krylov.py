@@ -149,6 +149,44 @@ def test_gmres_coloured_and_mixed_reach_1e10(prec, port, ucfd):
     assert np.abs(x.cpu().numpy() - xr).max() <= 1e-8 * np.abs(xr).max()
 
 
+@pytest.mark.parametrize("prec", [0, 1])
+def test_gmres_cycle_exit(prec, port, ucfd):
+    """UCFDSolverSetCycleExit: the FP64 GMRES ends its cycle once the residual
+    estimate is low enough -- fewer Arnoldi steps than the reference's full
+    cycle, the same status, at most one more restart check, the true
+    residual within tol and the solution within 1e-8 of the oracle's."""
+    from ucfd_sparse_gb300.krylov import Precon, Solver, SpMat
+    s0 = cases.bsr_case(mesh=8, seed=2)
+    s, ic = colour_renumbered(s0)
+    n = s["bn"] * 5
+    d = {k: dev(s[k]) for k in ("rowptr", "colidx", "values", "diagslots", "rhs")}
+    A = SpMat(s["bn"], 5, d["rowptr"], d["colidx"], d["values"], cuda=True)
+    pc = Precon(d["rowptr"], d["colidx"], d["diagslots"], d["values"])
+    pc.set_pblusgs(s["bn"], 5, len(ic) - 1, np.array(ic, dtype=np.int32), cuda=True)
+    pc.set_precision(prec)
+    pc.prepare()
+    tol = 1e-10 * float(np.linalg.norm(s["rhs"]))
+    steps, xs = {}, {}
+    for on in (False, True):
+        sv = Solver(n, 30, 50, tol, cuda=True)
+        sv.set_precision(prec)
+        sv.set_cycle_exit(on)
+        x = torch.zeros(n, dtype=torch.float64, device="cuda")
+        sv.solve(pc, A, x, d["rhs"])
+        st, it, res = sv.result()
+        assert st == 0 and res <= tol
+        steps[on] = (it, sv.arnoldi_steps())
+        xs[on] = x.cpu().numpy()
+        y = d["rhs"].clone()
+        A.mult(-1.0, x, 1.0, y)
+        assert float(torch.linalg.norm(y)) <= 1.01 * tol
+    xr, st_o, it_o, res_o, _ = port.gmres(s, s["rhs"], m=30, maxiter=50, tol=tol, pc="pblusgs", icolors=ic)
+    assert steps[False][0] == it_o
+    assert steps[True][0] <= it_o + 1           # at most one extra restart check
+    assert steps[True][1] < steps[False][1]
+    assert np.abs(xs[True] - xr).max() <= 1e-8 * np.abs(xr).max()
+
+
 # ---- block / scalar ILU(0) and BiCGSTAB -----------------------------------------
 def scalar_case(s):
     """A CSR matrix (blk 1) on the BSR pattern: the (0, 0) entry of each block."""

@@ -47,7 +47,7 @@ def _noalloc(S, out):
              else ctypes.addressof(out))
 
 
-@pytest.mark.parametrize("prec", [0, 2])
+@pytest.mark.parametrize("prec", [0, 1, 2])
 def test_noalloc_residual_matches_existing_entry_point(prec, ucfd):
     S, _ = _system(prec)
     for sweeps in (1, 2):

@@ -39,6 +39,7 @@ struct Work {
     DevBuf<S> r, delta;                    // refinement
     DevBuf<S> fl_geo[2];                   // face lists (lower, upper): normal + fa * rv per entry
     DevBuf<double> u64;                    // FP32 mode: FP64 master of the packed state (UCFDLUSGS_Run)
+    DevBuf<S> crhs;                        // fast modes: D^-1 rhs, the block sweeps' right-hand side
 };
 
 }  // namespace
@@ -78,6 +79,7 @@ struct _FlowSys {
     DevBuf<double> jt;  // Prepare scratch: face Jacobians, one record per face
     DevBuf<int> d_sweep_err;  // set by a bulk-copy block sweep whose copy wait gave up
     bool du64_valid = false;
+    bool c_valid[2] = {false, false};  // crhs of the NS / turbulence rows matches rhs and the factors
     bool x_zero = false;  // the correction du is all zeros (Reset, no sweep since)
     DevBuf<double> part, red, resid;
     PinnedBuf<double> h_red;
@@ -411,6 +413,23 @@ const S *blu_LU(FlowSys s, bool turb) {
     else return turb ? s->w32.tLU.p : s->w32.LU.p;
 }
 
+// Right-hand side of the fast modes' block sweeps (their blocks are
+// M = D^-1 J fv, so a sweep starts from D^-1 rhs): computed from the packed
+// rhs when Pack or Prepare changed it; the exact mode sweeps rhs itself.
+template <typename S, bool EX>
+const S *sweep_rhs(FlowSys s, bool turb) {
+    Work<S> &w = work<S>(s);
+    if constexpr (EX) return w.rhs.p;
+    const int B = turb ? s->ntvars : s->nfvars;
+    const int var0 = turb ? s->nfvars : 0;
+    if (!s->c_valid[turb ? 1 : 0]) {
+        w.crhs.ensure((size_t)s->nvars * s->N);
+        kfast::fs_blusgs_rhs_solve<S>(B, s->N, var0, blu_LU<S>(s, turb), w.rhs.p, w.crhs.p, s->stream());
+        s->c_valid[turb ? 1 : 0] = true;
+    }
+    return w.crhs.p;
+}
+
 template <typename S, bool EX>
 void blusgs_sweep_into(FlowSys s, bool turb, bool upper, const S *rhs, S *du) {
     Work<S> &w = work<S>(s);
@@ -433,7 +452,7 @@ void blusgs_residual(FlowSys s, const Sx *x, R *r_out, double *rnorm, double *bn
     s->red.ensure(2);
     const double *J64 = s->prec == UCFD_PREC_FP32 ? s->J64.p : s->w64.J.p;
     const double *rhs64 = s->prec == UCFD_PREC_FP32 ? s->rhs64.p : s->w64.rhs.p;
-    // the FMA mode's blocks already carry the face factor (nullptr face areas)
+    // the FMA mode's blocks are M = D^-1 J fv (nullptr face areas)
     const double *fa = s->prec == UCFD_PREC_FP64_FMA ? nullptr : s->fa64.p;
     int nb = 0;
     if constexpr (EX)
@@ -1048,6 +1067,7 @@ ucfd_status_t UCFDBLUSGS_Pack(FlowSys s, UCFDInt eidx, UCFDReal a0) {
         KCALL(EX, fs_blusgs_pack<S>, e.neles, s->nvars, s->nfvars, s->N, a0, ids, s->d_iperm.p, rh, dt,
               blu_rhs<S>(s), r64, s->dd.p, st);
     });
+    s->c_valid[0] = s->c_valid[1] = false;
     finish(s, !is_device_ptr(e.rhs));
     UCFD_API_END
 }
@@ -1070,6 +1090,7 @@ static ucfd_status_t tpack_api(FlowSys s, int model, UCFDInt eidx, UCFDReal fact
     dispatch(s, [&]<typename S, bool EX>() { blusgs_alloc<S>(s); });
     kfast::fs_tblusgs_pack(model, e.neles, s->nvars, s->ntvars, s->N, a0, factor, constants().betast, ids,
                            s->d_iperm.p, up, ds, dt, s->tD.p, st);
+    s->c_valid[1] = false;
     finish(s, !is_device_ptr(e.uptsb));
     UCFD_API_END
 }
@@ -1110,6 +1131,7 @@ static ucfd_status_t blusgs_prepare_api(FlowSys s, bool turb) {
         KCALL(EX, fs_blusgs_prepare<S>, B, s->N, s->P, (long long)s->nfaces, s->d_nei.p, s->d_slot.p, s->d_side.p,
               s->fa64.p, s->rv64.p, jd, dd, D, LU64, LU_s, turb ? w.tJ.p : w.J.p, J64, jt, st);
     });
+    s->c_valid[turb ? 1 : 0] = false;
     finish(s, !is_device_ptr(jm));
     UCFD_API_END
 }
@@ -1125,7 +1147,8 @@ static ucfd_status_t blusgs_sweep_api(FlowSys s, bool turb, bool upper) {
     dispatch(s, [&]<typename S, bool EX>() {
         Work<S> &w = work<S>(s);
         UCFD_REQUIRE(w.rhs.p, "sweep before Pack");
-        blusgs_sweep_into<S, EX>(s, turb, upper, w.rhs.p, w.bdu.p);
+        UCFD_REQUIRE(blu_LU<S>(s, turb), "sweep before Prepare");
+        blusgs_sweep_into<S, EX>(s, turb, upper, sweep_rhs<S, EX>(s, turb), w.bdu.p);
     });
     s->du64_valid = false;
     s->x_zero = false;
@@ -1244,6 +1267,8 @@ ucfd_status_t UCFDBLUSGS_Solve(FlowSys s, UCFDReal rtol, UCFDInt max_sweeps, UCF
         blusgs_residual<double, float, false>(s, s->x_zero ? nullptr : s->x64.p, w.r.p, &rn, &bn);
         rel = bn > 0 ? rn / bn : rn;
         while (rel > rtol && pairs < max_sweeps) {
+            // the sweeps' right-hand side D^-1 r (their blocks are D^-1 J fv)
+            kfast::fs_blusgs_rhs_solve<float>(s->nfvars, s->N, 0, w.LU.p, w.r.p, w.r.p, st);
             w.delta.zero(n, st);
             const int m = std::min(inner_sweeps, max_sweeps - pairs);
             for (int q = 0; q < m; ++q) {
@@ -1271,8 +1296,9 @@ ucfd_status_t UCFDBLUSGS_Solve(FlowSys s, UCFDReal rtol, UCFDInt max_sweeps, UCF
                     blusgs_sweep_into<double, true>(s, false, false, w.rhs.p, w.bdu.p);
                     blusgs_sweep_into<double, true>(s, false, true, w.rhs.p, w.bdu.p);
                 } else {
-                    blusgs_sweep_into<double, false>(s, false, false, w.rhs.p, w.bdu.p);
-                    blusgs_sweep_into<double, false>(s, false, true, w.rhs.p, w.bdu.p);
+                    const double *c = sweep_rhs<double, false>(s, false);
+                    blusgs_sweep_into<double, false>(s, false, false, c, w.bdu.p);
+                    blusgs_sweep_into<double, false>(s, false, true, c, w.bdu.p);
                 }
             }
             pairs += m;
@@ -1302,7 +1328,7 @@ bool ucfd::flowsys_block_view(FlowSys s, BlockSystemView &v) {
     t.P = s->P;
     t.B = s->nfvars;
     t.nei = s->d_nei.p;
-    t.fa = s->prec == UCFD_PREC_FP64_FMA ? nullptr : s->fa64.p;  // FMA mode: J64 carries fa * rv
+    t.fa = s->prec == UCFD_PREC_FP64_FMA ? nullptr : s->fa64.p;  // FMA mode: J64 holds D^-1 J fa rv
     t.rv = s->rv64.p;
     t.D = s->D.p;
     if (s->prec == UCFD_PREC_FP32) {

@@ -11,7 +11,8 @@ struct BlockSystemView {
     int P = 0;              // ELL width
     int B = 0;              // NS block size (nfvars)
     const int *nei = nullptr;
-    // fa == nullptr: the blocks J64 already carry the face factor fa * rv
+    // fa == nullptr: J64 holds M = D^-1 J fa rv (the FP64 fused multiply-add
+    // mode's sweep blocks); the residual is then rhs - D (x + sum_f M x_nb)
     const double *fa = nullptr, *rv = nullptr, *J64 = nullptr, *D = nullptr, *rhs64 = nullptr;
     const double *x64 = nullptr;  // current increment (FP64), or
     const float *x32 = nullptr;   // current increment (FP32 sweeps)

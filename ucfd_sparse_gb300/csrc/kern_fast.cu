@@ -32,6 +32,7 @@ namespace kfast {
     template void fs_blusgs_residual<T, T>(int, long long, int, int, int, const int *, const double *,         \
                                            const double *, const double *, const double *, const double *,     \
                                            const T *, T *, double *, int, int *, cudaStream_t);                \
+    template void fs_blusgs_rhs_solve<T>(int, long long, int, const T *, const T *, T *, cudaStream_t);        \
     template void fs_blusgs_subres<T>(int, int, long long, const int *, const int *, const double *,           \
                                       const T *, T *, double *, cudaStream_t);                                 \
     template void fs_blusgs_update<T>(int, int, long long, const int *, const int *, const T *, double *,      \

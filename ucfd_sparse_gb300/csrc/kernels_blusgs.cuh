@@ -212,9 +212,9 @@ __device__ __forceinline__ double xor_sign(double x, unsigned hi_mask) {
 
 // pre_blusgs: blusgs.c:200-246, plus the gather of each cell-face's
 // off-diagonal block (the half the sweeps use) into the ELL layout.  The
-// fast build stores the sweep blocks J_s times the face factor fv and
-// reciprocal pivots (kFold); J64, the FP64 copy the FP32 mode's residual
-// reads, always holds the unscaled blocks.
+// fast build (kFold) stores reciprocal pivots and, as the sweep blocks J_s,
+// M = D^-1 J fv; J64, the FP64 copy the FP32 mode's residual reads, always
+// holds the unscaled blocks.
 // The block starts from dd[k] I when dd is given (NS pack), else from D.
 // jt holds the face-major records written by jmat_face_major_kernel.
 // The side's sign goes into the face factor once per face: the diagonal
@@ -278,6 +278,49 @@ __global__ void fs_blusgs_prepare_kernel(long long N, int P, const int *nei, con
         if (LU64) LU64[dbase + (e << 5)] = dm[e];
         if (LU_s) LU_s[dbase + (e << 5)] = (S)dm[e];
     }
+    if constexpr (kFold) {
+        // the sweep blocks become M = D^-1 J fv, column by column through the
+        // factors just formed (in the sweep precision), so that a sweep is
+        // du_k = D^-1 rhs_k - sum_f M_f du_nb with no block solve per cell
+        S lu[B2];
+#pragma unroll
+        for (int e = 0; e < B2; ++e) lu[e] = (S)dm[e];
+        for (int p = 0; p < P; ++p) {
+            if (nei[p * N + k] < 0) break;
+            S m[B2];
+#pragma unroll
+            for (int e = 0; e < B2; ++e) m[e] = J_s[jbase + ((long long)(p * B2 + e) << 5)];
+#pragma unroll
+            for (int c = 0; c < B; ++c) {
+                S col[B];
+#pragma unroll
+                for (int r = 0; r < B; ++r) col[r] = m[r * B + c];
+                lusub_dev<S, B, true>(lu, col);
+#pragma unroll
+                for (int r = 0; r < B; ++r) m[r * B + c] = col[r];
+            }
+#pragma unroll
+            for (int e = 0; e < B2; ++e) J_s[jbase + ((long long)(p * B2 + e) << 5)] = m[e];
+        }
+    }
+}
+
+// c = D^-1 b for the fast build's sweeps (variables var0 .. var0 + B - 1 of
+// every cell, through the factors LU with reciprocal pivots); c may be b.
+template <typename S, int B>
+__global__ void fs_blusgs_rhs_solve_kernel(long long N, int var0, const S *LU, const S *b, S *c) {
+    const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    constexpr int B2 = B * B;
+    S lu[B2], v[B];
+    const S *LUk = LU + ::ucfd::tile_index(k, 0, B2);
+#pragma unroll
+    for (int e = 0; e < B2; ++e) lu[e] = LUk[e << 5];
+#pragma unroll
+    for (int r = 0; r < B; ++r) v[r] = b[(var0 + r) * N + k];
+    lusub_dev<S, B, true>(lu, v);
+#pragma unroll
+    for (int r = 0; r < B; ++r) c[(var0 + r) * N + k] = v[r];
 }
 
 // lower_sweep / upper_sweep of blusgs.c:273-373 for one level: every
@@ -383,11 +426,13 @@ __global__ void __launch_bounds__(256) fs_blusgs_sweep_kernel(int t0, int t1, lo
             }
         }
     }
-    S lu[B2];
-    const S *LUk = LU + ::ucfd::tile_index(k, 0, B2);
+    if constexpr (!kFold) {
+        S lu[B2];
+        const S *LUk = LU + ::ucfd::tile_index(k, 0, B2);
 #pragma unroll
-    for (int e = 0; e < B2; ++e) lu[e] = __ldcs(LUk + (e << 5));
-    lusub_dev<S, B, kFold>(lu, b);
+        for (int e = 0; e < B2; ++e) lu[e] = __ldcs(LUk + (e << 5));
+        lusub_dev<S, B>(lu, b);
+    }
 #pragma unroll
     for (int r = 0; r < B; ++r) du[(var0 + r) * N + k] = b[r];
 }
@@ -423,8 +468,10 @@ __global__ void __launch_bounds__(128) fs_blusgs_sweep_small_kernel(int t0, int 
 #pragma unroll
         for (int e = 0; e < B2; ++e) jv[p][e] = __ldcs(Jk + ((p * B2 + e) << 5));
     }
+    if constexpr (!kFold) {
 #pragma unroll
-    for (int e = 0; e < B2; ++e) lu[e] = __ldcs(LUk + (e << 5));
+        for (int e = 0; e < B2; ++e) lu[e] = __ldcs(LUk + (e << 5));
+    }
     asm volatile("griddepcontrol.wait;" ::: "memory");
     float x[PW][B];
 #pragma unroll
@@ -450,7 +497,7 @@ __global__ void __launch_bounds__(128) fs_blusgs_sweep_small_kernel(int t0, int 
             }
         }
     }
-    lusub_dev<float, B, kFold>(lu, b);
+    if constexpr (!kFold) lusub_dev<float, B>(lu, b);
 #pragma unroll
     for (int r = 0; r < B; ++r) du[(var0 + r) * N + k] = b[r];
 }
@@ -464,8 +511,9 @@ __global__ void __launch_bounds__(128) fs_blusgs_sweep_small_kernel(int t0, int 
 // while it gathers the neighbour increments of the current tile and
 // computes it; with NST == 1 twice as many warps fit, each with one
 // buffer.  Per cell the arithmetic is that of fs_blusgs_sweep_kernel
-// (same products and subtractions, same order).  A copy that has not
-// landed after max_spin polls sets *err; the warp then waits (bounded)
+// (same products and subtractions, same order); in the fast build the
+// blocks are M = D^-1 J fv and the LU tile is not needed.  A copy that has
+// not landed after max_spin polls sets *err; the warp then waits (bounded)
 // for its other copy and returns.
 template <int B, int PW, int NST>
 __global__ void __launch_bounds__(NST == 2 ? 128 : 256)
@@ -475,7 +523,7 @@ __global__ void __launch_bounds__(NST == 2 ? 128 : 256)
                                 const float *__restrict__ rhs, float *du, int *err, long long max_spin) {
     constexpr int B2 = B * B;
     constexpr int JT = PW * B2 * 32;  // floats of J in one tile
-    constexpr int LT = B2 * 32;       // floats of LU in one tile
+    constexpr int LT = kFold ? 0 : B2 * 32;  // floats of LU in one tile (the fast build's blocks need none)
     constexpr int ST = JT + LT;       // floats per buffer
     constexpr unsigned JBYTES = JT * 4, LBYTES = LT * 4;
     static_assert(JBYTES % 16 == 0 && LBYTES % 16 == 0, "bulk copies move multiples of 16 bytes");
@@ -500,7 +548,7 @@ __global__ void __launch_bounds__(NST == 2 ? 128 : 256)
             ::ucfd::dev::fence_proxy_async_smem();
             ::ucfd::dev::mbar_arrive_expect_tx(&bar[q], JBYTES + LBYTES);
             ::ucfd::dev::bulk_copy_g2s(buf + q * ST, J + tt * JT, JBYTES, &bar[q]);
-            ::ucfd::dev::bulk_copy_g2s(buf + q * ST + JT, LU + tt * LT, LBYTES, &bar[q]);
+            if constexpr (LBYTES > 0) ::ucfd::dev::bulk_copy_g2s(buf + q * ST + JT, LU + tt * LT, LBYTES, &bar[q]);
         }
     };
     if (t < tile1) issue(t, 0);
@@ -556,10 +604,12 @@ __global__ void __launch_bounds__(NST == 2 ? 128 : 256)
                 }
             }
         }
-        float lu[B2];
+        if constexpr (!kFold) {
+            float lu[B2];
 #pragma unroll
-        for (int e = 0; e < B2; ++e) lu[e] = sJ[JT + (e << 5)];
-        lusub_dev<float, B, kFold>(lu, b);
+            for (int e = 0; e < B2; ++e) lu[e] = sJ[JT + (e << 5)];
+            lusub_dev<float, B>(lu, b);
+        }
         if (act) {
 #pragma unroll
             for (int r = 0; r < B; ++r) du[(var0 + r) * N + k] = b[r];
@@ -570,8 +620,8 @@ __global__ void __launch_bounds__(NST == 2 ? 128 : 256)
 }
 
 // FP64 residual of the packed system: r = rhs - D x - sum_f J x_nb fv.
-// fa == nullptr: J64 holds the blocks already multiplied by fv (the FP64
-// fused multiply-add mode's sweep blocks), so r = rhs - D x - sum_f J x_nb.
+// fa == nullptr: J64 holds the FP64 fused multiply-add mode's sweep blocks
+// M = D^-1 J fv, so r = rhs - D (x + sum_f M x_nb).
 // Writes r (as R) when r_out != nullptr and accumulates per-block partial
 // sums of r^2 and rhs^2 into part[2*blockIdx.x + {0,1}].
 template <typename Sx, typename R, int B>
@@ -588,11 +638,14 @@ __global__ void fs_blusgs_residual_kernel(long long N, int P, int var0, int nvar
         // x == nullptr: x is known to be zero, r = rhs (no matrix reads)
 #pragma unroll
         for (int c = 0; c < B; ++c) xk[c] = x ? (double)x[(var0 + c) * N + k] : 0.0;
+        // M form: t = x + sum_f M x_nb, then r = rhs - D t (below)
+        double t[B];
 #pragma unroll
         for (int r = 0; r < B; ++r) {
+            t[r] = xk[r];
             double v = rhs64[(var0 + r) * N + k];
             bb += v * v;
-            if (x) {
+            if (x && fa) {
 #pragma unroll
                 for (int c = 0; c < B; ++c) v -= D[::ucfd::tile_index(k, r * B + c, B2)] * xk[c];
             }
@@ -627,9 +680,15 @@ __global__ void fs_blusgs_residual_kernel(long long N, int P, int var0, int nvar
                     for (int c = 0; c < B; ++c)
                         val += J64[::ucfd::tile_index(k, (long long)p * B2 + r * B + c, (long long)P * B2)] * xn[q][c];
                     if (fa) res[r] -= val * fv;
-                    else res[r] -= val;
+                    else t[r] += val;
                 }
             }
+        }
+        if (x && !fa) {
+#pragma unroll
+            for (int r = 0; r < B; ++r)
+#pragma unroll
+                for (int c = 0; c < B; ++c) res[r] -= D[::ucfd::tile_index(k, r * B + c, B2)] * t[c];
         }
 #pragma unroll
         for (int r = 0; r < B; ++r) {

@@ -416,6 +416,10 @@ struct _Solver {
     // mixed precision: a cycle ends when its residual estimate drops below
     // this fraction of the cycle's start (FP32 operator accuracy)
     double mixed_floor = 1e-6;
+    // FP64 modes, on request: a cycle also ends once its residual estimate
+    // has fallen by the factor the true residual still needs (x 0.1), instead
+    // of always building m vectors (UCFDSolverSetCycleExit)
+    bool cycle_exit = false;
     long long arnoldi = 0;
     long long ldv = 0;
     DevBuf<double> V, w, r, H, cs, sn, y, h2, part, abeta;
@@ -541,6 +545,9 @@ struct _Solver {
                 stat = CONVERGED;
                 break;
             }
+            // the cycle's floor on its (preconditioned) residual estimate,
+            // relative to the cycle's start
+            const double floor = mixed ? mixed_floor : cycle_exit ? std::min(0.5, 0.1 * tol / ab) : 0.0;
             pc->apply(r.p, s);
             kfast::gm_sumsq(n, r.p, part.p, s);
             kfast::gm_cycle_begin(nb, part.p, st.p, y.p, nullptr, s);
@@ -556,10 +563,9 @@ struct _Solver {
                 kfast::gm_update(n, K, V.p, ldv, Hc, w.p, 0, part.p, s);
                 kfast::gm_reduce(nb, K, part.p, h2.p, 0, s);
                 kfast::gm_update(n, K, V.p, ldv, h2.p, w.p, 1, part.p, s);
-                kfast::gm_givens(j, ld, nb, part.p, H.p, h2.p, cs.p, sn.p, y.p, haptol, mixed ? mixed_floor : 0.0,
-                                 st.p, s);
+                kfast::gm_givens(j, ld, nb, part.p, H.p, h2.p, cs.p, sn.p, y.p, haptol, floor, st.p, s);
                 kfast::gm_scale(n, st.p, w.p, V.p + (size_t)(j + 1) * ldv, s);
-                if (mixed) {
+                if (floor > 0.0) {
                     // an FP32 operator cannot resolve the cycle below its floor: stop
                     // launching once the device reports it (one host read per step)
                     UCFD_CUDA(cudaMemcpyAsync(h_st.p, st.p, kfast::gm_state_bytes(), cudaMemcpyDeviceToHost, s));
@@ -878,6 +884,13 @@ ucfd_status_t UCFDSolverSetHappyTol(Solver solver, UCFDReal haptol) {
     UCFD_API_BEGIN
     UCFD_REQUIRE(solver, "null Solver");
     solver->haptol = haptol;
+    UCFD_API_END
+}
+
+ucfd_status_t UCFDSolverSetCycleExit(Solver solver, int on) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(solver, "null Solver");
+    solver->cycle_exit = on != 0;
     UCFD_API_END
 }
 

@@ -269,7 +269,8 @@ static void sweep_bulk_go(int t0, int t1, long long N, int var0, const int *nei,
                           int *err, long long max_spin, cudaStream_t s) {
     auto kern = fs_blusgs_sweep_bulk_kernel<B, PW, NST>;
     constexpr int threads = NST == 2 ? 128 : 256;
-    constexpr size_t smem = (size_t)(threads / 32) * NST * ((PW + 1) * B * B * 32 * sizeof(float) + 8);
+    constexpr int tiles_per_buf = kFold ? PW : PW + 1;  // J (and, in the exact build, LU) tiles
+    constexpr size_t smem = (size_t)(threads / 32) * NST * (tiles_per_buf * B * B * 32 * sizeof(float) + 8);
     static int cap = 0;  // per instantiation: co-resident blocks on the device
     if (!cap) {
         UCFD_CUDA(cudaFuncSetAttribute((const void *)kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -384,6 +385,12 @@ void fs_blusgs_sweep(int B, int t0, int t1, long long N, int P, int var0, const 
         UCFD_BSW(B, (fs_blusgs_sweep_kernel<S, BB, 0><<<g, block, 0, s>>>(t0, t1, N, P, var0, nei, fa, rv, J, LU,
                                                                           rhs, du)));
     }
+}
+
+template <typename S>
+void fs_blusgs_rhs_solve(int B, long long N, int var0, const S *LU, const S *b, S *c, cudaStream_t s) {
+    if (N <= 0) return;
+    UCFD_BSW(B, (fs_blusgs_rhs_solve_kernel<S, BB><<<grid_for(N), kBlock, 0, s>>>(N, var0, LU, b, c)));
 }
 
 template <typename Sx, typename R>

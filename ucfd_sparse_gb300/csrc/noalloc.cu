@@ -84,7 +84,7 @@ __device__ inline double warp_block_sum(double v, double *sh) {
 
 // Grid-stride variant of the FP64 residual kernel: per cell
 // r = rhs - D x - sum_f J x_nb fv (same per-cell arithmetic; fa == nullptr:
-// the blocks already carry fv), per block the
+// the blocks are M = D^-1 J fv and r = rhs - D (x + sum_f M x_nb)), per block the
 // partial sums of r^2 and rhs^2 go to scratch[2 b], scratch[2 b + 1].
 template <typename Sx, int B>
 __global__ void __launch_bounds__(kThreads) residual_noalloc_kernel(long long N, int P, const int *nei,
@@ -97,15 +97,17 @@ __global__ void __launch_bounds__(kThreads) residual_noalloc_kernel(long long N,
     double rr = 0.0, bb = 0.0;
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < N;
          k += (long long)gridDim.x * blockDim.x) {
-        double res[B], xk[B];
+        double res[B], xk[B], t[B];
 #pragma unroll
-        for (int c = 0; c < B; ++c) xk[c] = (double)x[c * N + k];
+        for (int c = 0; c < B; ++c) xk[c] = t[c] = (double)x[c * N + k];
 #pragma unroll
         for (int r = 0; r < B; ++r) {
             double v = rhs64[r * N + k];
             bb += v * v;
+            if (fa) {
 #pragma unroll
-            for (int c = 0; c < B; ++c) v -= D[::ucfd::tile_index(k, r * B + c, B2)] * xk[c];
+                for (int c = 0; c < B; ++c) v -= D[::ucfd::tile_index(k, r * B + c, B2)] * xk[c];
+            }
             res[r] = v;
         }
         for (int p = 0; p < P; ++p) {
@@ -122,8 +124,15 @@ __global__ void __launch_bounds__(kThreads) residual_noalloc_kernel(long long N,
                 for (int c = 0; c < B; ++c)
                     val += J64[::ucfd::tile_index(k, (long long)p * B2 + r * B + c, (long long)P * B2)] * xn[c];
                 if (fa) res[r] -= val * fv;
-                else res[r] -= val;
+                else t[r] += val;
             }
+        }
+        if (!fa) {
+            // M form: r = rhs - D (x + sum_f M x_nb)
+#pragma unroll
+            for (int r = 0; r < B; ++r)
+#pragma unroll
+                for (int c = 0; c < B; ++c) res[r] -= D[::ucfd::tile_index(k, r * B + c, B2)] * t[c];
         }
 #pragma unroll
         for (int r = 0; r < B; ++r) rr += res[r] * res[r];

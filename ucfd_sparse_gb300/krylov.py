@@ -115,6 +115,11 @@ class Solver:
     def set_precision(self, prec):
         call("UCFDSolverSetPrecision", self._h, prec)
 
+    def set_cycle_exit(self, on=True):
+        """GMRES: end a restart cycle once its residual estimate is low enough
+        (UCFDSolverSetCycleExit; default off, the reference's iteration)."""
+        call("UCFDSolverSetCycleExit", self._h, 1 if on else 0)
+
     def trace(self):
         call("UCFDSolverTraceResidualHistory", self._h)
 

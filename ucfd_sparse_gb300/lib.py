@@ -173,6 +173,7 @@ SIGNATURES = {
     "UCFDSolverCreateCUDAGMRES": (_I, [POINTER(c_void_p), _I, _I, _I, _D]),
     "UCFDSolverSetPrecision": (_I, [_P, _I]),
     "UCFDSolverSetHappyTol": (_I, [_P, _D]),
+    "UCFDSolverSetCycleExit": (_I, [_P, _I]),
     "UCFDSolverGetArnoldiSteps": (_I, [_P, POINTER(c_int)]),
 }
 
