@@ -30,6 +30,7 @@ COMMON = ["-O3", "-std=c++20", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
 UNITS = [
     ("kern_exact.cu", ["-fmad=false"]),
     ("kern_fast.cu", []),
+    ("kern_gm.cu", []),
     ("runtime.cpp", []),
     ("graph.cpp", []),
     ("flowsys.cpp", []),

@@ -312,6 +312,14 @@ __global__ void scatter_rows_kernel(int bn, int B, const int *perm, const Ts *sr
 // ---- GMRES(m) device pieces (gmres.c:4-129) --------------------------------
 constexpr int kMaxK = 32;  // restart length + 1 <= kMaxK
 
+// Grid of the reduction kernels: capped so the per-block partial buffers
+// stay small (8 blocks x 152 SMs).
+constexpr int kRedBlocks = 1216;
+__host__ __device__ inline int gm_grid(long long n) {
+    const long long g = (n + kBlock - 1) / kBlock;
+    return (int)(g < kRedBlocks ? (g > 0 ? g : 1) : kRedBlocks);
+}
+
 // Per-block partial dots h[k] = sum_i V[k][i] * w[i], k < K.
 // Block partials of KM accumulators (only the first KK meaningful) into
 // part[block][k].

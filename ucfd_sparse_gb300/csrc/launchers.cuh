@@ -594,32 +594,9 @@ __global__ void __launch_bounds__(1024) sqrt_sum_kernel(int nb, const double *pa
 }
 
 // ---- GMRES pieces ----------------------------------------------------------
-// Reduction grids are capped so the per-block partial buffers stay small.
-constexpr int kRedBlocks = 1216;  // 8 x 152 SMs
+int gm_blocks(long long n) { return gm_grid(n); }
 
-int gm_blocks(long long n) {
-    long long g = (n + kBlock - 1) / kBlock;
-    return (int)(g < kRedBlocks ? (g > 0 ? g : 1) : kRedBlocks);
-}
-
-// the vector count K picks the smallest compiled bound (register footprint)
-void gm_dots(long long n, int K, const double *V, long long ldv, const double *w, double *part,
-             cudaStream_t s) {
-    const int g = gm_blocks(n);
-    if (K <= 4) gm_dots_kernel<4><<<g, kBlock, 0, s>>>(n, K, V, ldv, w, part);
-    else if (K <= 8) gm_dots_kernel<8><<<g, kBlock, 0, s>>>(n, K, V, ldv, w, part);
-    else if (K <= 16) gm_dots_kernel<16><<<g, kBlock, 0, s>>>(n, K, V, ldv, w, part);
-    else gm_dots_kernel<32><<<g, kBlock, 0, s>>>(n, K, V, ldv, w, part);
-}
-
-void gm_update(long long n, int K, const double *V, long long ldv, const double *h, double *w, int mode,
-               double *part, cudaStream_t s) {
-    const int g = gm_blocks(n);
-    if (K <= 4) gm_update_kernel<4><<<g, kBlock, 0, s>>>(n, K, V, ldv, h, w, mode, part);
-    else if (K <= 8) gm_update_kernel<8><<<g, kBlock, 0, s>>>(n, K, V, ldv, h, w, mode, part);
-    else if (K <= 16) gm_update_kernel<16><<<g, kBlock, 0, s>>>(n, K, V, ldv, h, w, mode, part);
-    else gm_update_kernel<32><<<g, kBlock, 0, s>>>(n, K, V, ldv, h, w, mode, part);
-}
+// gm_dots / gm_update: gm_launchers.cuh (their own translation unit, kern_gm.cu)
 
 void gm_reduce(int nblocks, int K, const double *part, double *out, int accumulate, cudaStream_t s) {
     if (K <= 0) return;
