@@ -1297,7 +1297,8 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--rtol", type=float, default=1e-10)
     ap.add_argument("--inner", type=int, default=20, help="FP32 sweep pairs per FP64 refinement step")
-    ap.add_argument("--check", type=int, default=4, help="FP64 solve: pairs between residual checks")
+    ap.add_argument("--check", type=int, default=20,
+                    help="FP64 solve: pairs between residual checks (as many as the FP32 solve's --inner)")
     ap.add_argument("--max-pairs", type=int, default=400)
     ap.add_argument("--ref-pairs", type=int, default=1)
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch configuration")

@@ -31,7 +31,6 @@ void fail(ucfd_status_t st, const char *fmt, ...) {
 
 // ---- timed host<->device copies (UCFDSetTransferTiming) ------------------
 namespace {
-constexpr size_t kWaitCopyBytes = 32u << 20;
 std::mutex g_xfer_mu;
 bool g_xfer_on = false;
 UCFDTransferStats g_xfer{};
@@ -44,13 +43,6 @@ void timed_copy(void *dst, const void *src, size_t bytes, cudaMemcpyKind kind, c
     }
     if (!on) {
         UCFD_CUDA(cudaMemcpyAsync(dst, src, bytes, kind, s));
-        // A large host -> device staging copy is waited for before the
-        // kernels that read it are enqueued.  Measured on GB300 (2.5 GB of
-        // face Jacobians per Prepare from pinned memory): the copy then runs
-        // at the link's 211 GB/s every time, while with the launches queued
-        // behind it it ran at 100-150 GB/s in most repetitions.  The calls
-        // that stage host arrays synchronise before returning anyway.
-        if (kind == cudaMemcpyHostToDevice && bytes >= kWaitCopyBytes) UCFD_CUDA(cudaStreamSynchronize(s));
         return;
     }
     thread_local cudaEvent_t ev[2] = {nullptr, nullptr};
