@@ -246,7 +246,7 @@ def launches_per_step(nlev, pairs, inner, mixed):
     n += 2                                         # initial residual + reduction
     n += outer * 2 + pairs * 2 * nlev              # residual per outer loop, sweeps
     if mixed:
-        n += 2 + outer                             # conversions, x += delta
+        n += 2 + 2 * outer                         # conversions; per outer step x += delta and D^-1 r
     return n
 
 

@@ -158,3 +158,20 @@ def test_blusgs_turbulence_packs_and_sweeps(port, ucfd):
             fn(5, 2, N, 7, nF, P(rp), P(ci), P(sd), P(sl), P(fa), P(rv), P(rr), P(tdg), P(tj), P(du))
     L.oracle_blusgs_update(N, N, 7, P(ids), P(du), P(upts))
     np.testing.assert_array_equal(e["upts"], upts)
+
+
+def test_transfer_timing_counts_host_copies(ucfd):
+    """UCFDSetTransferTiming / UCFDGetTransferStats: a step on host arrays
+    counts the staged inputs (at least the face Jacobians) and the state
+    copied back; timing off leaves the counters alone."""
+    from ucfd_sparse_gb300 import lib
+    b = cases.blusgs_case(m=6, seed=2)
+    S, e = make(b)
+    lib.transfer_timing(True)
+    run_sweeps(S, 1)
+    st = lib.transfer_stats()
+    lib.transfer_timing(False)
+    assert st["h2d_bytes"] >= b["jmat"].nbytes and st["h2d_copies"] >= 1 and st["h2d_ms"] > 0
+    assert st["d2h_bytes"] >= b["upts"].nbytes and st["d2h_copies"] >= 1
+    run_sweeps(S, 1)
+    assert lib.transfer_stats() == st
