@@ -605,6 +605,21 @@ def run_gpu(args):
                                     for k, v in xfer_copies.items()},
                 "how": "CUDA events around every host<->device copy the library makes, the same steps repeated; "
                        "then the steps once more without timing"}
+    # the same steps with the face Jacobians read in place from pinned host
+    # memory by the Prepare kernels (UCFD_HOST_MAP) instead of staged copies
+    host_access0 = _lib.host_array_access()
+    _lib.set_host_array_access(1 - host_access0)
+    Ph.step(args.rtol, args.max_pairs, args.inner)
+    torch.cuda.synchronize()
+    map_calls = {}
+    t3 = time.perf_counter()
+    map_pe = [Ph.step(args.rtol, args.max_pairs, args.inner, map_calls)[0] for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    other_s = (time.perf_counter() - t3) / args.steps
+    _lib.set_host_array_access(host_access0)
+    other_access = {"mode": ("UCFD_HOST_MAP" if host_access0 == 0 else "UCFD_HOST_STAGE"),
+                    "ms_per_step": other_s * 1e3, "value": N * statistics.mean(map_pe) / other_s,
+                    "ms_per_call": {k: v * 1e3 / K for k, v in map_calls.items()}}
     # the same pinned jmat copied alone (torch copy, one transfer): the host link's rate for it
     jdev = torch.empty(Ph.e["jmat"].shape, dtype=Ph.e["jmat"].dtype, device=device)
     torch.cuda.synchronize()
@@ -636,7 +651,9 @@ def run_gpu(args):
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": Ph.h2d_bytes(),
                     "d2h_bytes_per_step": Ph.d2h_bytes(), "ms_per_step": e2e_s * 1e3,
                     "ms_per_call": {k: v * 1e3 / args.steps for k, v in calls.items()},
-                    "jmat_copy_GBps": jmat_gbps, "copies_timed": xfer_out},
+                    "jmat_copy_GBps": jmat_gbps, "copies_timed": xfer_out,
+                    "host_array_access": "UCFD_HOST_MAP" if host_access0 == 1 else "UCFD_HOST_STAGE",
+                    "other_host_array_access": other_access},
             "gpu_launches": launches_per_step(nlev, int(round(pairs_mean)), args.inner, True) * args.steps,
             "clocks": clocks,
             "launch": tuned or "defaults (--no-autotune)",
@@ -654,15 +671,24 @@ def _events(stream):
     return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
 
-def lusgs_iter_bytes(rowptr, elt, nfv=5, nt=1):
+def lusgs_iter_bytes(rowptr, elt, nfv=5, nt=1, both=False):
     """Algorithmic bytes of one scalar LU-SGS pseudo-time iteration per
     UCFDLUSGS_Run (NS + RANS prepare, lower and upper sweeps, update), FlowSys
     layout: per face its index, area, spectral radius and (once, in the sweep
     where it is active) its normal; per cell the packed diagonal, the state
-    and increment of every variable read/written once."""
+    and increment of every variable read/written once.  both: the loop's
+    one-pass kernels (one prepare and one sweep per direction for both
+    systems), which read each face's index and area once per kernel."""
     nnz = int(rowptr[-1])
     N = rowptr.shape[0] - 1
     nv = nfv + nt
+    if both:
+        per_face = (4 + 3 * elt) + 2 * (4 + 3 * elt) + 3 * elt    # prepare, 2 sweeps, normal once
+        per_cell = 2 * nv * elt                                    # du = rhs copy
+        per_cell += elt + 2 * nv * elt                             # rcp_vol, diag from base
+        per_cell += 2 * (elt + nfv * elt + 3 * nv * elt)           # sweeps: rv, u, du own r/w + nbr, diag
+        per_cell += 3 * nv * elt                                   # u += du
+        return nnz * per_face + N * per_cell
     per_face = (4 + 2 * elt) * 2 + (4 + 3 * elt + 2 * elt)   # NS prepare + sweeps
     per_face += (4 + 2 * elt) + (4 + 3 * elt + 2 * elt)      # RANS prepare + sweeps
     per_cell = 2 * nv * elt                                    # du = rhs copy
@@ -734,20 +760,25 @@ def run_lusgs(args):
         # tuned launch and every variant at 256 threads
         if mode == 0:
             S.lusgs_ns_prepare(1.0)
+            S.lusgs_rans_prepare(1.0)
 
-            def lower_ms():
-                S.lusgs_ns_lower(1.0)
+            def lower_ms(sweep=S.lusgs_ns_lower):
+                sweep(1.0)
                 torch.cuda.synchronize()
                 e0, e1 = _events(stream)
                 e0.record(stream)
                 for _ in range(10):
-                    S.lusgs_ns_lower(1.0)
+                    sweep(1.0)
                 e1.record(stream)
                 torch.cuda.synchronize()
                 return e0.elapsed_time(e1) / 10
 
             res["sweep_ms"] = lower_ms()
             res["sweep_launch"] = S.launch_config()
+            # the loop's sweep with the turbulence system: both systems in one
+            # pass (one thread per cell), or the RANS sweep after the NS sweep
+            res["rans_sweep_ms"] = lower_ms(S.lusgs_rans_lower)
+            res["nsrans_sweep_ms"] = lower_ms(S.lusgs_nsrans_lower)
             cand = {}
             for var in (0, 1, 2, 3, 5):
                 S.set_launch_config(threads_per_block=256, sweep_variant=var)
@@ -785,7 +816,9 @@ def run_lusgs(args):
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    bytes_iter = lusgs_iter_bytes(c["rowptr"], 4)
+    # the loop sweeps both systems in one pass with one thread per cell
+    both = res["sweep_launch"]["sweep_variant"] <= 2
+    bytes_iter = lusgs_iter_bytes(c["rowptr"], 4, both=both)
     best = min(res[0]["ms"], res[1]["ms"])
     rp = c["rowptr"]
     nnz = int(rp[-1])
@@ -793,7 +826,12 @@ def run_lusgs(args):
     # per cell-face neighbour index, area, spectral radius, 3 normal components;
     # per cell rcp_vol and 4 x nvars state values (u and du of neighbours as
     # other cells' own data, du read and written, diag) -- 228 B/cell on hex
-    sweep_bytes_ = nnz * (4 + (2 + 3) * 4) + N * (4 + 4 * 5 * 4)
+    ns_bytes = nnz * (4 + (2 + 3) * 4) + N * (4 + 4 * 5 * 4)
+    # both systems: per cell-face also the turbulence spectral radius; per
+    # cell the 5 mean-flow state values the fluxes read and du (own + nbr),
+    # du written and diag of all 6 variables -- 264 B/cell on hex
+    both_bytes = nnz * (4 + (3 + 3) * 4) + N * (4 + 5 * 4 + 3 * 6 * 4)
+    sweep_bytes_, sweep_ms_ = (both_bytes, res["nsrans_sweep_ms"]) if both else (ns_bytes, res["sweep_ms"])
     out = {"workload": "lusgs", "metric": METRIC, "unit": UNIT,
            "config": {"workload": f"scalar LU-SGS pseudo-time loop, {m}^3 jittered permuted hex ({N} cells), "
                                   f"nvars 5 + 1 RANS, FP32, greedy colouring ({len(rg)} colours), "
@@ -805,15 +843,23 @@ def run_lusgs(args):
                           "GBps": bytes_iter * args.iters / (res[1]["ms"] * 1e-3) / 1e9},
            "bytes_per_cell_iteration": bytes_iter / N,
            "roofline": {"bound": "hbm",
-                        "kernel": ("scalar_sweep_faces_kernel<float,6,5,3,false>"
+                        "kernel": ("scalar_sweep_both_kernel<float,6,5,3> (both systems, lower sweep)" if both else
+                                   "scalar_sweep_faces_kernel<float,6,5,3,false>"
                                    if res["sweep_launch"]["sweep_variant"] == 5 else
                                    "scalar_sweep_pair_kernel<float,6,5,3,false>"
                                    if res["sweep_launch"]["sweep_variant"] in (3, 4) else
                                    "scalar_sweep_kernel<float,6,5,3,false>"),
-                        "launch": res["sweep_launch"], "candidates_ms": res["sweep_candidates_ms"],
-                        "achieved": sweep_bytes_ / (res["sweep_ms"] * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
-                        "frac": sweep_bytes_ / (res["sweep_ms"] * 1e-3) / 1e9 / peak,
-                        "sweep_ms": res["sweep_ms"], "algorithmic_bytes_per_sweep": sweep_bytes_},
+                        "launch": res["sweep_launch"],
+                        "achieved": sweep_bytes_ / (sweep_ms_ * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                        "frac": sweep_bytes_ / (sweep_ms_ * 1e-3) / 1e9 / peak,
+                        "sweep_ms": sweep_ms_, "algorithmic_bytes_per_sweep": sweep_bytes_},
+           "ns_sweep": {"kernel": "NS lower sweep alone (UCFDLUSGS_NSLowerSweep)", "ms": res["sweep_ms"],
+                        "GBps": ns_bytes / (res["sweep_ms"] * 1e-3) / 1e9,
+                        "frac": ns_bytes / (res["sweep_ms"] * 1e-3) / 1e9 / peak,
+                        "algorithmic_bytes": ns_bytes, "candidates_ms": res["sweep_candidates_ms"]},
+           "nsrans_sweep": {"ms": res["nsrans_sweep_ms"], "separate_ns_plus_rans_ms":
+                            res["sweep_ms"] + res["rans_sweep_ms"], "rans_ms": res["rans_sweep_ms"],
+                            "algorithmic_bytes": both_bytes},
            "loop_frac_of_peak": bytes_iter * args.iters / (best * 1e-3) / 1e9 / peak,
            "resid_fp64": [res[0]["resid_first"], res[0]["resid_last"]],
            "err_vs_fp64": err_lusgs,

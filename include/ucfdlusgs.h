@@ -60,6 +60,18 @@ UCFD_EXTERN ucfd_status_t UCFDLUSGS_NSLowerSweep(FlowSys sys, UCFDReal kappa);
 UCFD_EXTERN ucfd_status_t UCFDLUSGS_NSUpperSweep(FlowSys sys, UCFDReal kappa);
 UCFD_EXTERN ucfd_status_t UCFDLUSGS_RANSLowerSweep(FlowSys sys, UCFDReal kappa);
 UCFD_EXTERN ucfd_status_t UCFDLUSGS_RANSUpperSweep(FlowSys sys, UCFDReal kappa);
+/* Both systems in one call: NSRANSPrepare gives the values of NSPrepare
+ * followed by RANSPrepare, NSRANSLowerSweep those of NSLowerSweep followed
+ * by RANSLowerSweep, NSRANSUpperSweep those of NSUpperSweep followed by
+ * RANSUpperSweep (each system's sweep reads only the state and its own
+ * increments, so the two are independent).  With one thread per cell
+ * (sweep_variant 0-2) one kernel serves both systems and loads each
+ * neighbour index, face normal, area and mean-flow state once; the other
+ * variants run the two sweeps one after the other.  No counterpart in the
+ * reference, whose callers make the NS and RANS calls one by one. */
+UCFD_EXTERN ucfd_status_t UCFDLUSGS_NSRANSPrepare(FlowSys sys, UCFDReal kappa);
+UCFD_EXTERN ucfd_status_t UCFDLUSGS_NSRANSLowerSweep(FlowSys sys, UCFDReal kappa);
+UCFD_EXTERN ucfd_status_t UCFDLUSGS_NSRANSUpperSweep(FlowSys sys, UCFDReal kappa);
 
 /* ---- block LU-SGS (ucfdlusgs.h:28-40, blusgs.c) ----------------------- */
 UCFD_EXTERN ucfd_status_t UCFDFlowSysSetBLUSGS(FlowSys *sys, UCFDReal *jmat, UCFDReal *tjmat);
@@ -122,8 +134,10 @@ typedef struct {
 /* Times every launch candidate on the current system and keeps the fastest.
  * Block LU-SGS (after Pack + NSPrepare): threads_per_block x sweep_variant
  * on lower+upper sweep pairs into a scratch correction.  Scalar LU-SGS
- * (after Pack; fspr set): threads_per_block x run_mode on the iteration of
- * UCFDLUSGS_Run, the state saved before and restored after.  reps >= 1
+ * (after Pack; fspr set): threads_per_block x sweep_variant x run_mode on
+ * the iteration of UCFDLUSGS_Run -- with the turbulence system when the
+ * handle has one and tfspr is set -- the state saved before and restored
+ * after.  reps >= 1
  * timed repetitions per candidate after one untimed one.  Synchronises. */
 UCFD_EXTERN ucfd_status_t UCFDFlowSysAutotune(FlowSys sys, int reps, UCFDLaunchConfig *best);
 UCFD_EXTERN ucfd_status_t UCFDFlowSysGetLaunchConfig(FlowSys sys, UCFDLaunchConfig *cfg);
@@ -139,11 +153,17 @@ UCFD_EXTERN ucfd_status_t UCFDFlowSysSetStream(FlowSys sys, void *cuda_stream, i
  * grid-synchronised kernel per sweep (mode 1); mode -1 takes the run_mode
  * of the launch configuration (UCFDFlowSysAutotune).  Requires a prior Pack of
  * every element.  resid (optional, [niter]) receives sqrt(sum du^2)
- * accumulated in FP64 after each iteration.  Update() afterwards writes
- * the final state back to the element arrays.  With UCFD_PREC_FP32 the
- * sweeps read an FP32 copy of the state while u += du accumulates into an
- * FP64 master copy (made at Pack), so increments below the state's FP32
- * rounding unit are not lost; Update() writes that master back. */
+ * accumulated to FP64 accuracy after each iteration.  Update() afterwards
+ * writes the final state back to the element arrays.  With UCFD_PREC_FP32
+ * the sweeps read the FP32 state while u += du accumulates into a
+ * float-float pair (the FP32 state plus an FP32 low part made at Pack, 48
+ * significant bits), so increments below the state's FP32 rounding unit
+ * are not lost; Update() writes the pair's sum back.  With the
+ * turbulence system and one thread per cell (sweep_variant 0-2, and the
+ * persistent kernel) one kernel prepares both systems and one launch per
+ * level sweeps both: the two sweeps read only the state and their own
+ * increments, so the values are those of the separate calls, with each
+ * neighbour index, face normal, area and mean-flow state loaded once. */
 UCFD_EXTERN ucfd_status_t UCFDLUSGS_Run(FlowSys sys, UCFDInt niter, UCFDReal kappa, int rans,
                                         int mode, UCFDReal *resid);
 

@@ -58,6 +58,38 @@ def test_blusgs_natural_order_bitexact(name, on_device, golden, ucfd):
     np.testing.assert_array_equal(host(e["res"]), arr[f"{name}_resid"])
 
 
+@pytest.mark.parametrize("name", sorted(cases.BLUSGS))
+@pytest.mark.parametrize("prec", [0, 2])
+def test_blusgs_pinned_jacobians_read_in_place(name, prec, golden, ucfd):
+    """UCFD_HOST_MAP: face Jacobians in pinned host memory are read in place
+    by the Prepare kernels; the other host arrays are staged.  FP64 gives the
+    golden outputs bit for bit and every mode the staged run's values."""
+    from ucfd_sparse_gb300 import lib
+    meta, arr = golden
+    kw = cases.BLUSGS[name]
+    b = cases.blusgs_case(**kw)
+    outs = {}
+    for mode in (lib.HOST_STAGE, lib.HOST_MAP):
+        S, e = make(b, prec=prec)
+        jm = torch.from_numpy(np.ascontiguousarray(b["jmat"])).pin_memory()
+        S.set_blusgs(jm)
+        lib.set_host_array_access(mode)
+        try:
+            assert lib.host_array_access() == mode
+            run_sweeps(S, kw["nsweeps"])
+        finally:
+            lib.set_host_array_access(lib.HOST_STAGE)
+        outs[mode] = (np.array(e["upts"]), np.array(e["res"]))
+        S.destroy()
+    for a, r in zip(outs[lib.HOST_MAP], outs[lib.HOST_STAGE]):
+        np.testing.assert_array_equal(a, r)
+    if prec == 0:
+        np.testing.assert_array_equal(outs[lib.HOST_MAP][0], arr[f"{name}_upts"])
+        np.testing.assert_array_equal(outs[lib.HOST_MAP][1], arr[f"{name}_resid"])
+    with pytest.raises(lib.UCFDError):
+        lib.set_host_array_access(2)
+
+
 def test_blusgs_colored_equals_renumbered(port, ucfd):
     from ucfd_sparse_gb300 import coloredlusgs as cl
     from ucfd_sparse_gb300 import meshgen as mg

@@ -255,6 +255,71 @@ def test_flowsys_invalid_colouring_rejected(ucfd):
     assert ex.value.status == 2 and "colour" in str(ex.value)
 
 
+@pytest.mark.parametrize("name", sorted(cases.FLOWSYS))
+@pytest.mark.parametrize("mode", [0, 1])
+def test_flowsys_run_loop_bitexact(name, mode, golden, ucfd):
+    """UCFDLUSGS_Run with the turbulence system, FP64 mode, equals the
+    reference's Pack / NSPrepare / NS lower / NS upper / RANSPrepare / RANS
+    lower / RANS upper / Update repeated (the golden outputs) bit for bit.
+    With one thread per cell the loop prepares both systems in one kernel
+    and sweeps both in one launch per level (graph, mode 0) or in one
+    cooperative launch per sweep (mode 1)."""
+    meta, arr = golden
+    kw = cases.FLOWSYS[name]
+    fs, inp = cases.flowsys_case(**kw)
+    S, e = make_flowsys(fs, inp, prec=0, on_device=True)
+    S.set_launch_config(threads_per_block=128, sweep_variant=0, run_mode=mode)
+    S.lusgs_pack(0, kw["turb_factor"], kw["a0"])
+    S.lusgs_run(kw["nsteps"], kw["kappa"], rans=True, mode=mode)
+    S.lusgs_update(0)
+    np.testing.assert_array_equal(e["upts"].cpu().numpy(), arr[f"{name}_upts"])
+
+
+@pytest.mark.parametrize("name", sorted(cases.FLOWSYS))
+@pytest.mark.parametrize("variant", [0, 3])
+def test_nsrans_calls_bitexact(name, variant, golden, ucfd):
+    """NSRANSPrepare / NSRANSLowerSweep / NSRANSUpperSweep in place of the
+    six NS and RANS calls: the golden outputs bit for bit, with the one-pass
+    kernel (variant 0) and with the two sweeps one after the other
+    (variant 3, two threads per cell)."""
+    meta, arr = golden
+    kw = cases.FLOWSYS[name]
+    fs, inp = cases.flowsys_case(**kw)
+    S, e = make_flowsys(fs, inp, prec=0, on_device=True)
+    S.set_launch_config(threads_per_block=128, sweep_variant=variant)
+    for _ in range(kw["nsteps"]):
+        S.lusgs_pack(0, kw["turb_factor"], kw["a0"])
+        S.lusgs_nsrans_prepare(kw["kappa"])
+        S.lusgs_nsrans_lower(kw["kappa"])
+        S.lusgs_nsrans_upper(kw["kappa"])
+        S.lusgs_update(0)
+    np.testing.assert_array_equal(e["upts"].cpu().numpy(), arr[f"{name}_upts"])
+
+
+@pytest.mark.parametrize("prec", [0, 1, 2])
+def test_run_loop_both_systems_equal_separate_sweeps(prec, ucfd):
+    """The loop's one-pass sweeps of both systems (one thread per cell:
+    launch variants 0-2) give the values of the separate mean-flow and
+    turbulence sweeps (two threads per cell, variant 3, one system after the
+    other), state and residual history alike, in every arithmetic."""
+    kw = cases.FLOWSYS["fs5"]
+    fs, inp = cases.flowsys_case(**kw)
+    outs = []
+    for var in (0, 1, 2, 3):
+        S, e = make_flowsys(fs, inp, prec=prec, on_device=True)
+        S.set_launch_config(threads_per_block=64, sweep_variant=var)
+        S.lusgs_pack(0, kw["turb_factor"], kw["a0"])
+        res = np.zeros(3)
+        S.lusgs_run(3, kw["kappa"], rans=True, mode=0, resid=res)
+        S.lusgs_update(0)
+        outs.append((e["upts"].cpu().numpy(), res))
+    assert np.all(np.isfinite(outs[0][1])) and outs[0][1][0] > 0
+    assert np.abs(outs[0][0] - inp["upts"]).max() > 0
+    for up, res in outs[1:]:
+        np.testing.assert_array_equal(up, outs[0][0])
+        np.testing.assert_array_equal(res, outs[0][1])
+
+
 def test_flowsys_run_graph_matches_steps(ucfd):
     """UCFDLUSGS_Run (CUDA graph, device-resident) equals the same number of
     explicit Pack-free iterations driven through the API."""

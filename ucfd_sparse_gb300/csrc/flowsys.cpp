@@ -38,7 +38,7 @@ struct Work {
     DevBuf<S> rhs, bdu, dup, J, LU, tJ, tLU;        // block LU-SGS
     DevBuf<S> r, delta;                    // refinement
     DevBuf<S> fl_geo[2];                   // face lists (lower, upper): normal + fa * rv per entry
-    DevBuf<double> u64;                    // FP32 mode: FP64 master of the packed state (UCFDLUSGS_Run)
+    DevBuf<S> ulo;                         // FP32 mode: low part of the float-float state u + ulo (UCFDLUSGS_Run)
     DevBuf<S> crhs;                        // fast modes: D^-1 rhs, the block sweeps' right-hand side
 };
 
@@ -288,8 +288,11 @@ void ensure_face_lists(FlowSys s) {
     UCFD_CUDA(cudaStreamSynchronize(st));
 }
 
+// sys: 0 the mean-flow system, 1 the turbulence system, 2 both in one pass
+// (one thread per cell; the run loop's choice, see run_sweeps_both).
 template <typename S, bool EX>
-void lusgs_sweep(FlowSys s, bool rans, bool upper, double kappa, bool persistent = false) {
+void lusgs_sweep(FlowSys s, int sys, bool upper, double kappa, bool persistent = false) {
+    const bool rans = sys == 1;
     Work<S> &w = work<S>(s);
     const long long N = s->N;
     ScalarSweepArgs<S> a{};
@@ -302,6 +305,7 @@ void lusgs_sweep(FlowSys s, bool rans, bool upper, double kappa, bool persistent
     a.rv = geo_rv<S>(s);
     a.nrm = w.nrm.p;
     a.lam = rans ? w.lamT.p : w.lamN.p;
+    a.tlam = sys == 2 ? w.lamT.p : nullptr;
     a.u = w.u.p;
     a.nbsrc = w.du.p;
     a.own_in = w.du.p;
@@ -315,9 +319,9 @@ void lusgs_sweep(FlowSys s, bool rans, bool upper, double kappa, bool persistent
     // scalar sweeps: variant 1 / 2 = the builds for 3 / 4 resident blocks of
     // 256 per SM; 3 / 4 = two threads per cell, default / 64-register build
     a.regcap = (s->variant == 1) ? 3 : (s->variant == 2 || s->variant == 4) ? 4 : 0;
-    a.pair = (s->variant == 3 || s->variant == 4) ? 1 : 0;
+    a.pair = (s->variant == 3 || s->variant == 4) && sys != 2 ? 1 : 0;
     // 5: one thread per active face, from the face lists
-    a.facelist = (s->variant == 5 && !persistent) ? 1 : 0;
+    a.facelist = (s->variant == 5 && !persistent && sys != 2) ? 1 : 0;
     if (a.facelist) {
         ensure_face_lists<S>(s);
         const int dir = upper ? 1 : 0;
@@ -330,7 +334,7 @@ void lusgs_sweep(FlowSys s, bool rans, bool upper, double kappa, bool persistent
     if (persistent) {
         // one cooperative launch per sweep, bounded grid barrier between levels
         a.t0 = a.t1 = a.lo = a.hi = 0;
-        KCALL(EX, scalar_sweep_persistent<S>, a, s->nvars, s->nfvars, s->ndims, rans ? 1 : 0, s->d_lev_off.p, L,
+        KCALL(EX, scalar_sweep_persistent<S>, a, s->nvars, s->nfvars, s->ndims, sys, s->d_lev_off.p, L,
               s->d_bar.p, s->d_err.p, kBarrierMaxSpin, s->stream());
         return;
     }
@@ -340,7 +344,7 @@ void lusgs_sweep(FlowSys s, bool rans, bool upper, double kappa, bool persistent
         a.t1 = s->sch.lev_off[l + 1];
         a.lo = a.t0;
         a.hi = a.t1;
-        KCALL(EX, scalar_sweep<S>, a, s->nvars, s->nfvars, s->ndims, rans ? 1 : 0, s->block, s->stream());
+        KCALL(EX, scalar_sweep<S>, a, s->nvars, s->nfvars, s->ndims, sys, s->block, s->stream());
     }
 }
 
@@ -473,6 +477,17 @@ void blusgs_residual(FlowSys s, const Sx *x, R *r_out, double *rnorm, double *bn
 }  // namespace
 
 namespace {
+// Whether a run loop with the turbulence system sweeps both systems in one
+// pass per level: with one thread per cell (launch variants 0-2 and the
+// persistent kernel).  The two systems' sweeps read only the state and
+// their own increments, so sweeping them together gives the values of
+// NS Prepare, lower, upper, then RANS Prepare, lower, upper, while every
+// neighbour index, face normal, area and mean-flow state is loaded once
+// instead of twice.
+bool run_sweeps_both(FlowSys s, bool persistent) {
+    return s->ntvars > 0 && (persistent || s->variant <= 2);
+}
+
 // One pseudo-time iteration on device-resident state (see UCFDLUSGS_Run).
 template <typename S, bool EX>
 void lusgs_iteration(FlowSys s, bool rans, double kappa, double *resid_slot, bool persistent) {
@@ -480,19 +495,26 @@ void lusgs_iteration(FlowSys s, bool rans, double kappa, double *resid_slot, boo
     cudaStream_t st = s->stream();
     const size_t n = (size_t)s->nvars * s->N;
     UCFD_CUDA(cudaMemcpyAsync(w.du.p, w.rhs0.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
-    lusgs_prepare<S, EX>(s, false, kappa, w.base.p);
-    lusgs_sweep<S, EX>(s, false, false, kappa, persistent);
-    lusgs_sweep<S, EX>(s, false, true, kappa, persistent);
-    if (rans) {
-        lusgs_prepare<S, EX>(s, true, kappa, w.base.p);
-        lusgs_sweep<S, EX>(s, true, false, kappa, persistent);
-        lusgs_sweep<S, EX>(s, true, true, kappa, persistent);
+    if (rans && run_sweeps_both(s, persistent)) {
+        KCALL(EX, fs_lusgs_prepare_both<S>, s->N, s->P, s->nfvars, s->nvars, (S)kappa, s->d_nei.p, geo_fa<S>(s),
+              geo_rv<S>(s), w.lamN.p, w.lamT.p, w.base.p, w.diag.p, st);
+        lusgs_sweep<S, EX>(s, 2, false, kappa, persistent);
+        lusgs_sweep<S, EX>(s, 2, true, kappa, persistent);
+    } else {
+        lusgs_prepare<S, EX>(s, false, kappa, w.base.p);
+        lusgs_sweep<S, EX>(s, 0, false, kappa, persistent);
+        lusgs_sweep<S, EX>(s, 0, true, kappa, persistent);
+        if (rans) {
+            lusgs_prepare<S, EX>(s, true, kappa, w.base.p);
+            lusgs_sweep<S, EX>(s, 1, false, kappa, persistent);
+            lusgs_sweep<S, EX>(s, 1, true, kappa, persistent);
+        }
     }
     // u += du over the swept variables, ||du|| in FP64; FP32 mode adds into
     // the FP64 master state and rounds the working copy from it
     const int v1 = rans ? s->nvars : s->nfvars;
     if constexpr (std::is_same<S, float>::value)
-        kfast::axpy_master((long long)v1 * s->N, w.du.p, w.u64.p, w.u.p, s->part.p, resid_slot, st);
+        kfast::axpy_master((long long)v1 * s->N, w.du.p, w.u.p, w.ulo.p, s->part.p, resid_slot, st);
     else
         kfast::axpy_norm<S>((long long)v1 * s->N, w.du.p, w.u.p, s->part.p, resid_slot, st);
 }
@@ -815,17 +837,21 @@ ucfd_status_t UCFDFlowSysAutotune(FlowSys s, int reps, UCFDLaunchConfig *best) {
         dispatch(s, [&]<typename S, bool EX>() {
             Work<S> &w = work<S>(s);
             UCFD_REQUIRE(w.u.p, "Autotune before Pack");
+            // the loop of the handle's systems: with the turbulence system
+            // when its spectral radius is set
+            const bool rans = s->ntvars > 0 && s->tfspr;
             // the loop writes u, du, diag and the spectral radii: keep them
-            DevBuf<S> su, sdu, sdiag, slam;
-            DevBuf<double> su64;
+            DevBuf<S> su, sdu, sdiag, slam, slamT;
+            DevBuf<S> sulo;
             const size_t nl = (size_t)s->P * s->N;
             const bool had_lam = w.lamN.p != nullptr;
+            const bool had_lamT = w.lamT.p != nullptr;
             su.ensure(n);
             sdu.ensure(n);
             sdiag.ensure(n);
-            if (w.u64.p) {
-                su64.ensure(n);
-                UCFD_CUDA(cudaMemcpyAsync(su64.p, w.u64.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+            if (w.ulo.p) {
+                sulo.ensure(n);
+                UCFD_CUDA(cudaMemcpyAsync(sulo.p, w.ulo.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
             }
             UCFD_CUDA(cudaMemcpyAsync(su.p, w.u.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
             UCFD_CUDA(cudaMemcpyAsync(sdu.p, w.du.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
@@ -834,7 +860,11 @@ ucfd_status_t UCFDFlowSysAutotune(FlowSys s, int reps, UCFDLaunchConfig *best) {
                 slam.ensure(nl);
                 UCFD_CUDA(cudaMemcpyAsync(slam.p, w.lamN.p, nl * sizeof(S), cudaMemcpyDeviceToDevice, st));
             }
-            run_gather_lambda<S>(s, false, 1);
+            if (rans && had_lamT) {
+                slamT.ensure(nl);
+                UCFD_CUDA(cudaMemcpyAsync(slamT.p, w.lamT.p, nl * sizeof(S), cudaMemcpyDeviceToDevice, st));
+            }
+            run_gather_lambda<S>(s, rans, 1);
             // variant 0: unconstrained registers; 1 / 2: at most 80 / 64 registers;
             // 3 / 4: two threads per cell; 5: one thread per active face (the
             // persistent kernel stays one per cell)
@@ -843,7 +873,7 @@ ucfd_status_t UCFDFlowSysAutotune(FlowSys s, int reps, UCFDLaunchConfig *best) {
                 for (int b : kTuneBlocks) {
                     s->block = b;
                     run_graph_drop(s);
-                    run_graph_build<S, EX>(s, false, 1.0);
+                    run_graph_build<S, EX>(s, rans, 1.0);
                     const double ms = time_ms(st, reps, [&] { UCFD_CUDA(cudaGraphLaunch(s->run_exec, st)); });
                     consider(ms, b, v, 0);
                 }
@@ -852,17 +882,20 @@ ucfd_status_t UCFDFlowSysAutotune(FlowSys s, int reps, UCFDLaunchConfig *best) {
                 // the persistent kernel has its own fixed launch shape
                 run_persistent_begin(s);
                 const double pms =
-                    time_ms(st, reps, [&] { lusgs_iteration<S, EX>(s, false, 1.0, s->red.p, true); });
+                    time_ms(st, reps, [&] { lusgs_iteration<S, EX>(s, rans, 1.0, s->red.p, true); });
                 run_persistent_check(s);
                 consider(pms, 256, v, 1);
             }
             UCFD_CUDA(cudaMemcpyAsync(w.u.p, su.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
-            if (w.u64.p) UCFD_CUDA(cudaMemcpyAsync(w.u64.p, su64.p, n * sizeof(double), cudaMemcpyDeviceToDevice, st));
+            if (w.ulo.p) UCFD_CUDA(cudaMemcpyAsync(w.ulo.p, sulo.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
             UCFD_CUDA(cudaMemcpyAsync(w.du.p, sdu.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
             UCFD_CUDA(cudaMemcpyAsync(w.diag.p, sdiag.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
             if (had_lam) UCFD_CUDA(cudaMemcpyAsync(w.lamN.p, slam.p, nl * sizeof(S), cudaMemcpyDeviceToDevice, st));
+            if (rans && had_lamT)
+                UCFD_CUDA(cudaMemcpyAsync(w.lamT.p, slamT.p, nl * sizeof(S), cudaMemcpyDeviceToDevice, st));
             UCFD_CUDA(cudaStreamSynchronize(st));
             if (!had_lam) w.lamN.release();
+            if (rans && !had_lamT) w.lamT.release();
         });
     }
     keep.done = true;
@@ -921,8 +954,8 @@ ucfd_status_t UCFDLUSGS_Pack(FlowSys s, UCFDInt eidx, UCFDReal turb_factor, UCFD
         KCALL(EX, fs_lusgs_pack<S>, e.neles, s->nvars, s->nfvars, s->N, turb_factor, a0, ids, s->d_iperm.p, up, rh,
               dt, ds, w.u.p, w.du.p, w.diag.p, st);
         if constexpr (std::is_same<S, float>::value) {
-            w.u64.ensure((size_t)s->nvars * s->N);
-            kfast::state64_pack(e.neles, s->nvars, s->N, ids, s->d_iperm.p, up, w.u64.p, st);
+            w.ulo.ensure((size_t)s->nvars * s->N);
+            kfast::state_lo_pack(e.neles, s->nvars, s->N, ids, s->d_iperm.p, up, w.ulo.p, st);
         }
         const size_t n = (size_t)s->nvars * s->N;
         UCFD_CUDA(cudaMemcpyAsync(w.base.p, w.diag.p, n * sizeof(S), cudaMemcpyDeviceToDevice, st));
@@ -948,61 +981,88 @@ ucfd_status_t UCFDLUSGS_Update(FlowSys s, UCFDInt eidx) {
         Work<S> &w = work<S>(s);
         UCFD_REQUIRE(w.du.p, "Update before Pack");
         // after UCFDLUSGS_Run the device-resident state itself is written back
-        // (FP32 mode: its FP64 master)
-        if (std::is_same<S, float>::value && s->run_state)
-            kfast::fs_lusgs_update<double>(e.neles, s->nvars, s->N, ids, s->d_iperm.p, w.u64.p, up, 1, st);
-        else
-            KCALL(EX, fs_lusgs_update<S>, e.neles, s->nvars, s->N, ids, s->d_iperm.p, s->run_state ? w.u.p : w.du.p,
-                  up, s->run_state ? 1 : 0, st);
+        // (FP32 mode: its float-float pair, summed in FP64)
+        if constexpr (std::is_same<S, float>::value) {
+            if (s->run_state) {
+                kfast::state_ff_update(e.neles, s->nvars, s->N, ids, s->d_iperm.p, w.u.p, w.ulo.p, up, st);
+                return;
+            }
+        }
+        KCALL(EX, fs_lusgs_update<S>, e.neles, s->nvars, s->N, ids, s->d_iperm.p, s->run_state ? w.u.p : w.du.p, up,
+              s->run_state ? 1 : 0, st);
     });
     if (!dev) copy_d2h(e.uptsb, up, nv * sizeof(double), st);
     finish(s, !dev);
     UCFD_API_END
 }
 
-static ucfd_status_t lusgs_prepare_api(FlowSys s, bool rans, UCFDReal kappa) {
+// sys: 0 mean-flow system (NS*), 1 turbulence system (RANS*), 2 both
+// (NSRANS*: one kernel over the faces, the values of NS* then RANS*).
+static ucfd_status_t lusgs_prepare_api(FlowSys s, int sys, UCFDReal kappa) {
     UCFD_API_BEGIN
     need_mode(s, MODE_LUSGS);
     build_topology(s);
-    const double *lf = rans ? s->tfspr : s->fspr;
-    UCFD_REQUIRE(lf, "%s is not set", rans ? "tfspr" : "fspr");
-    if (rans) UCFD_REQUIRE(s->ntvars > 0, "RANS prepare needs turbulence variables (nvars > nfvars)");
+    UCFD_REQUIRE(sys == 1 || s->fspr, "fspr is not set");
+    UCFD_REQUIRE(sys == 0 || s->tfspr, "tfspr is not set");
+    if (sys != 0) UCFD_REQUIRE(s->ntvars > 0, "RANS prepare needs turbulence variables (nvars > nfvars)");
     cudaStream_t st = s->stream();
-    static thread_local DevBuf<double> stage;
-    const double *lfd = device_view<double>(lf, (size_t)s->nfaces, stage, st);
+    static thread_local DevBuf<double> stageN, stageT;
+    const double *lfN = sys != 1 ? device_view<double>(s->fspr, (size_t)s->nfaces, stageN, st) : nullptr;
+    const double *lfT = sys != 0 ? device_view<double>(s->tfspr, (size_t)s->nfaces, stageT, st) : nullptr;
     dispatch(s, [&]<typename S, bool EX>() {
         Work<S> &w = work<S>(s);
         UCFD_REQUIRE(w.diag.p, "Prepare before Pack");
-        DevBuf<S> &lam = rans ? w.lamT : w.lamN;
-        lam.ensure((size_t)s->P * s->N);
-        kfast::gather_idx<S>((long long)s->P * s->N, s->d_slot.p, lfd, lam.p, st);
-        lusgs_prepare<S, EX>(s, rans, kappa, nullptr);
+        const long long nl = (long long)s->P * s->N;
+        if (lfN) {
+            w.lamN.ensure((size_t)nl);
+            kfast::gather_idx<S>(nl, s->d_slot.p, lfN, w.lamN.p, st);
+        }
+        if (lfT) {
+            w.lamT.ensure((size_t)nl);
+            kfast::gather_idx<S>(nl, s->d_slot.p, lfT, w.lamT.p, st);
+        }
+        if (sys == 2)
+            KCALL(EX, fs_lusgs_prepare_both<S>, s->N, s->P, s->nfvars, s->nvars, (S)kappa, s->d_nei.p, geo_fa<S>(s),
+                  geo_rv<S>(s), w.lamN.p, w.lamT.p, (const S *)nullptr, w.diag.p, st);
+        else
+            lusgs_prepare<S, EX>(s, sys == 1, kappa, nullptr);
     });
-    finish(s, !is_device_ptr(lf));
+    finish(s, (lfN && !is_device_ptr(s->fspr)) || (lfT && !is_device_ptr(s->tfspr)));
     UCFD_API_END
 }
 
-static ucfd_status_t lusgs_sweep_api(FlowSys s, bool rans, bool upper, UCFDReal kappa) {
+static ucfd_status_t lusgs_sweep_api(FlowSys s, int sys, bool upper, UCFDReal kappa) {
     UCFD_API_BEGIN
     need_mode(s, MODE_LUSGS);
     build_topology(s);
-    if (rans) UCFD_REQUIRE(s->ntvars > 0, "RANS sweep needs turbulence variables (nvars > nfvars)");
+    if (sys != 0) UCFD_REQUIRE(s->ntvars > 0, "RANS sweep needs turbulence variables (nvars > nfvars)");
     dispatch(s, [&]<typename S, bool EX>() {
         Work<S> &w = work<S>(s);
         UCFD_REQUIRE(w.du.p, "sweep before Pack");
-        UCFD_REQUIRE((rans ? w.lamT.p : w.lamN.p), "sweep before %s", rans ? "RANSPrepare" : "NSPrepare");
-        lusgs_sweep<S, EX>(s, rans, upper, kappa);
+        UCFD_REQUIRE(sys == 1 || w.lamN.p, "sweep before NSPrepare");
+        UCFD_REQUIRE(sys == 0 || w.lamT.p, "sweep before RANSPrepare");
+        if (sys == 2 && s->variant > 2) {
+            // the one-pass kernel is one thread per cell; the other launch
+            // variants sweep the two systems one after the other
+            lusgs_sweep<S, EX>(s, 0, upper, kappa);
+            lusgs_sweep<S, EX>(s, 1, upper, kappa);
+        } else {
+            lusgs_sweep<S, EX>(s, sys, upper, kappa);
+        }
     });
     finish(s);
     UCFD_API_END
 }
 
-ucfd_status_t UCFDLUSGS_NSPrepare(FlowSys s, UCFDReal kappa) { return lusgs_prepare_api(s, false, kappa); }
-ucfd_status_t UCFDLUSGS_RANSPrepare(FlowSys s, UCFDReal kappa) { return lusgs_prepare_api(s, true, kappa); }
-ucfd_status_t UCFDLUSGS_NSLowerSweep(FlowSys s, UCFDReal kappa) { return lusgs_sweep_api(s, false, false, kappa); }
-ucfd_status_t UCFDLUSGS_NSUpperSweep(FlowSys s, UCFDReal kappa) { return lusgs_sweep_api(s, false, true, kappa); }
-ucfd_status_t UCFDLUSGS_RANSLowerSweep(FlowSys s, UCFDReal kappa) { return lusgs_sweep_api(s, true, false, kappa); }
-ucfd_status_t UCFDLUSGS_RANSUpperSweep(FlowSys s, UCFDReal kappa) { return lusgs_sweep_api(s, true, true, kappa); }
+ucfd_status_t UCFDLUSGS_NSPrepare(FlowSys s, UCFDReal kappa) { return lusgs_prepare_api(s, 0, kappa); }
+ucfd_status_t UCFDLUSGS_RANSPrepare(FlowSys s, UCFDReal kappa) { return lusgs_prepare_api(s, 1, kappa); }
+ucfd_status_t UCFDLUSGS_NSLowerSweep(FlowSys s, UCFDReal kappa) { return lusgs_sweep_api(s, 0, false, kappa); }
+ucfd_status_t UCFDLUSGS_NSUpperSweep(FlowSys s, UCFDReal kappa) { return lusgs_sweep_api(s, 0, true, kappa); }
+ucfd_status_t UCFDLUSGS_RANSLowerSweep(FlowSys s, UCFDReal kappa) { return lusgs_sweep_api(s, 1, false, kappa); }
+ucfd_status_t UCFDLUSGS_RANSUpperSweep(FlowSys s, UCFDReal kappa) { return lusgs_sweep_api(s, 1, true, kappa); }
+ucfd_status_t UCFDLUSGS_NSRANSPrepare(FlowSys s, UCFDReal kappa) { return lusgs_prepare_api(s, 2, kappa); }
+ucfd_status_t UCFDLUSGS_NSRANSLowerSweep(FlowSys s, UCFDReal kappa) { return lusgs_sweep_api(s, 2, false, kappa); }
+ucfd_status_t UCFDLUSGS_NSRANSUpperSweep(FlowSys s, UCFDReal kappa) { return lusgs_sweep_api(s, 2, true, kappa); }
 
 ucfd_status_t UCFDLUSGS_Run(FlowSys s, UCFDInt niter, UCFDReal kappa, int rans, int mode, UCFDReal *resid) {
     UCFD_API_BEGIN
@@ -1112,7 +1172,10 @@ static ucfd_status_t blusgs_prepare_api(FlowSys s, bool turb) {
     cudaStream_t st = s->stream();
     const int B = turb ? s->ntvars : s->nfvars;
     static thread_local DevBuf<double> stage;
-    const double *jd = device_view<double>(jm, (size_t)2 * B * B * s->nfaces, stage, st);
+    // page-locked host Jacobians are read in place by the transpose kernel
+    // under UCFD_HOST_MAP; otherwise staged
+    const double *jd = (const double *)host_mapped(jm);
+    if (!jd) jd = device_view<double>(jm, (size_t)2 * B * B * s->nfaces, stage, st);
     dispatch(s, [&]<typename S, bool EX>() {
         Work<S> &w = work<S>(s);
         UCFD_REQUIRE(w.rhs.p, "Prepare before Pack");

@@ -46,6 +46,8 @@ struct ScalarSweepArgs {
     const T *rv;           // [ld] reciprocal volume or nullptr
     const T *nrm;          // [nface][ndims][ld] outward unit normals
     const T *lam;          // [nface][ld] spectral radius
+    const T *tlam;         // [nface][ld] spectral radius of the turbulence system when one launch
+                           // sweeps both systems (rans == 2), else unused
     const T *u;            // [nvars][ld]
     const T *nbsrc;        // [nvars][ld] neighbour increments
     const T *own_in;       // [nvars][ld]

@@ -16,6 +16,9 @@ template void fs_lusgs_pack<double>(int, int, int, long long, double, double, co
 template void fs_lusgs_update<double>(int, int, long long, const int *, const int *, const double *, double *, int, cudaStream_t);
 template void fs_lusgs_prepare<double>(long long, int, int, int, double, const int *, const double *, const double *,
                                        const double *, const double *, double *, cudaStream_t);
+template void fs_lusgs_prepare_both<double>(long long, int, int, int, double, const int *, const double *,
+                                            const double *, const double *, const double *, const double *,
+                                            double *, cudaStream_t);
 template void gather_idx<double>(long long, const int *, const double *, double *, cudaStream_t);
 template void fs_blusgs_pack<double>(int, int, int, long long, double, const int *, const int *, const double *,
                                      const double *, double *, double *, double *, cudaStream_t);

@@ -19,6 +19,8 @@ namespace kfast {
                                      cudaStream_t);                                                            \
     template void fs_lusgs_prepare<T>(long long, int, int, int, T, const int *, const T *, const T *,          \
                                       const T *, const T *, T *, cudaStream_t);                                \
+    template void fs_lusgs_prepare_both<T>(long long, int, int, int, T, const int *, const T *, const T *,     \
+                                           const T *, const T *, const T *, T *, cudaStream_t);                \
     template void gather_idx<T>(long long, const int *, const double *, T *, cudaStream_t);                    \
     template void fs_blusgs_pack<T>(int, int, int, long long, double, const int *, const int *,                \
                                     const double *, const double *, T *, double *, double *, cudaStream_t);    \

@@ -129,7 +129,14 @@ using ScalarSweepArgs = ::ucfd::ScalarSweepArgs<T>;
 // lower_sweep / upper_sweep of lusgs.c:157-257 for one level (or colour):
 // every cell of the range is independent of the others.
 template <typename T, int NV, int NFV, int NDIMS, bool RANS, bool COHERENT = false>
-__device__ __forceinline__ void scalar_sweep_cell(const ScalarSweepArgs<T> &a, int t);
+__device__ __forceinline__ void scalar_sweep_cell(const ScalarSweepArgs<T> &a, int t, int lo, int hi);
+
+// Both systems of one level in one pass (the mean-flow variables with the
+// spectral radius lam, the turbulence variables with tlam): the two sweeps
+// are independent of each other, since each reads only the state u and its
+// own increments, so this gives every value the separate sweeps give.
+template <typename T, int NV, int NFV, int NDIMS, bool COHERENT = false>
+__device__ __forceinline__ void scalar_sweep_cell_both(const ScalarSweepArgs<T> &a, int t, int lo, int hi);
 
 // MINB: minimum resident blocks of 256 threads per SM the compiler must
 // allow (1: no register cap, about 106 registers; 3 / 4: at most 80 / 64
@@ -139,7 +146,7 @@ template <typename T, int NV, int NFV, int NDIMS, bool RANS, int MINB = 1>
 __global__ void __launch_bounds__(256, MINB) scalar_sweep_kernel(ScalarSweepArgs<T> a) {
     const int t = a.t0 + blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.t1) return;
-    scalar_sweep_cell<T, NV, NFV, NDIMS, RANS>(a, t);
+    scalar_sweep_cell<T, NV, NFV, NDIMS, RANS>(a, t, a.lo, a.hi);
 }
 
 // Grid-wide barrier for a cooperative launch (all blocks co-resident).
@@ -184,19 +191,20 @@ __device__ inline bool grid_barrier_bounded(unsigned *count, unsigned *gen, int 
 // One whole sweep (every level, ascending or descending) in one
 // cooperative launch: the blocks stride over the cells of a level, then
 // meet at the bounded grid barrier before the next level.
-template <typename T, int NV, int NFV, int NDIMS, bool RANS, int MINB = 1>
+// BOTH: both systems per cell (scalar_sweep_cell_both).
+template <typename T, int NV, int NFV, int NDIMS, bool RANS, int MINB = 1, bool BOTH = false>
 __global__ void __launch_bounds__(256, MINB) scalar_sweep_persistent_kernel(ScalarSweepArgs<T> a, const int *lev_off,
                                                                       int nlev, unsigned *bar, int *err,
                                                                       long long max_spin) {
+    // the level's bounds are passed on their own: a copy of the whole
+    // argument struct per level would live in registers
     for (int q = 0; q < nlev; ++q) {
         const int l = a.upper ? nlev - 1 - q : q;
-        ScalarSweepArgs<T> b = a;
-        b.t0 = lev_off[l];
-        b.t1 = lev_off[l + 1];
-        b.lo = b.t0;
-        b.hi = b.t1;
-        for (int t = b.t0 + blockIdx.x * blockDim.x + threadIdx.x; t < b.t1; t += gridDim.x * blockDim.x)
-            scalar_sweep_cell<T, NV, NFV, NDIMS, RANS, true>(b, t);
+        const int t0 = lev_off[l], t1 = lev_off[l + 1];
+        for (int t = t0 + blockIdx.x * blockDim.x + threadIdx.x; t < t1; t += gridDim.x * blockDim.x) {
+            if constexpr (BOTH) scalar_sweep_cell_both<T, NV, NFV, NDIMS, true>(a, t, t0, t1);
+            else scalar_sweep_cell<T, NV, NFV, NDIMS, RANS, true>(a, t, t0, t1);
+        }
         if (q + 1 < nlev && !grid_barrier_bounded(bar, bar + 1, err, max_spin)) return;
     }
 }
@@ -212,7 +220,8 @@ __device__ __forceinline__ double mul_rn(double x, double y) { return __dmul_rn(
 // this sweep (a lower colour / level for the lower sweep, a higher one for
 // the upper sweep).
 template <typename T, int NB>
-__device__ __forceinline__ unsigned active_faces(const ScalarSweepArgs<T> &a, int ci, const int *nb) {
+__device__ __forceinline__ unsigned active_faces(const ScalarSweepArgs<T> &a, int lo, int hi, int ci,
+                                                 const int *nb) {
     unsigned m = 0;
 #pragma unroll
     for (int q = 0; q < NB; ++q) {
@@ -221,7 +230,7 @@ __device__ __forceinline__ unsigned active_faces(const ScalarSweepArgs<T> &a, in
             const int cn = nb[q] >= 0 ? __ldg(a.lcolor + nb[q]) : ci;
             act = a.upper ? (cn > ci) : (cn < ci);
         } else {
-            act = nb[q] >= 0 && (a.upper ? (nb[q] >= a.hi) : (nb[q] < a.lo));
+            act = nb[q] >= 0 && (a.upper ? (nb[q] >= hi) : (nb[q] < lo));
         }
         m |= act ? (1u << q) : 0u;
     }
@@ -353,8 +362,8 @@ __device__ __forceinline__ int face_terms(const ScalarSweepArgs<T> &a, int i, T 
 // In the level-major layout the first level of a lower sweep and the last
 // of an upper sweep have no active face at all.
 template <typename T>
-__device__ __forceinline__ bool no_active_face(const ScalarSweepArgs<T> &a) {
-    return !a.lcolor && (a.upper ? a.hi >= a.ld : a.lo <= 0);
+__device__ __forceinline__ bool no_active_face(const ScalarSweepArgs<T> &a, int lo, int hi) {
+    return !a.lcolor && (a.upper ? hi >= a.ld : lo <= 0);
 }
 
 // The cell's new increment from its own input, diagonal and df.
@@ -364,7 +373,7 @@ __device__ __forceinline__ T sweep_result(bool upper, T own, T df, T dg) {
 }
 
 template <typename T, int NV, int NFV, int NDIMS, bool RANS, bool COHERENT>
-__device__ __forceinline__ void scalar_sweep_cell(const ScalarSweepArgs<T> &a, int t) {
+__device__ __forceinline__ void scalar_sweep_cell(const ScalarSweepArgs<T> &a, int t, int lo, int hi) {
     constexpr int NV0 = RANS ? NFV : 0;
     constexpr int DNV = RANS ? NV - NFV : NFV;
     const long long ld = a.ld;
@@ -385,13 +394,13 @@ __device__ __forceinline__ void scalar_sweep_cell(const ScalarSweepArgs<T> &a, i
     // gathers' latency); the terms are added to df in the reference's face
     // order.
     constexpr int FB = 3;
-    if (no_active_face(a)) {
+    if (no_active_face(a, lo, hi)) {
     } else if (a.nface <= 2 * FB) {
         // every neighbour index of the cell up front, then its active faces
         int nba[2 * FB];
 #pragma unroll
         for (int p = 0; p < 2 * FB; ++p) nba[p] = p < a.nface ? __ldg(a.nei + p * ld + i) : -1;
-        unsigned m = active_faces<T, 2 * FB>(a, ci, nba);
+        unsigned m = active_faces<T, 2 * FB>(a, lo, hi, ci, nba);
         face_terms<T, NV, NFV, NDIMS, RANS, COHERENT, 2 * FB, FB, true>(a, i, rvi, 0, nba, m, nullptr, df);
         if (m) face_terms<T, NV, NFV, NDIMS, RANS, COHERENT, 2 * FB, FB, true>(a, i, rvi, 0, nba, m, nullptr, df);
     } else {
@@ -399,12 +408,113 @@ __device__ __forceinline__ void scalar_sweep_cell(const ScalarSweepArgs<T> &a, i
             int nb[FB];
 #pragma unroll
             for (int q = 0; q < FB; ++q) nb[q] = (f0 + q < a.nface) ? __ldg(a.nei + (f0 + q) * ld + i) : -1;
-            unsigned m = active_faces<T, FB>(a, ci, nb);
+            unsigned m = active_faces<T, FB>(a, lo, hi, ci, nb);
             face_terms<T, NV, NFV, NDIMS, RANS, COHERENT, FB, FB, true>(a, i, rvi, f0, nb, m, nullptr, df);
         }
     }
 #pragma unroll
     for (int k = 0; k < DNV; ++k) a.own_out[(k + NV0) * ld + i] = sweep_result(a.upper != 0, own[k], df[k], dg[k]);
+}
+
+// face_terms for both systems at once: each active face's neighbour index,
+// normal, area and mean-flow state are loaded once and give the face's
+// mean-flow term (spectral radius lam) and turbulence term (tlam), each
+// added to its own sums in face order.  The terms are formed by face_term
+// exactly as the single-system sweeps form them.  FP64 also loads the
+// turbulence state, which its flux difference reads; in FP32 only the
+// increments of the turbulence variables move.
+template <typename T, int NV, int NFV, int NDIMS, bool COHERENT, int NB, int KB>
+__device__ __forceinline__ void face_terms_both(const ScalarSweepArgs<T> &a, int i, T rvi, int f0, const int *nb,
+                                                unsigned &m, T *df) {
+    const long long ld = a.ld;
+    bool on[KB];
+    int fk[KB], gk[KB];
+#pragma unroll
+    for (int k = 0; k < KB; ++k) {
+        on[k] = m != 0u;
+        const int q = on[k] ? __ffs(m) - 1 : 0;
+        m &= m - 1u;
+        int g = nb[0];
+#pragma unroll
+        for (int r = 1; r < NB; ++r) g = (q == r) ? nb[r] : g;
+        fk[k] = f0 + q;
+        gk[k] = g;
+    }
+    T uu[KB][NV], dn[KB][NV], nf[KB][NDIMS], fv[KB], kl[KB], klt[KB];
+#pragma unroll
+    for (int k = 0; k < KB; ++k) {
+        if (!on[k]) continue;
+        const int g = gk[k];
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+            uu[k][v] = (v < NFV || sizeof(T) == 8) ? __ldg(a.u + v * ld + g) : T(0);
+#pragma unroll
+        for (int j = 0; j < NV; ++j) dn[k][j] = COHERENT ? __ldcg(a.nbsrc + j * ld + g) : a.nbsrc[j * ld + g];
+        const int f = fk[k];
+#pragma unroll
+        for (int d = 0; d < NDIMS; ++d) nf[k][d] = __ldg(a.nrm + (f * NDIMS + d) * ld + i);
+        fv[k] = __ldg(a.fa + f * ld + i);
+        kl[k] = __ldg(a.lam + f * ld + i);
+        klt[k] = __ldg(a.tlam + f * ld + i);
+    }
+#pragma unroll
+    for (int k = 0; k < KB; ++k) {
+        if (!on[k]) continue;
+        const T fvk = a.rv ? fv[k] * rvi : fv[k];
+        T tn[NFV], tt[NV - NFV];
+        // the mean-flow flux may raise the energy of uu[k] to the pressure
+        // floor (as its own sweep does to its copy); the turbulence flux
+        // does not read the energy
+        face_term<T, NV, NFV, NDIMS, false>(a, uu[k], dn[k], nf[k], fvk, kl[k], tn);
+        face_term<T, NV, NFV, NDIMS, true>(a, uu[k], dn[k] + NFV, nf[k], fvk, klt[k], tt);
+#pragma unroll
+        for (int j = 0; j < NFV; ++j) df[j] += tn[j];
+#pragma unroll
+        for (int j = 0; j < NV - NFV; ++j) df[NFV + j] += tt[j];
+    }
+}
+
+template <typename T, int NV, int NFV, int NDIMS, bool COHERENT>
+__device__ __forceinline__ void scalar_sweep_cell_both(const ScalarSweepArgs<T> &a, int t, int lo, int hi) {
+    const long long ld = a.ld;
+    const int i = a.cells ? __ldg(a.cells + t) : t;
+    const int ci = a.lcolor ? __ldg(a.lcolor + i) : 0;
+    T own[NV], dg[NV], df[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        own[k] = a.own_in[k * ld + i];
+        dg[k] = a.diag[k * a.diag_vs + i];
+        df[k] = T(0);
+    }
+    const T rvi = a.rv ? __ldg(a.rv + i) : T(1);
+    constexpr int FB = 3;
+    if (no_active_face(a, lo, hi)) {
+    } else if (a.nface <= 2 * FB) {
+        int nba[2 * FB];
+#pragma unroll
+        for (int p = 0; p < 2 * FB; ++p) nba[p] = p < a.nface ? __ldg(a.nei + p * ld + i) : -1;
+        unsigned m = active_faces<T, 2 * FB>(a, lo, hi, ci, nba);
+        face_terms_both<T, NV, NFV, NDIMS, COHERENT, 2 * FB, FB>(a, i, rvi, 0, nba, m, df);
+        if (m) face_terms_both<T, NV, NFV, NDIMS, COHERENT, 2 * FB, FB>(a, i, rvi, 0, nba, m, df);
+    } else {
+        for (int f0 = 0; f0 < a.nface; f0 += FB) {
+            int nb[FB];
+#pragma unroll
+            for (int q = 0; q < FB; ++q) nb[q] = (f0 + q < a.nface) ? __ldg(a.nei + (f0 + q) * ld + i) : -1;
+            unsigned m = active_faces<T, FB>(a, lo, hi, ci, nb);
+            face_terms_both<T, NV, NFV, NDIMS, COHERENT, FB, FB>(a, i, rvi, f0, nb, m, df);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < NV; ++k) a.own_out[k * ld + i] = sweep_result(a.upper != 0, own[k], df[k], dg[k]);
+}
+
+// One level of both systems' sweeps, one thread per cell.
+template <typename T, int NV, int NFV, int NDIMS, int MINB = 1>
+__global__ void __launch_bounds__(256, MINB) scalar_sweep_both_kernel(ScalarSweepArgs<T> a) {
+    const int t = a.t0 + blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.t1) return;
+    scalar_sweep_cell_both<T, NV, NFV, NDIMS>(a, t, a.lo, a.hi);
 }
 
 // One level of the sweep with one thread per active face.  A block owns
@@ -517,7 +627,7 @@ __global__ void __launch_bounds__(256, MINB) scalar_sweep_pair_kernel(ScalarSwee
     }
     int n = 0;  // active faces of this lane, terms in c[0 .. n-1] in face order
     T c[FB][DNV];
-    if (live && !no_active_face(a)) {
+    if (live && !no_active_face(a, a.lo, a.hi)) {
         const T rvi = a.rv ? __ldg(a.rv + i) : T(1);
         int nb[FB];
 #pragma unroll
@@ -525,7 +635,7 @@ __global__ void __launch_bounds__(256, MINB) scalar_sweep_pair_kernel(ScalarSwee
             const int p = h * FB + q;
             nb[q] = p < a.nface ? __ldg(a.nei + p * ld + i) : -1;
         }
-        unsigned m = active_faces<T, FB>(a, ci, nb);
+        unsigned m = active_faces<T, FB>(a, a.lo, a.hi, ci, nb);
         n = face_terms<T, NV, NFV, NDIMS, RANS, false, FB, FB, false>(a, i, rvi, h * FB, nb, m, c, nullptr);
     }
     // the odd lane's terms to the even lane
@@ -610,6 +720,57 @@ __global__ void fs_lusgs_update_kernel(int neles, int nvars, long long N, const 
     }
 }
 
+// pre_lusgs's sum over a cell's faces (lusgs.c:87-113): slots p in order,
+// up to the first padding slot, of 0.5 * (lam * kappa) * fa * rv, for one
+// spectral radius (sd) or two (sd from lam, st from tlam).  Rows of up to 8
+// slots issue every load before the first sum (one round trip instead of
+// one per face, the same sums in the same order); wider rows loop.
+template <typename T, bool TWO>
+__device__ __forceinline__ void prepare_sums(long long N, int maxdeg, long long k, T kappa, const int *nei,
+                                             const T *fa, const T *rv, const T *lam, const T *tlam, T &sd,
+                                             T &st) {
+    sd = T(0);
+    st = T(0);
+    const T r = rv[k];
+    constexpr int PM = 8;
+    if (maxdeg <= PM) {
+        int nb[PM];
+        T f[PM], l[PM], lt[PM];
+#pragma unroll
+        for (int p = 0; p < PM; ++p) {
+            const bool in = p < maxdeg;
+            nb[p] = in ? nei[p * N + k] : -1;
+            f[p] = in ? fa[p * N + k] : T(0);
+            l[p] = in ? lam[p * N + k] : T(0);
+            if constexpr (TWO) lt[p] = in ? tlam[p * N + k] : T(0);
+        }
+        bool live = true;
+#pragma unroll
+        for (int p = 0; p < PM; ++p) {
+            live = live && nb[p] >= 0;
+            if (live) {
+                const T lamf = l[p] * kappa;
+                sd += T(0.5) * lamf * f[p] * r;
+                if constexpr (TWO) {
+                    const T lamt = lt[p] * kappa;
+                    st += T(0.5) * lamt * f[p] * r;
+                }
+            }
+        }
+        return;
+    }
+    for (int p = 0; p < maxdeg; ++p) {
+        if (nei[p * N + k] < 0) break;
+        const T f = fa[p * N + k];
+        const T lamf = lam[p * N + k] * kappa;
+        sd += T(0.5) * lamf * f * r;
+        if constexpr (TWO) {
+            const T lamt = tlam[p * N + k] * kappa;
+            st += T(0.5) * lamt * f * r;
+        }
+    }
+}
+
 // pre_lusgs: lusgs.c:87-113.  lam is the per cell-face copy of lambdaf.
 // With base != nullptr the result is base + sd (a pseudo-time loop
 // re-preparing from the packed diagonal), otherwise diag += sd.
@@ -619,16 +780,30 @@ __global__ void fs_lusgs_prepare_kernel(long long N, int maxdeg, int nv0, int nv
                                         const T *base, T *diag) {
     const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (k >= N) return;
-    T sd = T(0);
-    for (int p = 0; p < maxdeg; ++p) {
-        if (nei[p * N + k] < 0) break;
-        const T lamf = lam[p * N + k] * kappa;
-        sd += T(0.5) * lamf * fa[p * N + k] * rv[k];
-    }
+    T sd, st;
+    prepare_sums<T, false>(N, maxdeg, k, kappa, nei, fa, rv, lam, nullptr, sd, st);
     if (base)
         for (int v = nv0; v < nv1; ++v) diag[k + v * N] = base[k + v * N] + sd;
     else
         for (int v = nv0; v < nv1; ++v) diag[k + v * N] += sd;
+}
+
+// pre_lusgs of both systems in one pass over the faces: the mean-flow
+// variables [0, nfv) from lam, the turbulence variables [nfv, nv) from
+// tlam, each sum formed as fs_lusgs_prepare_kernel forms it;
+// diag = base + sum, or diag += sum without base.
+template <typename T>
+__global__ void fs_lusgs_prepare_both_kernel(long long N, int maxdeg, int nfv, int nv, T kappa, const int *nei,
+                                             const T *fa, const T *rv, const T *lam, const T *tlam, const T *base,
+                                             T *diag) {
+    const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    T sd, st;
+    prepare_sums<T, true>(N, maxdeg, k, kappa, nei, fa, rv, lam, tlam, sd, st);
+    if (base)
+        for (int v = 0; v < nv; ++v) diag[k + v * N] = base[k + v * N] + (v < nfv ? sd : st);
+    else
+        for (int v = 0; v < nv; ++v) diag[k + v * N] += v < nfv ? sd : st;
 }
 
 // dst[i] = src[idx[i]] (0 where idx[i] < 0): per cell-face copies of

@@ -42,6 +42,10 @@
     void fs_lusgs_prepare(long long N, int maxdeg, int nv0, int nv1, T kappa, const int *nei,      \
                           const T *fa, const T *rv, const T *lam, const T *base, T *diag,          \
                           cudaStream_t s);                                                         \
+    template <typename T>                                                                          \
+    void fs_lusgs_prepare_both(long long N, int maxdeg, int nfv, int nv, T kappa, const int *nei,  \
+                               const T *fa, const T *rv, const T *lam, const T *tlam,              \
+                               const T *base, T *diag, cudaStream_t s);                            \
     template <typename Td>                                                                         \
     void gather_idx(long long n, const int *idx, const double *src, Td *dst, cudaStream_t s);      \
     void pair_reduce(int nblocks, const double *part, double *out, cudaStream_t s);                \
@@ -108,10 +112,12 @@
     void axpy_into(long long n, const Ts *x, double *y, cudaStream_t s);                           \
     template <typename S>                                                                          \
     void axpy_norm(long long n, const S *x, S *y, double *part, double *out, cudaStream_t s);      \
-    void axpy_master(long long n, const float *x, double *y64, float *y, double *part, double *out,  \
+    void axpy_master(long long n, const float *x, float *hi, float *lo, double *part, double *out,   \
                      cudaStream_t s);                                                              \
-    void state64_pack(int neles, int nvars, long long N, const int *cell_ids, const int *iperm,    \
-                      const double *upts, double *u64, cudaStream_t s);                            \
+    void state_lo_pack(int neles, int nvars, long long N, const int *cell_ids, const int *iperm,   \
+                       const double *upts, float *lo, cudaStream_t s);                             \
+    void state_ff_update(int neles, int nvars, long long N, const int *cell_ids, const int *iperm, \
+                         const float *hi, const float *lo, double *upts, cudaStream_t s);          \
     /* ---- adjoint of the colored LU-SGS step ---- */                                            \
     template <typename T>                                                                          \
     void adj_upper(const ::ucfd::AdjArgs &a, int nfv, int ndims, T gamma, T pmin, const T *fnv,    \

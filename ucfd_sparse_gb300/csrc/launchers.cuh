@@ -82,13 +82,32 @@ static void sweep_go(const ::ucfd::ScalarSweepArgs<T> &a, int block, cudaStream_
         scalar_sweep_kernel<T, NV, NFV, NDIMS, RANS, 1><<<grid_for(n, block), block, 0, s>>>(a);
 }
 
+// Both systems in one launch per level (one thread per cell; the register
+// caps of the single-system kernels).
+template <typename T, int NV, int NFV, int NDIMS>
+static void sweep_both_go(const ::ucfd::ScalarSweepArgs<T> &a, int block, cudaStream_t s) {
+    const long long n = a.t1 - a.t0;
+    if (n <= 0) return;
+    if (a.facelist || a.pair)
+        ::ucfd::fail(UCFD_ERR_UNSUPPORTED, "both-system sweep: one thread per cell only");
+    if (a.regcap == 4)
+        scalar_sweep_both_kernel<T, NV, NFV, NDIMS, 4><<<grid_for(n, block), block, 0, s>>>(a);
+    else if (a.regcap == 3)
+        scalar_sweep_both_kernel<T, NV, NFV, NDIMS, 3><<<grid_for(n, block), block, 0, s>>>(a);
+    else
+        scalar_sweep_both_kernel<T, NV, NFV, NDIMS, 1><<<grid_for(n, block), block, 0, s>>>(a);
+}
+
+// rans: 0 mean-flow system, 1 turbulence system, 2 both in one launch.
 template <typename T>
 void scalar_sweep(const ::ucfd::ScalarSweepArgs<T> &a, int nv, int nfv, int ndims, int rans,
                   int block, cudaStream_t s) {
     if (block <= 0) block = kBlock;
 #define UCFD_SW(NV, NFV, ND)                                                   \
     if (nv == NV && nfv == NFV && ndims == ND) {                               \
-        if (rans) {                                                            \
+        if (rans == 2) {                                                       \
+            if constexpr (NV > NFV) return sweep_both_go<T, NV, NFV, ND>(a, block, s); \
+        } else if (rans) {                                                     \
             if constexpr (NV > NFV) return sweep_go<T, NV, NFV, ND, true>(a, block, s); \
         } else {                                                               \
             return sweep_go<T, NV, NFV, ND, false>(a, block, s);               \
@@ -107,10 +126,10 @@ void scalar_sweep(const ::ucfd::ScalarSweepArgs<T> &a, int nv, int nfv, int ndim
                  nv, nfv, ndims, rans ? "RANS" : "NS");
 }
 
-template <typename T, int NV, int NFV, int NDIMS, bool RANS, int MINB>
+template <typename T, int NV, int NFV, int NDIMS, bool RANS, int MINB, bool BOTH = false>
 static void persistent_minb_go(const ::ucfd::ScalarSweepArgs<T> &a, const int *lev_off, int nlev, unsigned *bar,
                                int *err, long long max_spin, cudaStream_t s) {
-    auto kern = scalar_sweep_persistent_kernel<T, NV, NFV, NDIMS, RANS, MINB>;
+    auto kern = scalar_sweep_persistent_kernel<T, NV, NFV, NDIMS, RANS, MINB, BOTH>;
     static int grid = 0;  // per instantiation: blocks that fit co-resident
     if (!grid) {
         int per_sm = 0, dev = 0, sms = 0;
@@ -125,12 +144,15 @@ static void persistent_minb_go(const ::ucfd::ScalarSweepArgs<T> &a, const int *l
     UCFD_CUDA(cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(kBlock), args, 0, s));
 }
 
-template <typename T, int NV, int NFV, int NDIMS, bool RANS>
+template <typename T, int NV, int NFV, int NDIMS, bool RANS, bool BOTH = false>
 static void persistent_go(const ::ucfd::ScalarSweepArgs<T> &a, const int *lev_off, int nlev, unsigned *bar,
                           int *err, long long max_spin, cudaStream_t s) {
-    if (a.regcap == 4) persistent_minb_go<T, NV, NFV, NDIMS, RANS, 4>(a, lev_off, nlev, bar, err, max_spin, s);
-    else if (a.regcap == 3) persistent_minb_go<T, NV, NFV, NDIMS, RANS, 3>(a, lev_off, nlev, bar, err, max_spin, s);
-    else persistent_minb_go<T, NV, NFV, NDIMS, RANS, 1>(a, lev_off, nlev, bar, err, max_spin, s);
+    if (a.regcap == 4)
+        persistent_minb_go<T, NV, NFV, NDIMS, RANS, 4, BOTH>(a, lev_off, nlev, bar, err, max_spin, s);
+    else if (a.regcap == 3)
+        persistent_minb_go<T, NV, NFV, NDIMS, RANS, 3, BOTH>(a, lev_off, nlev, bar, err, max_spin, s);
+    else
+        persistent_minb_go<T, NV, NFV, NDIMS, RANS, 2, BOTH>(a, lev_off, nlev, bar, err, max_spin, s);
 }
 
 // Whole sweep (all nlev levels) as one cooperative launch with a bounded
@@ -141,7 +163,10 @@ void scalar_sweep_persistent(const ::ucfd::ScalarSweepArgs<T> &a, int nv, int nf
                              cudaStream_t s) {
 #define UCFD_PSW(NV, NFV, ND)                                                                              \
     if (nv == NV && nfv == NFV && ndims == ND) {                                                           \
-        if (rans) {                                                                                        \
+        if (rans == 2) {                                                                                   \
+            if constexpr (NV > NFV) return persistent_go<T, NV, NFV, ND, true, true>(a, lev_off, nlev, bar, \
+                                                                                      err, max_spin, s);   \
+        } else if (rans) {                                                                                 \
             if constexpr (NV > NFV) return persistent_go<T, NV, NFV, ND, true>(a, lev_off, nlev, bar, err, \
                                                                                 max_spin, s);              \
         } else {                                                                                           \
@@ -195,6 +220,14 @@ void fs_lusgs_prepare(long long N, int maxdeg, int nv0, int nv1, T kappa, const 
     if (N <= 0) return;
     fs_lusgs_prepare_kernel<T><<<grid_for(N), kBlock, 0, s>>>(N, maxdeg, nv0, nv1, kappa, nei, fa, rv, lam,
                                                               base, diag);
+}
+
+template <typename T>
+void fs_lusgs_prepare_both(long long N, int maxdeg, int nfv, int nv, T kappa, const int *nei, const T *fa,
+                           const T *rv, const T *lam, const T *tlam, const T *base, T *diag, cudaStream_t s) {
+    if (N <= 0) return;
+    fs_lusgs_prepare_both_kernel<T><<<grid_for(N), kBlock, 0, s>>>(N, maxdeg, nfv, nv, kappa, nei, fa, rv, lam,
+                                                                   tlam, base, diag);
 }
 
 template <typename Td>
@@ -639,43 +672,85 @@ void axpy_norm(long long n, const S *x, S *y, double *part, double *out, cudaStr
     sqrt_sum_kernel<<<1, 1024, 0, s>>>(nb, part, out);
 }
 
-// The FP32 pseudo-time update with an FP64 master state: y64 += x,
-// y = (float)y64, out = ||x||_2 accumulated in FP64.  An increment far
-// below the state's FP32 rounding unit is kept in y64 instead of being
-// rounded away at every iteration.
-__global__ void axpy_master_kernel(long long n, const float *x, double *y64, float *y, double *part) {
-    double t = 0.0;
+// The FP32 pseudo-time loop's state u += x, kept as a float-float pair: the
+// working FP32 state hi (what the sweeps read) and a low part lo, together
+// 48 significant bits, so an increment far below hi's rounding unit is kept
+// in lo instead of being rounded away at every iteration.  The pair is
+// updated by an error-free sum (Knuth's TwoSum of hi and x, the error added
+// to lo) and renormalised (Dekker's Fast2Sum), all on the FP32 pipe: an FP64
+// master would put four FP64 operations per value on GB300's narrow FP64
+// pipe.  out = ||x||_2: each thread sums x^2 exactly split (x*x rounded plus
+// its fma remainder) into a float-float accumulator, the thread sums are
+// added in FP64.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    const float bp = s - a;
+    e = (a - (s - bp)) + (b - bp);
+}
+
+__global__ void axpy_master_kernel(long long n, const float *x, float *hi, float *lo, double *part) {
+    float ah = 0.f, al = 0.f;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const double xv = (double)x[i];
-        const double v = y64[i] + xv;
-        y64[i] = v;
-        y[i] = (float)v;
-        t += xv * xv;
+        const float xv = x[i];
+        float sh, se;
+        two_sum(hi[i], xv, sh, se);
+        const float t = lo[i] + se;
+        const float nh = sh + t;
+        hi[i] = nh;
+        lo[i] = t - (nh - sh);
+        const float p = __fmul_rn(xv, xv);
+        const float pe = fmaf(xv, xv, -p);
+        float qh, qe;
+        two_sum(ah, p, qh, qe);
+        const float ql = al + (qe + pe);
+        ah = qh + ql;
+        al = ql - (ah - qh);
     }
+    double t = (double)ah + (double)al;
     t = block_sum(t);
     if (threadIdx.x == 0) part[blockIdx.x] = t;
 }
 
-void axpy_master(long long n, const float *x, double *y64, float *y, double *part, double *out, cudaStream_t s) {
+void axpy_master(long long n, const float *x, float *hi, float *lo, double *part, double *out, cudaStream_t s) {
     const int nb = gm_blocks(n);
-    axpy_master_kernel<<<nb, kBlock, 0, s>>>(n, x, y64, y, part);
+    axpy_master_kernel<<<nb, kBlock, 0, s>>>(n, x, hi, lo, part);
     sqrt_sum_kernel<<<1, 1024, 0, s>>>(nb, part, out);
 }
 
-// The FP64 master copy of the packed state (lusgs_pack's state, lusgs.c:8-37,
-// without rounding): u64[k + v N] = upts[idx + v neles], k = iperm[cell_ids[idx]].
-__global__ void state64_pack_kernel(int neles, int nvars, long long N, const int *cell_ids, const int *iperm,
-                                    const double *upts, double *u64) {
+// Low part of the packed state (lusgs_pack's state, lusgs.c:8-37): with
+// hi = (float)upts as fs_lusgs_pack rounds it, lo = (float)(upts - hi).
+__global__ void state_lo_pack_kernel(int neles, int nvars, long long N, const int *cell_ids, const int *iperm,
+                                     const double *upts, float *lo) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= neles) return;
     const long long k = iperm[cell_ids[idx]];
-    for (int v = 0; v < nvars; ++v) u64[k + v * N] = upts[idx + (long long)v * neles];
+    for (int v = 0; v < nvars; ++v) {
+        const double x = upts[idx + (long long)v * neles];
+        lo[k + v * N] = (float)(x - (double)(float)x);
+    }
 }
 
-void state64_pack(int neles, int nvars, long long N, const int *cell_ids, const int *iperm, const double *upts,
-                  double *u64, cudaStream_t s) {
+void state_lo_pack(int neles, int nvars, long long N, const int *cell_ids, const int *iperm, const double *upts,
+                   float *lo, cudaStream_t s) {
     if (neles <= 0) return;
-    state64_pack_kernel<<<grid_for(neles), kBlock, 0, s>>>(neles, nvars, N, cell_ids, iperm, upts, u64);
+    state_lo_pack_kernel<<<grid_for(neles), kBlock, 0, s>>>(neles, nvars, N, cell_ids, iperm, upts, lo);
+}
+
+// rank_lusgs_update's write-back (lusgs.c:54-70) of the float-float state:
+// upts = hi + lo in FP64.
+__global__ void state_ff_update_kernel(int neles, int nvars, long long N, const int *cell_ids, const int *iperm,
+                                       const float *hi, const float *lo, double *upts) {
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= neles) return;
+    const long long k = iperm[cell_ids[idx]];
+    for (int v = 0; v < nvars; ++v)
+        upts[idx + (long long)v * neles] = (double)hi[k + v * N] + (double)lo[k + v * N];
+}
+
+void state_ff_update(int neles, int nvars, long long N, const int *cell_ids, const int *iperm, const float *hi,
+                     const float *lo, double *upts, cudaStream_t s) {
+    if (neles <= 0) return;
+    state_ff_update_kernel<<<grid_for(neles), kBlock, 0, s>>>(neles, nvars, N, cell_ids, iperm, hi, lo, upts);
 }
 
 __global__ void __launch_bounds__(256) norm_finalize_kernel(int nblocks, const double *part, double *out) {

@@ -1,5 +1,6 @@
 // runtime.cpp -- error reporting, device selection, pointer kinds, constants.
 #include <cstdarg>
+#include <atomic>
 #include <mutex>
 
 #include "ucfd_internal.h"
@@ -97,6 +98,21 @@ int sm_count() {
     return g_sm_count;
 }
 
+namespace {
+std::atomic<int> g_host_access{UCFD_HOST_STAGE};
+}
+
+const void *host_mapped(const void *ptr) {
+    if (!ptr || g_host_access.load(std::memory_order_relaxed) != UCFD_HOST_MAP) return nullptr;
+    cudaPointerAttributes attr;
+    cudaError_t e = cudaPointerGetAttributes(&attr, ptr);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return attr.type == cudaMemoryTypeHost ? attr.devicePointer : nullptr;
+}
+
 bool is_device_ptr(const void *ptr) {
     if (!ptr) return false;
     cudaPointerAttributes attr;
@@ -135,6 +151,16 @@ ucfd_status_t UCFDSetTransferTiming(int on) {
     ucfd::g_xfer_on = on != 0;
     UCFD_API_END
 }
+
+ucfd_status_t UCFDSetHostArrayAccess(int mode) {
+    UCFD_API_BEGIN
+    UCFD_REQUIRE(mode == UCFD_HOST_STAGE || mode == UCFD_HOST_MAP,
+                 "host array access must be UCFD_HOST_STAGE (0) or UCFD_HOST_MAP (1), got %d", mode);
+    ucfd::g_host_access.store(mode, std::memory_order_relaxed);
+    UCFD_API_END
+}
+
+int UCFDGetHostArrayAccess(void) { return ucfd::g_host_access.load(std::memory_order_relaxed); }
 
 ucfd_status_t UCFDGetTransferStats(UCFDTransferStats *stats) {
     UCFD_API_BEGIN

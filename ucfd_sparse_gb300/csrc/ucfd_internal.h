@@ -122,6 +122,11 @@ struct PinnedBuf {
 };
 
 // ---- pointer kinds ----------------------------------------------------------
+// Under UCFD_HOST_MAP (UCFDSetHostArrayAccess): the device address of
+// page-locked host memory (pinned or registered), which kernels can read in
+// place over the host link; otherwise nullptr (stage the array instead).
+const void *host_mapped(const void *ptr);
+
 // True when the GPU can dereference ptr directly (device or managed memory).
 bool is_device_ptr(const void *ptr);
 

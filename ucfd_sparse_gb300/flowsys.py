@@ -121,6 +121,16 @@ class FlowSys:
     def lusgs_rans_upper(self, kappa=1.0):
         call("UCFDLUSGS_RANSUpperSweep", self._h, kappa)
 
+    # both systems per call: the values of the NS call followed by the RANS call
+    def lusgs_nsrans_prepare(self, kappa=1.0):
+        call("UCFDLUSGS_NSRANSPrepare", self._h, kappa)
+
+    def lusgs_nsrans_lower(self, kappa=1.0):
+        call("UCFDLUSGS_NSRANSLowerSweep", self._h, kappa)
+
+    def lusgs_nsrans_upper(self, kappa=1.0):
+        call("UCFDLUSGS_NSRANSUpperSweep", self._h, kappa)
+
     def lusgs_run(self, niter, kappa=1.0, rans=False, mode=0, resid=None):
         call("UCFDLUSGS_Run", self._h, niter, kappa, 1 if rans else 0, mode, ptr(resid))
 

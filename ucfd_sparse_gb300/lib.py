@@ -42,6 +42,19 @@ def transfer_stats() -> dict:
     return st.as_dict()
 
 
+HOST_STAGE, HOST_MAP = 0, 1
+
+
+def set_host_array_access(mode: int) -> None:
+    """UCFD_HOST_STAGE (0): host arrays are copied to the GPU; UCFD_HOST_MAP
+    (1): page-locked host face Jacobians are read in place by the kernels."""
+    call("UCFDSetHostArrayAccess", int(mode))
+
+
+def host_array_access() -> int:
+    return int(load().UCFDGetHostArrayAccess())
+
+
 class LaunchConfig(ctypes.Structure):
     """``UCFDLaunchConfig`` of ucfdlusgs.h."""
 
@@ -62,6 +75,8 @@ SIGNATURES = {
     "UCFDSelfTestTimeouts": (_I, [POINTER(c_int), POINTER(c_int)]),
     "UCFDSetTransferTiming": (_I, [_I]),
     "UCFDGetTransferStats": (_I, [_P]),
+    "UCFDSetHostArrayAccess": (_I, [_I]),
+    "UCFDGetHostArrayAccess": (_I, []),
     # ucfdmesh.h
     "UCFDMakeNeiEle": (_I, [_I, _I, _I, _P]),
     "UCFDMakeColoring": (_I, [_I, _I, _I, _P]),
@@ -81,6 +96,9 @@ SIGNATURES = {
     "UCFDLUSGS_NSUpperSweep": (_I, [_P, _D]),
     "UCFDLUSGS_RANSLowerSweep": (_I, [_P, _D]),
     "UCFDLUSGS_RANSUpperSweep": (_I, [_P, _D]),
+    "UCFDLUSGS_NSRANSPrepare": (_I, [_P, _D]),
+    "UCFDLUSGS_NSRANSLowerSweep": (_I, [_P, _D]),
+    "UCFDLUSGS_NSRANSUpperSweep": (_I, [_P, _D]),
     "UCFDFlowSysSetBLUSGS": (_I, [POINTER(c_void_p), _P, _P]),
     "UCFDBLUSGS_Pack": (_I, [_P, _I, _D]),
     "UCFDBLUSGS_KWSST_Pack": (_I, [_P, _I, _D, _D]),
