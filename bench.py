@@ -34,8 +34,9 @@ sys.path.insert(0, ROOT)
 METRIC = "LU-SGS cell-updates/s & HBM GB/s @2.1M cells; FP32+refine vs FP64 @1e-10"
 UNIT = "cell-updates/s"
 # DRAM bytes per cell update of the unrolled FP32 block sweep measured by
-# ncu on the 96^3 mesh (profiles/fs_blusgs_sweep_96cubed.md)
-SWEEP_TRAFFIC_PER_CELL = 711.0
+# ncu on the 96^3 mesh (profiles/fs_blusgs_sweep_96cubed.md); None until
+# measured for the current kernel
+SWEEP_TRAFFIC_PER_CELL = None
 
 
 # ---------------------------------------------------------------------------
@@ -156,14 +157,16 @@ def make_case(m: int, seed: int = 0):
 
 
 def sweep_bytes(rowptr: np.ndarray, elt: int, B: int = 5) -> int:
-    """Algorithmic bytes of one lower (or upper) BLU-SGS sweep over all
-    cells as the FP32 / FMA-mode kernels run it: per cell-face its neighbour
-    index (4) and block (B*B*elt: M = D^-1 J fv, formed at Prepare); per
-    cell its right-hand side (D^-1 rhs) and du read (as the neighbours'
-    data, once) and written."""
+    """Algorithmic bytes of one BLU-SGS sweep over all cells (the mean of a
+    lower and an upper sweep) as the FP32 / FMA-mode kernels run it: per
+    cell-face its neighbour index (4) in every sweep and its block (B*B*elt:
+    M = D^-1 J fv, formed at Prepare) in the one sweep of the pair that
+    updates that neighbour's side; per cell its right-hand side (D^-1 rhs),
+    du read (as the neighbours' data, once) and written, and the stored
+    other side's sums read and its own written."""
     nnz = int(rowptr[-1])
     N = rowptr.shape[0] - 1
-    return nnz * (4 + B * B * elt) + N * (3 * B * elt)
+    return nnz * 4 + (nnz * B * B * elt) // 2 + N * (5 * B * elt)
 
 
 class Problem:
@@ -530,7 +533,8 @@ def run_gpu(args):
              4: "fs_blusgs_sweep_kernel<float,5,6,true>"}.get(cfg32["sweep_variant"], "fs_blusgs_sweep_kernel")
     # DRAM bytes per cell update from ncu (dram__bytes_read.sum + write) of
     # the unrolled FP32 sweep on the 64^3 case, scaled to this launch's cells
-    traffic = SWEEP_TRAFFIC_PER_CELL * N / nlev if cfg32["sweep_variant"] in (0, 4) else None
+    traffic = (SWEEP_TRAFFIC_PER_CELL * N / nlev if SWEEP_TRAFFIC_PER_CELL and cfg32["sweep_variant"] in (0, 4)
+               else None)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "kernel": kname, "threads_per_block": cfg32["threads_per_block"],
                 "algorithmic_bytes_per_launch": launch_bytes, "launch_ms": sweep_ms / nlev,
@@ -605,21 +609,27 @@ def run_gpu(args):
                                     for k, v in xfer_copies.items()},
                 "how": "CUDA events around every host<->device copy the library makes, the same steps repeated; "
                        "then the steps once more without timing"}
-    # the same steps with the face Jacobians read in place from pinned host
-    # memory by the Prepare kernels (UCFD_HOST_MAP) instead of staged copies
+    # staged copies of the face Jacobians (UCFD_HOST_STAGE) against reading
+    # them in place from pinned host memory in the Prepare kernels
+    # (UCFD_HOST_MAP): steps alternate between the two, so both see the same
+    # phases of the host link
     host_access0 = _lib.host_array_access()
-    _lib.set_host_array_access(1 - host_access0)
-    Ph.step(args.rtol, args.max_pairs, args.inner)
-    torch.cuda.synchronize()
-    map_calls = {}
-    t3 = time.perf_counter()
-    map_pe = [Ph.step(args.rtol, args.max_pairs, args.inner, map_calls)[0] for _ in range(args.steps)]
-    torch.cuda.synchronize()
-    other_s = (time.perf_counter() - t3) / args.steps
+    per_mode = {0: [], 1: []}
+    calls_mode = {0: {}, 1: {}}
+    for _ in range(args.steps):
+        for mode in (0, 1):
+            _lib.set_host_array_access(mode)
+            torch.cuda.synchronize()
+            t3 = time.perf_counter()
+            Ph.step(args.rtol, args.max_pairs, args.inner, calls_mode[mode])
+            torch.cuda.synchronize()
+            per_mode[mode].append(time.perf_counter() - t3)
     _lib.set_host_array_access(host_access0)
-    other_access = {"mode": ("UCFD_HOST_MAP" if host_access0 == 0 else "UCFD_HOST_STAGE"),
-                    "ms_per_step": other_s * 1e3, "value": N * statistics.mean(map_pe) / other_s,
-                    "ms_per_call": {k: v * 1e3 / K for k, v in map_calls.items()}}
+    other_access = {("UCFD_HOST_MAP" if m else "UCFD_HOST_STAGE"):
+                    {"median_ms_per_step": statistics.median(v) * 1e3, "ms_per_step": [x * 1e3 for x in v],
+                     "ms_per_call": {k: x * 1e3 / K for k, x in calls_mode[m].items()}}
+                    for m, v in per_mode.items()}
+    other_access["how"] = "steps alternating between the two modes, each timed alone (wall clock, synchronised)"
     # the same pinned jmat copied alone (torch copy, one transfer): the host link's rate for it
     jdev = torch.empty(Ph.e["jmat"].shape, dtype=Ph.e["jmat"].dtype, device=device)
     torch.cuda.synchronize()
@@ -653,7 +663,7 @@ def run_gpu(args):
                     "ms_per_call": {k: v * 1e3 / args.steps for k, v in calls.items()},
                     "jmat_copy_GBps": jmat_gbps, "copies_timed": xfer_out,
                     "host_array_access": "UCFD_HOST_MAP" if host_access0 == 1 else "UCFD_HOST_STAGE",
-                    "other_host_array_access": other_access},
+                    "host_array_access_compared": other_access},
             "gpu_launches": launches_per_step(nlev, int(round(pairs_mean)), args.inner, True) * args.steps,
             "clocks": clocks,
             "launch": tuned or "defaults (--no-autotune)",

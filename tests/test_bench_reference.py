@@ -25,12 +25,12 @@ def test_reference_arm_loads_no_product_library():
 
 def test_cpu_step_composition_and_sweep_bytes():
     """The CPU legs' step is Pack+Prepare+Reset + Update + 40 pairs of
-    (lower, upper + SubResidual); the FP32 sweep moves 684 B per interior hex
-    cell (6 faces x (4 + 100) + 60)."""
+    (lower, upper + SubResidual); the FP32 sweep moves 424 B per interior hex
+    cell (6 indices x 4, half the 6 blocks of 100 B, 5 vectors of 20 B)."""
     import numpy as np
     import bench
     assert bench.PAIRS_PER_STEP == 40
     assert bench.compose_cpu_step(2.0, 0.5, 1.0, 1.5) == 2.0 + 0.5 + 40 * 2.5
     rowptr = np.arange(0, 6 * 11, 6)              # 10 cells of 6 faces each
-    assert bench.sweep_bytes(rowptr, 4, 5) == 10 * 684
-    assert bench.sweep_bytes(rowptr, 8, 5) == 10 * 1344
+    assert bench.sweep_bytes(rowptr, 4, 5) == 10 * 424
+    assert bench.sweep_bytes(rowptr, 8, 5) == 10 * 824

@@ -40,6 +40,17 @@ struct Work {
     DevBuf<S> fl_geo[2];                   // face lists (lower, upper): normal + fa * rv per entry
     DevBuf<S> ulo;                         // FP32 mode: low part of the float-float state u + ulo (UCFDLUSGS_Run)
     DevBuf<S> crhs;                        // fast modes: D^-1 rhs, the block sweeps' right-hand side
+    DevBuf<S> spart;                       // fast modes: each block sweep's own-side sums (SweepSplit)
+};
+
+// Which increments the fast block sweeps' stored sums (Work::spart) belong
+// to: the sweeps into du in direction dir (0 lower, 1 upper) with the
+// blocks of Prepare number ver.  The next sweep in the other direction
+// into the same du reads them instead of forming that side again.
+struct SplitState {
+    const void *du = nullptr;
+    int dir = -1;
+    unsigned ver = 0;
 };
 
 }  // namespace
@@ -81,6 +92,9 @@ struct _FlowSys {
     bool du64_valid = false;
     bool c_valid[2] = {false, false};  // crhs of the NS / turbulence rows matches rhs and the factors
     bool x_zero = false;  // the correction du is all zeros (Reset, no sweep since)
+    SplitState split[2];           // NS / turbulence rows of the fast block sweeps
+    unsigned jver[2] = {1, 1};     // Prepare count of the NS / turbulence blocks
+    bool has_self = false;         // some CSR row lists itself
     DevBuf<double> part, red, resid;
     PinnedBuf<double> h_red;
 
@@ -132,9 +146,27 @@ void build_topology(FlowSys s) {
 
     s->sch = s->colored ? schedule_colored(n, rp.data(), ci.data(), s->color.data())
                         : schedule_natural(n, rp.data(), ci.data());
+    s->has_self = false;
+    for (int i = 0; i < n && !s->has_self; ++i)
+        for (int q = rp[i]; q < rp[i + 1]; ++q) s->has_self = s->has_self || ci[q] == i;
     // spatial locality inside each level (the cells of a level are
     // independent, so the order does not change any result)
-    sort_levels_by(s->sch, bfs_rank(n, rp.data(), ci.data()));
+    const std::vector<int> bfs = bfs_rank(n, rp.data(), ci.data());
+    if (s->mode == MODE_BLUSGS) {
+        // block LU-SGS: inside each level the cells with the same set of
+        // faces towards earlier levels first come together (then breadth-
+        // first), so the fast sweeps that skip the other side's faces skip
+        // whole sectors of the block arrays
+        std::vector<int> lev(n), mask(n, 0);
+        for (int l = 0; l < s->sch.nlev; ++l)
+            for (int k = s->sch.lev_off[l]; k < s->sch.lev_off[l + 1]; ++k) lev[s->sch.perm[k]] = l;
+        for (int i = 0; i < n; ++i)
+            for (int q = rp[i]; q < rp[i + 1] && q - rp[i] < 30; ++q)
+                if (lev[ci[q]] < lev[i]) mask[i] |= 1 << (q - rp[i]);
+        sort_levels_by(s->sch, mask, bfs);
+    } else {
+        sort_levels_by(s->sch, bfs);
+    }
     const Schedule &sch = s->sch;
     int P = 0;
     for (int i = 0; i < n; ++i) P = std::max(P, rp[i + 1] - rp[i]);
@@ -440,13 +472,40 @@ void blusgs_sweep_into(FlowSys s, bool turb, bool upper, const S *rhs, S *du) {
     const int B = turb ? s->ntvars : s->nfvars;
     const int var0 = turb ? s->nfvars : 0;
     const int L = s->sch.nlev;
+    SweepSplit<S> sp;
+    if constexpr (!EX) {
+        // the fast build's split sums: partial when the stored sums are the
+        // previous opposite sweep's into the same du with the same blocks
+        SplitState &ss = s->split[turb ? 1 : 0];
+        sp.part = w.spart.ensure((size_t)s->nvars * s->N);
+        sp.upper = upper ? 1 : 0;
+        // (a face to the cell itself changes with the cell's own increment:
+        // such meshes always sweep in full mode)
+        sp.full = (!s->has_self && ss.du == du && ss.dir == (upper ? 0 : 1) && ss.ver == s->jver[turb ? 1 : 0])
+                      ? 0 : 1;
+    }
     for (int q = 0; q < L; ++q) {
         const int l = upper ? L - 1 - q : q;
         KCALL(EX, fs_blusgs_sweep<S>, B, s->sch.lev_off[l], s->sch.lev_off[l + 1], s->N, s->P, var0,
               s->d_nei.p, geo_fa<S>(s), geo_rv<S>(s), turb ? w.tJ.p : w.J.p, blu_LU<S>(s, turb), rhs, du,
-              s->block, s->variant, s->d_sweep_err.p, kBulkMaxSpin, s->stream());
+              s->block, s->variant, s->d_sweep_err.p, kBulkMaxSpin, sp, s->stream());
     }
+    if constexpr (!EX) s->split[turb ? 1 : 0] = SplitState{du, upper ? 1 : 0, s->jver[turb ? 1 : 0]};
 }
+
+// du of the fast block sweeps was set to zero: both sides' sums are zero,
+// so the next lower sweep can start from stored (zero) sums.
+template <typename S>
+void split_zero(FlowSys s, bool turb, const S *du, cudaStream_t st) {
+    Work<S> &w = work<S>(s);
+    const int B = turb ? s->ntvars : s->nfvars;
+    const int var0 = turb ? s->nfvars : 0;
+    w.spart.ensure((size_t)s->nvars * s->N);
+    UCFD_CUDA(cudaMemsetAsync(w.spart.p + (size_t)var0 * s->N, 0, (size_t)B * s->N * sizeof(S), st));
+    s->split[turb ? 1 : 0] = SplitState{du, 1, s->jver[turb ? 1 : 0]};
+}
+
+void split_forget(FlowSys s) { s->split[0] = s->split[1] = SplitState{}; }
 
 // FP64 residual of the NS block system for x; returns ||r|| and ||rhs||.
 template <typename Sx, typename R, bool EX>
@@ -899,6 +958,7 @@ ucfd_status_t UCFDFlowSysAutotune(FlowSys s, int reps, UCFDLaunchConfig *best) {
         });
     }
     keep.done = true;
+    split_forget(s);  // the candidates swept into scratch buffers
     s->block = best_block;
     s->variant = best_var;
     s->run_mode = best_mode;
@@ -1195,6 +1255,7 @@ static ucfd_status_t blusgs_prepare_api(FlowSys s, bool turb) {
               s->fa64.p, s->rv64.p, jd, dd, D, LU64, LU_s, turb ? w.tJ.p : w.J.p, J64, jt, st);
     });
     s->c_valid[turb ? 1 : 0] = false;
+    ++s->jver[turb ? 1 : 0];  // new blocks: stored sweep sums are stale
     finish(s, !is_device_ptr(jm));
     UCFD_API_END
 }
@@ -1237,6 +1298,10 @@ ucfd_status_t UCFDBLUSGS_Reset(FlowSys s) {
         w.bdu.zero(n, st);
         w.dup.zero(n, st);
         if (std::is_same<S, float>::value) s->x64.zero(n, st);
+        if constexpr (!EX) {
+            split_zero<S>(s, false, w.bdu.p, st);
+            if (s->ntvars > 0) split_zero<S>(s, true, w.bdu.p, st);
+        }
     });
     s->du64_valid = false;
     s->x_zero = true;
@@ -1333,6 +1398,7 @@ ucfd_status_t UCFDBLUSGS_Solve(FlowSys s, UCFDReal rtol, UCFDInt max_sweeps, UCF
             // the sweeps' right-hand side D^-1 r (their blocks are D^-1 J fv)
             kfast::fs_blusgs_rhs_solve<float>(s->nfvars, s->N, 0, w.LU.p, w.r.p, w.r.p, st);
             w.delta.zero(n, st);
+            split_zero<float>(s, false, w.delta.p, st);
             const int m = std::min(inner_sweeps, max_sweeps - pairs);
             for (int q = 0; q < m; ++q) {
                 blusgs_sweep_into<float, false>(s, false, false, w.r.p, w.delta.p);
@@ -1346,6 +1412,7 @@ ucfd_status_t UCFDBLUSGS_Solve(FlowSys s, UCFDReal rtol, UCFDInt max_sweeps, UCF
         }
         kfast::convert<double, float>((long long)n, s->x64.p, w.bdu.p, st);
         s->du64_valid = true;
+        split_forget(s);  // du now holds the refined solution
     } else {
         Work<double> &w = s->w64;
         UCFD_REQUIRE(w.J.p, "Solve before NSPrepare");

@@ -146,6 +146,14 @@ void sort_levels_by(Schedule &s, const std::vector<int> &key) {
     for (int k = 0; k < (int)s.perm.size(); ++k) s.iperm[s.perm[k]] = k;
 }
 
+void sort_levels_by(Schedule &s, const std::vector<int> &major, const std::vector<int> &minor) {
+    for (int l = 0; l < s.nlev; ++l) {
+        auto b = s.perm.begin() + s.lev_off[l], e = s.perm.begin() + s.lev_off[l + 1];
+        std::sort(b, e, [&](int a, int c) { return major[a] != major[c] ? major[a] < major[c] : minor[a] < minor[c]; });
+    }
+    for (int k = 0; k < (int)s.perm.size(); ++k) s.iperm[s.perm[k]] = k;
+}
+
 std::vector<int> greedy_color_csr(int n, const int *rowptr, const int *colidx, int *ncolors) {
     std::vector<int> srp, sci;
     symmetrize(n, rowptr, colidx, srp, sci);

@@ -43,6 +43,8 @@ std::vector<int> bfs_rank(int n, const int *rowptr, const int *colidx);
 // Reorder the cells inside every level by key (does not change results:
 // the cells of a level are independent).
 void sort_levels_by(Schedule &s, const std::vector<int> &key);
+// The same with a major and a minor key.
+void sort_levels_by(Schedule &s, const std::vector<int> &major, const std::vector<int> &minor);
 
 // Symmetrised adjacency (CSR, no self entries, no duplicates).
 void symmetrize(int n, const int *rowptr, const int *colidx, std::vector<int> &srp,

@@ -70,6 +70,24 @@ struct ScalarSweepArgs {
     const T *fl_geo;       // [E][4] outward normal (zero-padded to 3 components) and fa * rv
 };
 
+// Block LU-SGS sweeps of the fast build (M = D^-1 J fv blocks): a cell's
+// face products are summed by the level of the neighbour -- S_lo over
+// earlier levels, S_up over later ones -- and du = c - S_lo - S_up.  A
+// lower sweep reaches a cell after every earlier level and before every
+// later one, an upper sweep the other way round, so the side a sweep does
+// not update is the sum the previous (opposite) sweep formed with the same
+// increments.  part keeps each sweep's own side for the next one; with
+// full == 0 a sweep reads the other side from part instead of loading
+// those faces again.  Either way the values are the same, bit for bit.
+// (A face to the cell itself goes with the other side's sum; a mesh with
+// such faces always sweeps in full mode.)
+template <typename S>
+struct SweepSplit {
+    S *part = nullptr;  // [nvars][N] sums of the sweep's own side (nullptr: exact build, no split)
+    int upper = 0;      // this sweep's direction
+    int full = 1;       // 1: form both sides; 0: the other side from part
+};
+
 // One colour of a transposed (adjoint) colored LU-SGS sweep.
 struct AdjArgs {
     int t0, t1;          // icolor slots of the colour

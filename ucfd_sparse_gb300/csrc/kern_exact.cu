@@ -27,7 +27,8 @@ template void fs_blusgs_prepare<double>(int, long long, int, long long, const in
                                         double *, double *, double *, double *, double *, cudaStream_t);
 template void fs_blusgs_sweep<double>(int, int, int, long long, int, int, const int *, const double *, const double *,
                                       const double *, const double *, const double *, double *, int, int,
-                                      int *, long long, cudaStream_t);
+                                      int *, long long,
+                                      const ::ucfd::SweepSplit<double> &, cudaStream_t);
 template void fs_blusgs_residual<double, double>(int, long long, int, int, int, const int *, const double *,
                                                  const double *, const double *, const double *, const double *,
                                                  const double *, double *, double *, int, int *, cudaStream_t);

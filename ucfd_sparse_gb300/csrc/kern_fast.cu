@@ -30,7 +30,7 @@ namespace kfast {
                                        cudaStream_t);                                                          \
     template void fs_blusgs_sweep<T>(int, int, int, long long, int, int, const int *, const T *, const T *,    \
                                      const T *, const T *, const T *, T *, int, int, int *, long long,         \
-                                     cudaStream_t);                                                            \
+                                     const ::ucfd::SweepSplit<T> &, cudaStream_t);                                                            \
     template void fs_blusgs_residual<T, T>(int, long long, int, int, int, const int *, const double *,         \
                                            const double *, const double *, const double *, const double *,     \
                                            const T *, T *, double *, int, int *, cudaStream_t);                \

@@ -327,6 +327,71 @@ __global__ void fs_blusgs_rhs_solve_kernel(long long N, int var0, const S *LU, c
 // neighbour contributes with its current value (lower levels already
 // updated, higher levels not yet), then the cell solves with its LU.
 //
+// ---- split sums of the fast build's sweeps (see SweepSplit in kargs.h) ----
+template <typename S>
+using SweepSplit = ::ucfd::SweepSplit<S>;
+
+// Side of a face whose neighbour is g, for a cell of the level [lo, hi) in
+// the level-major layout: 0 an earlier level, 1 a later level, 2 the cell
+// itself.
+__device__ __forceinline__ int split_side(int g, int lo, int hi) { return g < lo ? 0 : (g >= hi ? 1 : 2); }
+
+// Whether a sweep uses the face at all: its own side always, the other side
+// (and a face to the cell itself) in full mode only.  A mesh with faces to
+// the cell itself always sweeps in full mode (the host sees to it): such a
+// term changes with the cell's own increment, so it is never stored.
+template <typename S>
+__device__ __forceinline__ bool split_uses(const SweepSplit<S> &sp, int side) {
+    return side == sp.upper || sp.full != 0;
+}
+
+// One face's product M x (M(r, c) its block) added to the sum of its side:
+// ta the sweep's own side, to the other side (with the cell itself).  The
+// entries go in row by row, columns in order, one fused multiply-add each.
+template <typename S, int B, typename MF>
+__device__ __forceinline__ void split_add(const SweepSplit<S> &sp, int side, const S *x, MF m, S *ta, S *to) {
+    if (side == sp.upper) {
+#pragma unroll
+        for (int r = 0; r < B; ++r)
+#pragma unroll
+            for (int c = 0; c < B; ++c) ta[r] += m(r, c) * x[c];
+    } else {
+#pragma unroll
+        for (int r = 0; r < B; ++r)
+#pragma unroll
+            for (int c = 0; c < B; ++c) to[r] += m(r, c) * x[c];
+    }
+}
+
+// The other side's sum to start from: stored by the previous sweep in
+// partial mode (issued early, with the cell's other inputs), zero in full
+// mode.  In a dependent launch only after griddepcontrol.wait.
+template <typename S, int B>
+__device__ __forceinline__ void split_start(const SweepSplit<S> &sp, long long N, int var0, long long k, S *ta,
+                                            S *to) {
+#pragma unroll
+    for (int r = 0; r < B; ++r) {
+        ta[r] = S(0);
+        to[r] = sp.full ? S(0) : sp.part[(var0 + r) * N + k];
+    }
+}
+
+// b = c - S_lo - S_up in that order (S_lo the lower side's sum, S_up the
+// upper side's; faces to the cell itself are in the other side's sum); the
+// sweep's own side is written to part.
+template <typename S, int B>
+__device__ __forceinline__ void split_finish(const SweepSplit<S> &sp, long long N, int var0, long long k, S *b,
+                                             const S *ta, const S *to) {
+#pragma unroll
+    for (int r = 0; r < B; ++r) {
+        const S slo = sp.upper ? to[r] : ta[r];
+        const S sup = sp.upper ? ta[r] : to[r];
+        b[r] = (b[r] - slo) - sup;
+    }
+#pragma unroll
+    for (int r = 0; r < B; ++r) sp.part[(var0 + r) * N + k] = ta[r];
+}
+
 // PW > 0: the ELL width is the compile-time constant PW and the face loop
 // is fully unrolled: every neighbour index, then every neighbour increment
 // and block value, is requested before the first product, so one thread
@@ -348,11 +413,15 @@ __global__ void fs_blusgs_rhs_solve_kernel(long long N, int var0, const S *LU, c
 // DEP == false.  (An L2 bulk prefetch of each warp's J and LU tiles in
 // front of the wait measured slower at 2.1M cells: the early grids'
 // prefetches evict the running grid's data.)
+//
+// Fast build (kFold): the face products are split by side (split_add /
+// split_finish; SweepSplit in kargs.h).  In partial mode the faces of the
+// other side are neither loaded nor multiplied.
 template <typename S, int B, int PW, bool DEP = false>
 __global__ void __launch_bounds__(256) fs_blusgs_sweep_kernel(int t0, int t1, long long N, int P,
                                                               int var0, const int *nei, const S *fa,
                                                               const S *rv, const S *J, const S *LU,
-                                                              const S *rhs, S *du) {
+                                                              const S *rhs, S *du, SweepSplit<S> sp) {
     static_assert(!DEP || PW > 0, "the dependent-launch form is the unrolled one");
     if constexpr (DEP) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     // threads start at the tile boundary below t0, so every warp reads
@@ -364,14 +433,84 @@ __global__ void __launch_bounds__(256) fs_blusgs_sweep_kernel(int t0, int t1, lo
     S b[B];
 #pragma unroll
     for (int r = 0; r < B; ++r) b[r] = __ldcs(rhs + (var0 + r) * N + k);
-    const S rvk = kFold ? S(1) : rv[k];
+    if constexpr (kFold) {
+        S ta[B], to[B];
+        if constexpr (!DEP) split_start<S, B>(sp, N, var0, k, ta, to);
+        if constexpr (PW > 0) {
+            // the faces the sweep uses, as bits (own: those of its own side)
+            int nb[PW];
+            unsigned use = 0u, own = 0u;
+#pragma unroll
+            for (int p = 0; p < PW; ++p) {
+                nb[p] = __ldcs(nei + p * N + k);
+                const int sd = nb[p] >= 0 ? split_side(nb[p], t0, t1) : -1;
+                use |= (sd >= 0 && split_uses(sp, sd)) ? 1u << p : 0u;
+                own |= (sd == sp.upper) ? 1u << p : 0u;
+            }
+            if constexpr (DEP) {
+                asm volatile("griddepcontrol.wait;" ::: "memory");
+                split_start<S, B>(sp, N, var0, k, ta, to);
+            }
+            // KB used faces at a time, in face order: the step's neighbour
+            // increments are all requested before its products
+            constexpr int KB = sizeof(S) == 8 ? 2 : 3;
+#pragma unroll 1
+            while (use) {
+                int pk[KB];
+                bool on[KB];
+#pragma unroll
+                for (int q = 0; q < KB; ++q) {
+                    on[q] = use != 0u;
+                    pk[q] = on[q] ? __ffs(use) - 1 : 0;
+                    use &= on[q] ? use - 1u : use;
+                }
+                S x[KB][B];
+#pragma unroll
+                for (int q = 0; q < KB; ++q) {
+                    if (!on[q]) continue;
+                    int g = nb[0];
+#pragma unroll
+                    for (int p = 1; p < PW; ++p) g = pk[q] == p ? nb[p] : g;
+#pragma unroll
+                    for (int c = 0; c < B; ++c) x[q][c] = du[(var0 + c) * N + g];
+                }
+#pragma unroll
+                for (int q = 0; q < KB; ++q) {
+                    if (!on[q]) continue;
+                    const S *Jp = Jk + ((long long)pk[q] * B2 << 5);
+                    const int sd = (own >> pk[q]) & 1u ? sp.upper : 2;
+                    split_add<S, B>(sp, sd, x[q], [&](int r, int c) { return __ldcs(Jp + ((r * B + c) << 5)); }, ta,
+                                    to);
+                }
+            }
+        } else {
+            for (int p = 0; p < P; ++p) {
+                const int g = __ldcs(nei + p * N + k);
+                if (g < 0) break;
+                const int sd = split_side(g, t0, t1);
+                if (!split_uses(sp, sd)) continue;
+                S x[B];
+#pragma unroll
+                for (int c = 0; c < B; ++c) x[c] = du[(var0 + c) * N + g];
+                const S *Jp = Jk + ((long long)p * B2 << 5);
+                split_add<S, B>(sp, sd, x, [&](int r, int c) { return __ldcs(Jp + ((r * B + c) << 5)); }, ta, to);
+            }
+        }
+        split_finish<S, B>(sp, N, var0, k, b, ta, to);
+#pragma unroll
+        for (int r = 0; r < B; ++r) du[(var0 + r) * N + k] = b[r];
+        return;
+    }
+    // exact build: the reference's per-face products (blusgs.c:298-314),
+    // scaled by fv, then the LU solve of the diagonal block
+    const S rvk = rv[k];
     if constexpr (PW > 0) {
         int nb[PW];
         S fv[PW];
 #pragma unroll
         for (int p = 0; p < PW; ++p) {
             nb[p] = __ldcs(nei + p * N + k);
-            if constexpr (!kFold) fv[p] = __ldcs(fa + p * N + k) * rvk;
+            fv[p] = __ldcs(fa + p * N + k) * rvk;
         }
         if constexpr (DEP) asm volatile("griddepcontrol.wait;" ::: "memory");
         S x[PW][B];
@@ -390,16 +529,10 @@ __global__ void __launch_bounds__(256) fs_blusgs_sweep_kernel(int t0, int t1, lo
             if (nb[p] >= 0) {
 #pragma unroll
                 for (int r = 0; r < B; ++r) {
-                    if constexpr (kFold) {
-                        // straight into b: one fused multiply-add per block entry
+                    S val = S(0);
 #pragma unroll
-                        for (int c = 0; c < B; ++c) b[r] -= jv[r * B + c] * x[p][c];
-                    } else {
-                        S val = S(0);
-#pragma unroll
-                        for (int c = 0; c < B; ++c) val += jv[r * B + c] * x[p][c];
-                        b[r] -= val * fv[p];
-                    }
+                    for (int c = 0; c < B; ++c) val += jv[r * B + c] * x[p][c];
+                    b[r] -= val * fv[p];
                 }
             }
         }
@@ -407,32 +540,25 @@ __global__ void __launch_bounds__(256) fs_blusgs_sweep_kernel(int t0, int t1, lo
         for (int p = 0; p < P; ++p) {
             const int nb = __ldcs(nei + p * N + k);
             if (nb < 0) break;
-            const S fv = kFold ? S(1) : __ldcs(fa + p * N + k) * rvk;
+            const S fv = __ldcs(fa + p * N + k) * rvk;
             S x[B];
 #pragma unroll
             for (int c = 0; c < B; ++c) x[c] = du[(var0 + c) * N + nb];
             const S *Jp = Jk + ((long long)p * B2 << 5);
 #pragma unroll
             for (int r = 0; r < B; ++r) {
-                if constexpr (kFold) {
+                S val = S(0);
 #pragma unroll
-                    for (int c = 0; c < B; ++c) b[r] -= __ldcs(Jp + ((r * B + c) << 5)) * x[c];
-                } else {
-                    S val = S(0);
-#pragma unroll
-                    for (int c = 0; c < B; ++c) val += __ldcs(Jp + ((r * B + c) << 5)) * x[c];
-                    b[r] -= val * fv;
-                }
+                for (int c = 0; c < B; ++c) val += __ldcs(Jp + ((r * B + c) << 5)) * x[c];
+                b[r] -= val * fv;
             }
         }
     }
-    if constexpr (!kFold) {
-        S lu[B2];
-        const S *LUk = LU + ::ucfd::tile_index(k, 0, B2);
+    S lu[B2];
+    const S *LUk = LU + ::ucfd::tile_index(k, 0, B2);
 #pragma unroll
-        for (int e = 0; e < B2; ++e) lu[e] = __ldcs(LUk + (e << 5));
-        lusub_dev<S, B>(lu, b);
-    }
+    for (int e = 0; e < B2; ++e) lu[e] = __ldcs(LUk + (e << 5));
+    lusub_dev<S, B>(lu, b);
 #pragma unroll
     for (int r = 0; r < B; ++r) du[(var0 + r) * N + k] = b[r];
 }
@@ -440,64 +566,52 @@ __global__ void __launch_bounds__(256) fs_blusgs_sweep_kernel(int t0, int t1, lo
 // FP32 sweep of a small level (a colour of a few thousand cells), where a
 // launch costs one thread's chain of dependent memory round trips rather
 // than bandwidth.  Launched like the DEP form of fs_blusgs_sweep_kernel,
-// but every input the previous launch does not write -- rhs, rv, nei, fa,
-// all PW J blocks and the LU block -- is loaded into registers before
+// but every input the previous launch does not write -- rhs, nei and the
+// blocks of the faces the sweep uses -- is loaded into registers before
 // griddepcontrol.wait, so after the wait only the neighbour increments
-// are fetched.  Same products and subtractions in the same order.
+// (and, in partial mode, the other side's sums) are fetched.  The fast
+// build's split sums, formed as fs_blusgs_sweep_kernel forms them.
 template <int B, int PW>
 __global__ void __launch_bounds__(128) fs_blusgs_sweep_small_kernel(int t0, int t1, long long N, int var0,
-                                                                    const int *nei, const float *fa,
-                                                                    const float *rv, const float *J,
-                                                                    const float *LU, const float *rhs,
-                                                                    float *du) {
+                                                                    const int *nei, const float *J,
+                                                                    const float *rhs, float *du,
+                                                                    SweepSplit<float> sp) {
+    static_assert(kFold || B < 0, "the small-level kernel is the fast build's");
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     const int k = (t0 & ~31) + blockIdx.x * blockDim.x + threadIdx.x;
     if (k < t0 || k >= t1) return;
     constexpr int B2 = B * B;
     const float *Jk = J + ::ucfd::tile_index(k, 0, (long long)PW * B2);
-    const float *LUk = LU + ::ucfd::tile_index(k, 0, B2);
-    float b[B], fv[PW], jv[PW][B2], lu[B2];
-    int nb[PW];
+    float b[B], jv[PW][B2];
+    int nb[PW], side[PW];
 #pragma unroll
     for (int r = 0; r < B; ++r) b[r] = __ldcs(rhs + (var0 + r) * N + k);
-    const float rvk = kFold ? 1.f : rv[k];
 #pragma unroll
     for (int p = 0; p < PW; ++p) {
         nb[p] = __ldcs(nei + p * N + k);
-        if constexpr (!kFold) fv[p] = __ldcs(fa + p * N + k) * rvk;
+        side[p] = nb[p] >= 0 ? split_side(nb[p], t0, t1) : -1;
+        if (side[p] >= 0 && split_uses(sp, side[p])) {
 #pragma unroll
-        for (int e = 0; e < B2; ++e) jv[p][e] = __ldcs(Jk + ((p * B2 + e) << 5));
-    }
-    if constexpr (!kFold) {
-#pragma unroll
-        for (int e = 0; e < B2; ++e) lu[e] = __ldcs(LUk + (e << 5));
+            for (int e = 0; e < B2; ++e) jv[p][e] = __ldcs(Jk + ((p * B2 + e) << 5));
+        }
     }
     asm volatile("griddepcontrol.wait;" ::: "memory");
+    float ta[B], to[B];
+    split_start<float, B>(sp, N, var0, k, ta, to);
     float x[PW][B];
 #pragma unroll
     for (int p = 0; p < PW; ++p) {
-        const int g = nb[p] >= 0 ? nb[p] : k;
+        if (side[p] >= 0 && split_uses(sp, side[p])) {
 #pragma unroll
-        for (int c = 0; c < B; ++c) x[p][c] = du[(var0 + c) * N + g];
+            for (int c = 0; c < B; ++c) x[p][c] = du[(var0 + c) * N + nb[p]];
+        }
     }
 #pragma unroll
     for (int p = 0; p < PW; ++p) {
-        if (nb[p] >= 0) {
-#pragma unroll
-            for (int r = 0; r < B; ++r) {
-                if constexpr (kFold) {
-#pragma unroll
-                    for (int c = 0; c < B; ++c) b[r] -= jv[p][r * B + c] * x[p][c];
-                } else {
-                    float val = 0.f;
-#pragma unroll
-                    for (int c = 0; c < B; ++c) val += jv[p][r * B + c] * x[p][c];
-                    b[r] -= val * fv[p];
-                }
-            }
-        }
+        if (side[p] >= 0 && split_uses(sp, side[p]))
+            split_add<float, B>(sp, side[p], x[p], [&](int r, int c) { return jv[p][r * B + c]; }, ta, to);
     }
-    if constexpr (!kFold) lusub_dev<float, B>(lu, b);
+    split_finish<float, B>(sp, N, var0, k, b, ta, to);
 #pragma unroll
     for (int r = 0; r < B; ++r) du[(var0 + r) * N + k] = b[r];
 }
@@ -520,7 +634,8 @@ __global__ void __launch_bounds__(NST == 2 ? 128 : 256)
     fs_blusgs_sweep_bulk_kernel(int t0, int t1, long long N, int var0, const int *__restrict__ nei,
                                 const float *__restrict__ fa, const float *__restrict__ rv,
                                 const float *__restrict__ J, const float *__restrict__ LU,
-                                const float *__restrict__ rhs, float *du, int *err, long long max_spin) {
+                                const float *__restrict__ rhs, float *du, int *err, long long max_spin,
+                                SweepSplit<float> sp) {
     constexpr int B2 = B * B;
     constexpr int JT = PW * B2 * 32;  // floats of J in one tile
     constexpr int LT = kFold ? 0 : B2 * 32;  // floats of LU in one tile (the fast build's blocks need none)
@@ -564,19 +679,21 @@ __global__ void __launch_bounds__(NST == 2 ? 128 : 256)
 #pragma unroll
         for (int r = 0; r < B; ++r) b[r] = rhs[(var0 + r) * N + kk];
         const float rvk = kFold ? 1.f : rv[kk];
-        int nb[PW];
+        int nb[PW], side[PW];
         float fv[PW];
 #pragma unroll
         for (int p = 0; p < PW; ++p) {
             nb[p] = act ? __ldg(nei + p * N + kk) : -1;
+            side[p] = nb[p] >= 0 ? split_side(nb[p], t0, t1) : -1;
             if constexpr (!kFold) fv[p] = __ldg(fa + p * N + kk) * rvk;
         }
         float x[PW][B];
 #pragma unroll
         for (int p = 0; p < PW; ++p) {
-            const long long g = nb[p] >= 0 ? nb[p] : kk;
+            const bool use = kFold ? side[p] >= 0 && split_uses(sp, side[p]) : nb[p] >= 0;
+            const long long g = use ? nb[p] : kk;
 #pragma unroll
-            for (int c = 0; c < B; ++c) x[p][c] = nb[p] >= 0 ? du[(var0 + c) * N + g] : 0.f;
+            for (int c = 0; c < B; ++c) x[p][c] = use ? du[(var0 + c) * N + g] : 0.f;
         }
         const bool ok = __all_sync(0xffffffffu, ::ucfd::dev::mbar_wait_bounded(&bar[q], parity, max_spin));
         if (!ok) {
@@ -587,15 +704,22 @@ __global__ void __launch_bounds__(NST == 2 ? 128 : 256)
             return;
         }
         const float *sJ = buf + q * ST + lane;
+        if constexpr (kFold) {
+            float ta[B], to[B];
+            split_start<float, B>(sp, N, var0, kk, ta, to);
 #pragma unroll
-        for (int p = 0; p < PW; ++p) {
-            if (nb[p] >= 0) {
+            for (int p = 0; p < PW; ++p) {
+                if (side[p] >= 0 && split_uses(sp, side[p]))
+                    split_add<float, B>(sp, side[p], x[p], [&](int r, int c) { return sJ[(p * B2 + r * B + c) << 5]; },
+                                        ta, to);
+            }
+            if (act) split_finish<float, B>(sp, N, var0, k, b, ta, to);
+        } else {
 #pragma unroll
-                for (int r = 0; r < B; ++r) {
-                    if constexpr (kFold) {
+            for (int p = 0; p < PW; ++p) {
+                if (nb[p] >= 0) {
 #pragma unroll
-                        for (int c = 0; c < B; ++c) b[r] -= sJ[(p * B2 + r * B + c) << 5] * x[p][c];
-                    } else {
+                    for (int r = 0; r < B; ++r) {
                         float val = 0.f;
 #pragma unroll
                         for (int c = 0; c < B; ++c) val += sJ[(p * B2 + r * B + c) << 5] * x[p][c];
@@ -603,8 +727,6 @@ __global__ void __launch_bounds__(NST == 2 ? 128 : 256)
                     }
                 }
             }
-        }
-        if constexpr (!kFold) {
             float lu[B2];
 #pragma unroll
             for (int e = 0; e < B2; ++e) lu[e] = sJ[JT + (e << 5)];

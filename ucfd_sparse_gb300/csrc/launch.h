@@ -67,7 +67,8 @@
     template <typename S>                                                                          \
     void fs_blusgs_sweep(int B, int t0, int t1, long long N, int P, int var0, const int *nei,      \
                          const S *fa, const S *rv, const S *J, const S *LU, const S *rhs, S *du,   \
-                         int block, int variant, int *err, long long max_spin, cudaStream_t s);    \
+                         int block, int variant, int *err, long long max_spin,                     \
+                         const ::ucfd::SweepSplit<S> &sp, cudaStream_t s);                         \
     template <typename S>                                                                          \
     void fs_blusgs_rhs_solve(int B, long long N, int var0, const S *LU, const S *b, S *c,          \
                              cudaStream_t s);                                                      \

@@ -299,7 +299,7 @@ void fs_blusgs_prepare(int B, long long N, int P, long long nF, const int *nei, 
 template <int B, int PW, int NST>
 static void sweep_bulk_go(int t0, int t1, long long N, int var0, const int *nei, const float *fa,
                           const float *rv, const float *J, const float *LU, const float *rhs, float *du,
-                          int *err, long long max_spin, cudaStream_t s) {
+                          int *err, long long max_spin, const ::ucfd::SweepSplit<float> &sp, cudaStream_t s) {
     auto kern = fs_blusgs_sweep_bulk_kernel<B, PW, NST>;
     constexpr int threads = NST == 2 ? 128 : 256;
     constexpr int tiles_per_buf = kFold ? PW : PW + 1;  // J (and, in the exact build, LU) tiles
@@ -317,14 +317,15 @@ static void sweep_bulk_go(int t0, int t1, long long N, int var0, const int *nei,
     const long long tiles = (((long long)t1 + 31) >> 5) - (t0 >> 5);
     const long long want = (tiles + threads / 32 - 1) / (threads / 32);
     const unsigned g = (unsigned)(want < cap ? want : cap);
-    kern<<<g, threads, smem, s>>>(t0, t1, N, var0, nei, fa, rv, J, LU, rhs, du, err, max_spin);
+    kern<<<g, threads, smem, s>>>(t0, t1, N, var0, nei, fa, rv, J, LU, rhs, du, err, max_spin, sp);
 }
 
 // Unrolled sweep launched as a programmatic dependent of the previous
 // launch on the stream (cudaLaunchAttributeProgrammaticStreamSerialization).
 template <typename S, int B, int PW>
 static void sweep_dep_go(unsigned g, int block, cudaStream_t s, int t0, int t1, long long N, int P, int var0,
-                         const int *nei, const S *fa, const S *rv, const S *J, const S *LU, const S *rhs, S *du) {
+                         const int *nei, const S *fa, const S *rv, const S *J, const S *LU, const S *rhs, S *du,
+                         const ::ucfd::SweepSplit<S> &sp) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(g);
     cfg.blockDim = dim3(block);
@@ -336,7 +337,7 @@ static void sweep_dep_go(unsigned g, int block, cudaStream_t s, int t0, int t1, 
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     UCFD_CUDA(cudaLaunchKernelEx(&cfg, fs_blusgs_sweep_kernel<S, B, PW, true>, t0, t1, N, P, var0, nei, fa, rv, J,
-                                 LU, rhs, du));
+                                 LU, rhs, du, sp));
 }
 
 // Levels with at most this many cells take the register-hoisted kernel in
@@ -345,8 +346,8 @@ static void sweep_dep_go(unsigned g, int block, cudaStream_t s, int t0, int t1, 
 constexpr int kSmallLevel = 16384;
 
 template <int B, int PW>
-static void sweep_small_go(cudaStream_t s, int t0, int t1, long long N, int var0, const int *nei, const float *fa,
-                           const float *rv, const float *J, const float *LU, const float *rhs, float *du) {
+static void sweep_small_go(cudaStream_t s, int t0, int t1, long long N, int var0, const int *nei, const float *J,
+                           const float *rhs, float *du, const ::ucfd::SweepSplit<float> &sp) {
     constexpr int threads = 128;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid_for(t1 - (t0 & ~31), threads));
@@ -358,14 +359,14 @@ static void sweep_small_go(cudaStream_t s, int t0, int t1, long long N, int var0
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    UCFD_CUDA(cudaLaunchKernelEx(&cfg, fs_blusgs_sweep_small_kernel<B, PW>, t0, t1, N, var0, nei, fa, rv, J, LU,
-                                 rhs, du));
+    UCFD_CUDA(cudaLaunchKernelEx(&cfg, fs_blusgs_sweep_small_kernel<B, PW>, t0, t1, N, var0, nei, J, rhs, du, sp));
 }
 
 template <typename S>
 void fs_blusgs_sweep(int B, int t0, int t1, long long N, int P, int var0, const int *nei, const S *fa,
                      const S *rv, const S *J, const S *LU, const S *rhs, S *du, int block,
-                     int variant, int *err, long long max_spin, cudaStream_t s) {
+                     int variant, int *err, long long max_spin, const ::ucfd::SweepSplit<S> &sp,
+                     cudaStream_t s) {
     if (t1 <= t0) return;
     if (block <= 0) block = kBlock;
     // threads start at the tile boundary below t0 (see the kernel)
@@ -379,16 +380,16 @@ void fs_blusgs_sweep(int B, int t0, int t1, long long N, int P, int var0, const 
     // All apply the faces in the same order with the same operations.
     if (variant == 4 && (P == 6 || P == 4)) {
         if constexpr (std::is_same<S, float>::value) {
-            if (B == 5 && t1 - t0 <= kSmallLevel) {
-                if (P == 6) sweep_small_go<5, 6>(s, t0, t1, N, var0, nei, fa, rv, J, LU, rhs, du);
-                else sweep_small_go<5, 4>(s, t0, t1, N, var0, nei, fa, rv, J, LU, rhs, du);
+            if (kFold && B == 5 && t1 - t0 <= kSmallLevel) {
+                if (P == 6) sweep_small_go<5, 6>(s, t0, t1, N, var0, nei, J, rhs, du, sp);
+                else sweep_small_go<5, 4>(s, t0, t1, N, var0, nei, J, rhs, du, sp);
                 return;
             }
         }
         if (P == 6) {
-            UCFD_BSW(B, (sweep_dep_go<S, BB, 6>(g, block, s, t0, t1, N, P, var0, nei, fa, rv, J, LU, rhs, du)));
+            UCFD_BSW(B, (sweep_dep_go<S, BB, 6>(g, block, s, t0, t1, N, P, var0, nei, fa, rv, J, LU, rhs, du, sp)));
         } else {
-            UCFD_BSW(B, (sweep_dep_go<S, BB, 4>(g, block, s, t0, t1, N, P, var0, nei, fa, rv, J, LU, rhs, du)));
+            UCFD_BSW(B, (sweep_dep_go<S, BB, 4>(g, block, s, t0, t1, N, P, var0, nei, fa, rv, J, LU, rhs, du, sp)));
         }
         return;
     }
@@ -396,27 +397,27 @@ void fs_blusgs_sweep(int B, int t0, int t1, long long N, int P, int var0, const 
         if ((variant == 2 || variant == 3) && B == 5 && (P == 6 || P == 4)) {
             if (!err) ::ucfd::fail(UCFD_ERR_ARGUMENT, "bulk-copy sweep needs an error flag");
             if (P == 6) {
-                if (variant == 2) sweep_bulk_go<5, 6, 2>(t0, t1, N, var0, nei, fa, rv, J, LU, rhs, du, err, max_spin, s);
-                else sweep_bulk_go<5, 6, 1>(t0, t1, N, var0, nei, fa, rv, J, LU, rhs, du, err, max_spin, s);
+                if (variant == 2) sweep_bulk_go<5, 6, 2>(t0, t1, N, var0, nei, fa, rv, J, LU, rhs, du, err, max_spin, sp, s);
+                else sweep_bulk_go<5, 6, 1>(t0, t1, N, var0, nei, fa, rv, J, LU, rhs, du, err, max_spin, sp, s);
             } else {
-                if (variant == 2) sweep_bulk_go<5, 4, 2>(t0, t1, N, var0, nei, fa, rv, J, LU, rhs, du, err, max_spin, s);
-                else sweep_bulk_go<5, 4, 1>(t0, t1, N, var0, nei, fa, rv, J, LU, rhs, du, err, max_spin, s);
+                if (variant == 2) sweep_bulk_go<5, 4, 2>(t0, t1, N, var0, nei, fa, rv, J, LU, rhs, du, err, max_spin, sp, s);
+                else sweep_bulk_go<5, 4, 1>(t0, t1, N, var0, nei, fa, rv, J, LU, rhs, du, err, max_spin, sp, s);
             }
             return;
         }
     }
     if (variant == 1) {
         UCFD_BSW(B, (fs_blusgs_sweep_kernel<S, BB, 0><<<g, block, 0, s>>>(t0, t1, N, P, var0, nei, fa, rv, J, LU,
-                                                                          rhs, du)));
+                                                                          rhs, du, sp)));
     } else if (P == 6) {
         UCFD_BSW(B, (fs_blusgs_sweep_kernel<S, BB, 6><<<g, block, 0, s>>>(t0, t1, N, P, var0, nei, fa, rv, J, LU,
-                                                                          rhs, du)));
+                                                                          rhs, du, sp)));
     } else if (P == 4) {
         UCFD_BSW(B, (fs_blusgs_sweep_kernel<S, BB, 4><<<g, block, 0, s>>>(t0, t1, N, P, var0, nei, fa, rv, J, LU,
-                                                                          rhs, du)));
+                                                                          rhs, du, sp)));
     } else {
         UCFD_BSW(B, (fs_blusgs_sweep_kernel<S, BB, 0><<<g, block, 0, s>>>(t0, t1, N, P, var0, nei, fa, rv, J, LU,
-                                                                          rhs, du)));
+                                                                          rhs, du, sp)));
     }
 }
 
