@@ -33,10 +33,11 @@ sys.path.insert(0, ROOT)
 
 METRIC = "LU-SGS cell-updates/s & HBM GB/s @2.1M cells; FP32+refine vs FP64 @1e-10"
 UNIT = "cell-updates/s"
-# DRAM bytes per cell update of the unrolled FP32 block sweep measured by
-# ncu on the 96^3 mesh (profiles/fs_blusgs_sweep_96cubed.md); None until
-# measured for the current kernel
-SWEEP_TRAFFIC_PER_CELL = None
+# DRAM bytes per cell update of the unrolled FP32 block sweep: ncu
+# dram__bytes_read.sum + dram__bytes_write.sum over one lower + upper sweep
+# pair on the 96^3 mesh (718.1 MB for 2 x 884,736 cell updates;
+# profiles/fs_blusgs_sweep_96cubed.md)
+SWEEP_TRAFFIC_PER_CELL = 405.8
 
 
 # ---------------------------------------------------------------------------
@@ -538,7 +539,8 @@ def run_gpu(args):
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": traffic, "kernel": kname, "threads_per_block": cfg32["threads_per_block"],
                 "algorithmic_bytes_per_launch": launch_bytes, "launch_ms": sweep_ms / nlev,
-                "traffic_source": "ncu 96^3 capture, 711 B per cell update, scaled by cells per launch",
+                "traffic_source": f"ncu 96^3 capture of a sweep pair, {SWEEP_TRAFFIC_PER_CELL} B per cell update, "
+                                  "scaled by cells per launch",
                 "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s"}
 
     # ---- error of one step against the FP64 arithmetic of the oracle --------

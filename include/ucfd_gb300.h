@@ -89,13 +89,14 @@ UCFD_EXTERN ucfd_status_t UCFDGetTransferStats(UCFDTransferStats *stats);
 
 /* How host-memory array arguments reach the GPU (process-wide).
  * UCFD_HOST_STAGE: copied into library device buffers (cudaMemcpyAsync)
- * before the kernels that read them.  UCFD_HOST_MAP: an array in
- * page-locked host memory (cudaHostAlloc / cudaHostRegister / a pinned
- * torch tensor) is read in place by the kernel that consumes it, over the
- * host link, with no copy -- where the library supports it: the face
- * Jacobians of UCFDBLUSGS_NSPrepare / RANSPrepare.  Other arrays, and
- * pageable memory, are staged in either mode.  Results are identical.  No
- * counterpart in the reference (a CPU library). */
+ * before the kernels that read them.  UCFD_HOST_MAP (the default): an
+ * array in page-locked host memory (cudaHostAlloc / cudaHostRegister / a
+ * pinned torch tensor) is read in place by the kernel that consumes it,
+ * over the host link, with no copy and no device staging buffer -- where
+ * the library supports it: the face Jacobians of UCFDBLUSGS_NSPrepare /
+ * RANSPrepare.  Other arrays, and pageable memory, are staged in either
+ * mode.  Results are identical.  No counterpart in the reference (a CPU
+ * library). */
 typedef enum { UCFD_HOST_STAGE = 0, UCFD_HOST_MAP = 1 } ucfd_host_access_t;
 UCFD_EXTERN ucfd_status_t UCFDSetHostArrayAccess(int mode);
 UCFD_EXTERN int UCFDGetHostArrayAccess(void);

@@ -69,6 +69,8 @@ def test_blusgs_pinned_jacobians_read_in_place(name, prec, golden, ucfd):
     kw = cases.BLUSGS[name]
     b = cases.blusgs_case(**kw)
     outs = {}
+    mode0 = lib.host_array_access()
+    assert mode0 == lib.HOST_MAP  # the default
     for mode in (lib.HOST_STAGE, lib.HOST_MAP):
         S, e = make(b, prec=prec)
         jm = torch.from_numpy(np.ascontiguousarray(b["jmat"])).pin_memory()
@@ -78,7 +80,7 @@ def test_blusgs_pinned_jacobians_read_in_place(name, prec, golden, ucfd):
             assert lib.host_array_access() == mode
             run_sweeps(S, kw["nsweeps"])
         finally:
-            lib.set_host_array_access(lib.HOST_STAGE)
+            lib.set_host_array_access(mode0)
         outs[mode] = (np.array(e["upts"]), np.array(e["res"]))
         S.destroy()
     for a, r in zip(outs[lib.HOST_MAP], outs[lib.HOST_STAGE]):

@@ -99,7 +99,7 @@ int sm_count() {
 }
 
 namespace {
-std::atomic<int> g_host_access{UCFD_HOST_STAGE};
+std::atomic<int> g_host_access{UCFD_HOST_MAP};
 }
 
 const void *host_mapped(const void *ptr) {

@@ -47,7 +47,8 @@ HOST_STAGE, HOST_MAP = 0, 1
 
 def set_host_array_access(mode: int) -> None:
     """UCFD_HOST_STAGE (0): host arrays are copied to the GPU; UCFD_HOST_MAP
-    (1): page-locked host face Jacobians are read in place by the kernels."""
+    (1, the default): page-locked host face Jacobians are read in place by
+    the kernels."""
     call("UCFDSetHostArrayAccess", int(mode))
 
 
