@@ -323,10 +323,6 @@ __global__ void fs_blusgs_rhs_solve_kernel(long long N, int var0, const S *LU, c
     for (int r = 0; r < B; ++r) c[(var0 + r) * N + k] = v[r];
 }
 
-// lower_sweep / upper_sweep of blusgs.c:273-373 for one level: every
-// neighbour contributes with its current value (lower levels already
-// updated, higher levels not yet), then the cell solves with its LU.
-//
 // ---- split sums of the fast build's sweeps (see SweepSplit in kargs.h) ----
 template <typename S>
 using SweepSplit = ::ucfd::SweepSplit<S>;
@@ -392,6 +388,10 @@ __device__ __forceinline__ void split_finish(const SweepSplit<S> &sp, long long 
     for (int r = 0; r < B; ++r) sp.part[(var0 + r) * N + k] = ta[r];
 }
 
+// lower_sweep / upper_sweep of blusgs.c:273-373 for one level: every
+// neighbour contributes with its current value (lower levels already
+// updated, higher levels not yet), then the cell solves with its LU.
+//
 // PW > 0: the ELL width is the compile-time constant PW and the face loop
 // is fully unrolled: every neighbour index, then every neighbour increment
 // and block value, is requested before the first product, so one thread
