@@ -119,6 +119,99 @@ def test_blusgs_fp64_fma_within_tolerance(golden, ucfd):
     assert np.abs(d - r).max() <= 1e-12 * np.abs(r).max()
 
 
+SPLIT_ORDERS = {
+    "lower_twice": "LLUULU",
+    "upper_first": "ULUL",
+    "prepare_between": "LUPLUL",
+    "reset_between": "LURLU",
+}
+
+
+@pytest.mark.parametrize("order", sorted(SPLIT_ORDERS))
+def test_blusgs_fast_sweeps_any_call_order(order, ucfd):
+    """The fast build's sweeps reuse the face sums the opposite sweep stored
+    only when they belong to the same increments and the same blocks.  Any
+    order of lower (L) and upper (U) sweeps, Prepare (P) and Reset (R) gives
+    the exact mode's values: the FMA mode within 1e-12 and FP32 within 1e-5
+    of the largest change."""
+    b = cases.blusgs_case(m=8, seed=7)
+    outs = {}
+    for prec in (0, 1, 2):
+        S, e = make(b, prec=prec, on_device=True)
+        S.blusgs_pack(0, 0.0)
+        S.blusgs_ns_prepare()
+        S.blusgs_reset()
+        ops = {"L": S.blusgs_ns_lower, "U": S.blusgs_ns_upper, "P": S.blusgs_ns_prepare, "R": S.blusgs_reset}
+        for op in SPLIT_ORDERS[order]:
+            ops[op]()
+        S.blusgs_update(0)
+        outs[prec] = host(e["upts"]) - b["upts"]
+        S.destroy()
+    r = outs[0]
+    scale = np.abs(r).max()
+    assert scale > 0
+    assert np.abs(outs[1] - r).max() <= 1e-12 * scale
+    assert np.abs(outs[2] - r).max() <= 1e-5 * scale
+
+
+def with_self_faces(b, ncells, seed=0):
+    """The same system with a face from each of the first ncells boundary
+    cells to the cell itself (a CSR entry naming its own row, with a face of
+    its own), as legacy meshes list boundary faces."""
+    rng = np.random.default_rng(seed)
+    rp, ci, sl, sd = b["rowptr"], b["colidx"], b["slots"], b["sides"]
+    n, nF, nv = b["nlocal"], b["nfaces"], b["jmat"].shape[1]
+    rows = [i for i in range(n) if rp[i + 1] - rp[i] < 6][:ncells]
+    nrp, nci, nsl, nsd = [0], [], [], []
+    for i in range(n):
+        q0, q1 = rp[i], rp[i + 1]
+        nci += list(ci[q0:q1]); nsl += list(sl[q0:q1]); nsd += list(sd[q0:q1])
+        if i in rows:
+            nci.append(i); nsl.append(nF + rows.index(i)); nsd.append(1)
+        nrp.append(len(nci))
+    k = len(rows)
+    c = dict(b)
+    c["rowptr"] = np.array(nrp, dtype=np.int32)
+    c["colidx"] = np.array(nci, dtype=np.int32)
+    c["slots"] = np.array(nsl, dtype=np.int32)
+    c["sides"] = np.array(nsd, dtype=np.int8)
+    c["nfaces"] = nF + k
+    c["face_area"] = np.concatenate([b["face_area"], rng.uniform(0.5, 1.0, k)])
+    c["face_normal"] = np.concatenate([b["face_normal"], np.tile([[1.0], [0.0], [0.0]], (1, k))], axis=1)
+    extra = rng.normal(0.0, 0.05, (2, nv, nv, k))
+    for r in range(nv):
+        extra[0, r, r] += 1.0
+        extra[1, r, r] -= 1.0
+    c["jmat"] = np.ascontiguousarray(np.concatenate([b["jmat"], extra], axis=3))
+    return c
+
+
+def test_blusgs_faces_to_the_cell_itself(port, ucfd):
+    """A mesh with faces from a cell to itself: the exact mode matches the
+    oracle bit for bit; the fast build sweeps in full mode (such a face's
+    term changes with the cell's own increment) and stays within 1e-12 (FMA)
+    of it, in lower-upper pairs and in other call orders."""
+    b = with_self_faces(cases.blusgs_case(m=6, seed=2), ncells=12)
+    for order in ("LULULU", "LULUUL"):
+        outs = {}
+        for prec in (0, 1):
+            S, e = make(b, prec=prec, on_device=True)
+            S.blusgs_pack(0, 0.0)
+            S.blusgs_ns_prepare()
+            S.blusgs_reset()
+            for op in order:
+                (S.blusgs_ns_lower if op == "L" else S.blusgs_ns_upper)()
+            S.blusgs_update(0)
+            outs[prec] = host(e["upts"])
+            S.destroy()
+        if order == "LULULU":
+            ref = port.flowsys_blusgs(b, b["rhs"], b["dt"], b["jmat"], b["vol"], b["upts"], nsweeps=3)[0]
+            np.testing.assert_array_equal(outs[0], ref)
+        r = outs[0] - b["upts"]
+        assert np.abs(r).max() > 0
+        assert np.abs(outs[1] - outs[0]).max() <= 1e-12 * np.abs(r).max()
+
+
 @pytest.mark.parametrize("prec", [0, 2])
 def test_blusgs_solve_reaches_1e10(prec, port, ucfd):
     """Plain FP64 sweeps and FP32 sweeps + FP64 refinement both reach a

@@ -135,7 +135,8 @@ __device__ __forceinline__ void scalar_sweep_cell(const ScalarSweepArgs<T> &a, i
 // spectral radius lam, the turbulence variables with tlam): the two sweeps
 // are independent of each other, since each reads only the state u and its
 // own increments, so this gives every value the separate sweeps give.
-template <typename T, int NV, int NFV, int NDIMS, bool COHERENT = false>
+// FB: active faces gathered per step (fewer for the register-capped builds).
+template <typename T, int NV, int NFV, int NDIMS, bool COHERENT = false, int FB = 3>
 __device__ __forceinline__ void scalar_sweep_cell_both(const ScalarSweepArgs<T> &a, int t, int lo, int hi);
 
 // MINB: minimum resident blocks of 256 threads per SM the compiler must
@@ -202,7 +203,7 @@ __global__ void __launch_bounds__(256, MINB) scalar_sweep_persistent_kernel(Scal
         const int l = a.upper ? nlev - 1 - q : q;
         const int t0 = lev_off[l], t1 = lev_off[l + 1];
         for (int t = t0 + blockIdx.x * blockDim.x + threadIdx.x; t < t1; t += gridDim.x * blockDim.x) {
-            if constexpr (BOTH) scalar_sweep_cell_both<T, NV, NFV, NDIMS, true>(a, t, t0, t1);
+            if constexpr (BOTH) scalar_sweep_cell_both<T, NV, NFV, NDIMS, true, (MINB >= 3 ? 2 : 3)>(a, t, t0, t1);
             else scalar_sweep_cell<T, NV, NFV, NDIMS, RANS, true>(a, t, t0, t1);
         }
         if (q + 1 < nlev && !grid_barrier_bounded(bar, bar + 1, err, max_spin)) return;
@@ -474,7 +475,7 @@ __device__ __forceinline__ void face_terms_both(const ScalarSweepArgs<T> &a, int
     }
 }
 
-template <typename T, int NV, int NFV, int NDIMS, bool COHERENT>
+template <typename T, int NV, int NFV, int NDIMS, bool COHERENT, int FB>
 __device__ __forceinline__ void scalar_sweep_cell_both(const ScalarSweepArgs<T> &a, int t, int lo, int hi) {
     const long long ld = a.ld;
     const int i = a.cells ? __ldg(a.cells + t) : t;
@@ -487,7 +488,6 @@ __device__ __forceinline__ void scalar_sweep_cell_both(const ScalarSweepArgs<T> 
         df[k] = T(0);
     }
     const T rvi = a.rv ? __ldg(a.rv + i) : T(1);
-    constexpr int FB = 3;
     if (no_active_face(a, lo, hi)) {
     } else if (a.nface <= 2 * FB) {
         int nba[2 * FB];
@@ -509,12 +509,15 @@ __device__ __forceinline__ void scalar_sweep_cell_both(const ScalarSweepArgs<T> 
     for (int k = 0; k < NV; ++k) a.own_out[k * ld + i] = sweep_result(a.upper != 0, own[k], df[k], dg[k]);
 }
 
-// One level of both systems' sweeps, one thread per cell.
+// One level of both systems' sweeps, one thread per cell.  The builds
+// capped at 80 / 64 registers gather two active faces per step (three
+// otherwise), which keeps the 80-register build free of spills; the terms
+// are added in face order either way.
 template <typename T, int NV, int NFV, int NDIMS, int MINB = 1>
 __global__ void __launch_bounds__(256, MINB) scalar_sweep_both_kernel(ScalarSweepArgs<T> a) {
     const int t = a.t0 + blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= a.t1) return;
-    scalar_sweep_cell_both<T, NV, NFV, NDIMS>(a, t, a.lo, a.hi);
+    scalar_sweep_cell_both<T, NV, NFV, NDIMS, false, (MINB >= 3 ? 2 : 3)>(a, t, a.lo, a.hi);
 }
 
 // One level of the sweep with one thread per active face.  A block owns
