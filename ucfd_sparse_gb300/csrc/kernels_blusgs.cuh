@@ -241,6 +241,66 @@ __global__ void fs_blusgs_prepare_kernel(long long N, int P, const int *nei, con
         for (int e = 0; e < B2; ++e) dm[e] = D[::ucfd::tile_index(k, e, B2)];
     }
     const long long jbase = ::ucfd::tile_index(k, 0, (long long)P * B2);
+    if constexpr (kFold) {
+        // Fast build, two passes over the faces.  First the diagonal
+        // block from each record's diagonal half (side == 1: half 0, else
+        // half 1) only; then, with the block factored, each face's
+        // off-diagonal half becomes M = D^-1 J fv in registers and is
+        // stored once (no FP32 J stored, read back and rewritten).  Same
+        // values as forming J first.
+        for (int p = 0; p < P; ++p) {
+            if (nei[p * N + k] < 0) break;
+            const long long s = slot[p * N + k];
+            const bool pos = side[p * N + k] == 1;
+            const double fv = fa[p * N + k] * rv[k];
+            const double fvs = pos ? fv : -fv;
+            const double *hd = jt + s * R + (pos ? 0 : B2);
+#pragma unroll
+            for (int e = 0; e < B2; ++e) dm[e] += __ldg(hd + e) * fvs;  // == (pos ? h0 : -h1) * fv
+        }
+        const long long dbase = ::ucfd::tile_index(k, 0, B2);
+#pragma unroll
+        for (int e = 0; e < B2; ++e) D[dbase + (e << 5)] = dm[e];
+        ludcmp_dev<double, B, true, true>(dm);
+#pragma unroll
+        for (int e = 0; e < B2; ++e) {
+            if (LU64) LU64[dbase + (e << 5)] = dm[e];
+            if (LU_s) LU_s[dbase + (e << 5)] = (S)dm[e];
+        }
+        S lu[B2];
+#pragma unroll
+        for (int e = 0; e < B2; ++e) lu[e] = (S)dm[e];
+        for (int p = 0; p < P; ++p) {
+            if (nei[p * N + k] < 0) break;
+            const long long s = slot[p * N + k];
+            const bool pos = side[p * N + k] == 1;
+            const double fv = fa[p * N + k] * rv[k];
+            const unsigned neg = pos ? 0u : 0x80000000u;
+            const double *ho = jt + s * R + (pos ? B2 : 0);
+            S m[B2];
+#pragma unroll
+            for (int e = 0; e < B2; ++e) {
+                const double jv = xor_sign(__ldg(ho + e), neg);  // == pos ? h1 : -h0
+                const long long o = jbase + ((long long)(p * B2 + e) << 5);
+                if (J64) J64[o] = jv;
+                m[e] = (S)(jv * fv);
+            }
+            // M = D^-1 (J fv), column by column through the factors just
+            // formed (in the sweep precision)
+#pragma unroll
+            for (int c = 0; c < B; ++c) {
+                S col[B];
+#pragma unroll
+                for (int r = 0; r < B; ++r) col[r] = m[r * B + c];
+                lusub_dev<S, B, true>(lu, col);
+#pragma unroll
+                for (int r = 0; r < B; ++r) m[r * B + c] = col[r];
+            }
+#pragma unroll
+            for (int e = 0; e < B2; ++e) J_s[jbase + ((long long)(p * B2 + e) << 5)] = m[e];
+        }
+        return;
+    }
     for (int p = 0; p < P; ++p) {
         if (nei[p * N + k] < 0) break;
         const long long s = slot[p * N + k];
@@ -264,7 +324,7 @@ __global__ void fs_blusgs_prepare_kernel(long long N, int P, const int *nei, con
                 dm[c + r * B] += (pos ? h0 : h1) * fvs;    // == (pos ? h0 : -h1) * fv
                 const double jv = xor_sign(pos ? h1 : h0, neg);  // == pos ? h1 : -h0
                 const long long o = jbase + ((long long)(p * B2 + r * B + c) << 5);
-                J_s[o] = (S)(kFold ? jv * fv : jv);
+                J_s[o] = (S)jv;
                 if (J64) J64[o] = jv;
             }
         }
@@ -272,36 +332,11 @@ __global__ void fs_blusgs_prepare_kernel(long long N, int P, const int *nei, con
     const long long dbase = ::ucfd::tile_index(k, 0, B2);
 #pragma unroll
     for (int e = 0; e < B2; ++e) D[dbase + (e << 5)] = dm[e];
-    ludcmp_dev<double, B, kFold, kFold>(dm);
+    ludcmp_dev<double, B>(dm);
 #pragma unroll
     for (int e = 0; e < B2; ++e) {
         if (LU64) LU64[dbase + (e << 5)] = dm[e];
         if (LU_s) LU_s[dbase + (e << 5)] = (S)dm[e];
-    }
-    if constexpr (kFold) {
-        // the sweep blocks become M = D^-1 J fv, column by column through the
-        // factors just formed (in the sweep precision), so that a sweep is
-        // du_k = D^-1 rhs_k - sum_f M_f du_nb with no block solve per cell
-        S lu[B2];
-#pragma unroll
-        for (int e = 0; e < B2; ++e) lu[e] = (S)dm[e];
-        for (int p = 0; p < P; ++p) {
-            if (nei[p * N + k] < 0) break;
-            S m[B2];
-#pragma unroll
-            for (int e = 0; e < B2; ++e) m[e] = J_s[jbase + ((long long)(p * B2 + e) << 5)];
-#pragma unroll
-            for (int c = 0; c < B; ++c) {
-                S col[B];
-#pragma unroll
-                for (int r = 0; r < B; ++r) col[r] = m[r * B + c];
-                lusub_dev<S, B, true>(lu, col);
-#pragma unroll
-                for (int r = 0; r < B; ++r) m[r * B + c] = col[r];
-            }
-#pragma unroll
-            for (int e = 0; e < B2; ++e) J_s[jbase + ((long long)(p * B2 + e) << 5)] = m[e];
-        }
     }
 }
 
