@@ -1323,10 +1323,11 @@ def run_kernels(args):
     elt = 8 if prec != 2 else 4
     sw = 2 * sweep_bytes(case["rowptr"], elt, 5)
     # Prepare: jmat read twice (transpose in, face records out) + written once,
-    # face records read per cell-face, the sweep blocks written, read back and
-    # rewritten as D^-1 J fv, J64 (FP32 mode) / D / LU written, ELL index arrays
+    # face records read per cell-face (the diagonal half in the first pass,
+    # the off-diagonal half in the second), the sweep blocks D^-1 J fv written
+    # once, J64 (FP32 mode) / D / LU written, ELL index arrays read per pass
     jb = 25 * elt
-    prep_b = (nF * 400 * 3 + nnz * (400 + 3 * jb + (200 if prec == 2 else 0) + 4 + 4 + 1 + 8)
+    prep_b = (nF * 400 * 3 + nnz * (400 + jb + (200 if prec == 2 else 0) + 2 * (4 + 4 + 1 + 8))
               + N * (200 + 25 * elt + 8 + 8))
     res_b = nnz * (4 + 8 + 200) + N * (8 + 200 + 40 + 40 + 20)
     out = {"workload": "kernels", "unit": "ms", "config": {
