@@ -145,7 +145,10 @@ __global__ void __launch_bounds__(256) fingerprint_kernel(long long n, const int
 }
 
 // BLUSGSPreconPrepare: precon/blusgs.c:7-26 -- copy each diagonal block and
-// LU-factor it (FP64), optionally rounding the factors to Tl.
+// LU-factor it (FP64), optionally rounding the factors to Tl.  The fast
+// build (kFold) stores reciprocal pivots, so that the applies multiply
+// instead of dividing (FP64 division is a long sequence on GB300's narrow
+// FP64 pipe); the exact build keeps the reference's factors.
 template <typename Tl, int B>
 __global__ void pc_prepare_kernel(int bn, const int *perm, const long long *dslot,
                                   const double *values, double *LU64, Tl *LU_l, int factor) {
@@ -158,7 +161,7 @@ __global__ void pc_prepare_kernel(int bn, const int *perm, const long long *dslo
     for (int e = 0; e < B2; ++e) d[e] = values[s * B2 + e];
     // factor == 0: the diagonal block is already factorised (block ILU) or
     // kept as it is (scalar ILU)
-    if (factor) ludcmp_dev<double, B>(d);
+    if (factor) ludcmp_dev<double, B, kFold, kFold>(d);
 #pragma unroll
     for (int e = 0; e < B2; ++e) {
         LU64[(long long)e * bn + k] = d[e];
@@ -190,7 +193,7 @@ __global__ void __launch_bounds__(256) pc_lower_kernel(int t0, int t1, int bn, i
         T lu[B2];
 #pragma unroll
         for (int e = 0; e < B2; ++e) lu[e] = __ldg(LU + (long long)e * bn + k);
-        lusub_dev<T, B>(lu, arr);
+        lusub_dev<T, B, kFold>(lu, arr);  // reciprocal pivots in the fast build (pc_prepare)
     }
 #pragma unroll
     for (int r = 0; r < B; ++r) b[(long long)k * B + r] = arr[r];
@@ -219,7 +222,10 @@ __global__ void __launch_bounds__(256) pc_upper_kernel(int t0, int t1, int bn, i
         T lu[B2];
 #pragma unroll
         for (int e = 0; e < B2; ++e) lu[e] = __ldg(LU + (long long)e * bn + k);
-        lusub_dev<T, B>(lu, arr);
+        // the BLU-SGS factors carry reciprocal pivots in the fast build; the
+        // ILU factors come from the factorisation, as the reference stores them
+        if constexpr (MODE == PC_BLUSGS) lusub_dev<T, B, kFold>(lu, arr);
+        else lusub_dev<T, B>(lu, arr);
     }
 #pragma unroll
     for (int r = 0; r < B; ++r) {
