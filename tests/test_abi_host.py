@@ -189,3 +189,19 @@ def test_oracle_colouring_equals_native(ucfd, port):
         np.testing.assert_array_equal(ic, ic2)
         np.testing.assert_array_equal(lc, lc2)
         assert rg == rg2
+
+
+def test_host_array_access_setting(ucfd):
+    """UCFDSetHostArrayAccess / UCFDGetHostArrayAccess: process-wide, in-place
+    reads of page-locked host Jacobians (UCFD_HOST_MAP) by default; unknown
+    modes are rejected with UCFD_ERR_ARGUMENT and leave the setting alone."""
+    from ucfd_sparse_gb300 import lib
+    assert lib.host_array_access() == lib.HOST_MAP
+    try:
+        lib.set_host_array_access(lib.HOST_STAGE)
+        assert lib.host_array_access() == lib.HOST_STAGE
+        assert ucfd.UCFDSetHostArrayAccess(5) == 2 and "UCFD_HOST" in lib.last_error()
+        assert lib.host_array_access() == lib.HOST_STAGE
+    finally:
+        lib.set_host_array_access(lib.HOST_MAP)
+    assert lib.host_array_access() == lib.HOST_MAP
