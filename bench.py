@@ -541,7 +541,11 @@ def run_gpu(args):
                 "algorithmic_bytes_per_launch": launch_bytes, "launch_ms": sweep_ms / nlev,
                 "traffic_source": f"ncu 96^3 capture of a sweep pair, {SWEEP_TRAFFIC_PER_CELL} B per cell update, "
                                   "scaled by cells per launch",
-                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s"}
+                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if peaks else "fallback 6.8 TB/s",
+                "pair_ms": 2 * sweep_ms,
+                "algorithmic_bytes_per_cell_update": bytes_sweep / N,
+                "bytes_note": "split-sum sweeps: every neighbour index each sweep, each face block once per "
+                              "lower+upper pair (in the sweep that updates its side), 5 vectors per cell"}
 
     # ---- error of one step against the FP64 arithmetic of the oracle --------
     # (UCFD_PREC_FP64 runs the reference's operation order, bit-identical to
