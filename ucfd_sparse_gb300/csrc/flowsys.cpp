@@ -41,6 +41,8 @@ struct Work {
     DevBuf<S> ulo;                         // FP32 mode: low part of the float-float state u + ulo (UCFDLUSGS_Run)
     DevBuf<S> crhs;                        // fast modes: D^-1 rhs, the block sweeps' right-hand side
     DevBuf<S> spart;                       // fast modes: each block sweep's own-side sums (SweepSplit)
+    DevBuf<float4> geo4;                   // FP32 run loop with both systems: (normal, fa * rv) per cell-face
+    DevBuf<float2> lam2;                   // and (lam, tlam) per cell-face
 };
 
 // Which increments the fast block sweeps' stored sums (Work::spart) belong
@@ -322,8 +324,10 @@ void ensure_face_lists(FlowSys s) {
 
 // sys: 0 the mean-flow system, 1 the turbulence system, 2 both in one pass
 // (one thread per cell; the run loop's choice, see run_sweeps_both).
+// packed: the run loop's sweep of both systems in FP32 reads the packed
+// per cell-face geometry and spectral radii that run_gather_lambda formed.
 template <typename S, bool EX>
-void lusgs_sweep(FlowSys s, int sys, bool upper, double kappa, bool persistent = false) {
+void lusgs_sweep(FlowSys s, int sys, bool upper, double kappa, bool persistent = false, bool packed = false) {
     const bool rans = sys == 1;
     Work<S> &w = work<S>(s);
     const long long N = s->N;
@@ -338,6 +342,10 @@ void lusgs_sweep(FlowSys s, int sys, bool upper, double kappa, bool persistent =
     a.nrm = w.nrm.p;
     a.lam = rans ? w.lamT.p : w.lamN.p;
     a.tlam = sys == 2 ? w.lamT.p : nullptr;
+    if (sys == 2 && packed && w.geo4.p && w.lam2.p) {
+        a.geo4 = w.geo4.p;
+        a.lam2 = w.lam2.p;
+    }
     a.u = w.u.p;
     a.nbsrc = w.du.p;
     a.own_in = w.du.p;
@@ -557,8 +565,8 @@ void lusgs_iteration(FlowSys s, bool rans, double kappa, double *resid_slot, boo
     if (rans && run_sweeps_both(s, persistent)) {
         KCALL(EX, fs_lusgs_prepare_both<S>, s->N, s->P, s->nfvars, s->nvars, (S)kappa, s->d_nei.p, geo_fa<S>(s),
               geo_rv<S>(s), w.lamN.p, w.lamT.p, w.base.p, w.diag.p, st);
-        lusgs_sweep<S, EX>(s, 2, false, kappa, persistent);
-        lusgs_sweep<S, EX>(s, 2, true, kappa, persistent);
+        lusgs_sweep<S, EX>(s, 2, false, kappa, persistent, true);
+        lusgs_sweep<S, EX>(s, 2, true, kappa, persistent, true);
     } else {
         lusgs_prepare<S, EX>(s, false, kappa, w.base.p);
         lusgs_sweep<S, EX>(s, 0, false, kappa, persistent);
@@ -600,6 +608,18 @@ void run_gather_lambda(FlowSys s, bool rans, int niter) {
         w.lamT.ensure((size_t)s->P * s->N);
         kfast::gather_idx<S>((long long)s->P * s->N, s->d_slot.p, device_view<double>(s->tfspr, s->nfaces, stage, st),
                              w.lamT.p, st);
+        if constexpr (std::is_same<S, float>::value) {
+            // FP32 loop sweeping both systems: the geometry (fixed with the
+            // mesh) and both spectral radii packed per cell-face, so a face
+            // costs two vector loads instead of six
+            const long long nl = (long long)s->P * s->N;
+            if (!w.geo4.p) {
+                w.geo4.ensure((size_t)nl);
+                kfast::pack_geo4(s->N, s->P, s->ndims, w.nrm.p, geo_fa<S>(s), geo_rv<S>(s), w.geo4.p, st);
+            }
+            w.lam2.ensure((size_t)nl);
+            kfast::pack_lam2(nl, w.lamN.p, w.lamT.p, w.lam2.p, st);
+        }
     }
 }
 

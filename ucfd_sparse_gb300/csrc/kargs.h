@@ -48,6 +48,9 @@ struct ScalarSweepArgs {
     const T *lam;          // [nface][ld] spectral radius
     const T *tlam;         // [nface][ld] spectral radius of the turbulence system when one launch
                            // sweeps both systems (rans == 2), else unused
+    const void *geo4;      // FP32, both systems: float4 [nface][ld] (normal, fa * rv) per cell-face,
+                           // read instead of nrm / fa / rv (nullptr: not packed)
+    const void *lam2;      // with geo4: float2 [nface][ld] (lam, tlam) per cell-face
     const T *u;            // [nvars][ld]
     const T *nbsrc;        // [nvars][ld] neighbour increments
     const T *own_in;       // [nvars][ld]

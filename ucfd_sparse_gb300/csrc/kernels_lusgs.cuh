@@ -452,6 +452,21 @@ __device__ __forceinline__ void face_terms_both(const ScalarSweepArgs<T> &a, int
 #pragma unroll
         for (int j = 0; j < NV; ++j) dn[k][j] = COHERENT ? __ldcg(a.nbsrc + j * ld + g) : a.nbsrc[j * ld + g];
         const int f = fk[k];
+        if constexpr (sizeof(T) == 4) {
+            if (a.geo4) {
+                // packed per cell-face: (normal, fa * rv) and (lam, tlam),
+                // two vector loads instead of six
+                const float4 gq = __ldg(static_cast<const float4 *>(a.geo4) + f * ld + i);
+                const float2 l = __ldg(static_cast<const float2 *>(a.lam2) + f * ld + i);
+                nf[k][0] = gq.x;
+                if constexpr (NDIMS > 1) nf[k][1] = gq.y;
+                if constexpr (NDIMS > 2) nf[k][2] = gq.z;
+                fv[k] = gq.w;
+                kl[k] = l.x;
+                klt[k] = l.y;
+                continue;
+            }
+        }
 #pragma unroll
         for (int d = 0; d < NDIMS; ++d) nf[k][d] = __ldg(a.nrm + (f * NDIMS + d) * ld + i);
         fv[k] = __ldg(a.fa + f * ld + i);
@@ -461,7 +476,8 @@ __device__ __forceinline__ void face_terms_both(const ScalarSweepArgs<T> &a, int
 #pragma unroll
     for (int k = 0; k < KB; ++k) {
         if (!on[k]) continue;
-        const T fvk = a.rv ? fv[k] * rvi : fv[k];
+        // packed geometry holds the product fa * rv itself (the same rounding)
+        const T fvk = a.rv && !a.geo4 ? fv[k] * rvi : fv[k];
         T tn[NFV], tt[NV - NFV];
         // the mean-flow flux may raise the energy of uu[k] to the pressure
         // floor (as its own sweep does to its copy); the turbulence flux
@@ -487,7 +503,7 @@ __device__ __forceinline__ void scalar_sweep_cell_both(const ScalarSweepArgs<T> 
         dg[k] = a.diag[k * a.diag_vs + i];
         df[k] = T(0);
     }
-    const T rvi = a.rv ? __ldg(a.rv + i) : T(1);
+    const T rvi = a.rv && !a.geo4 ? __ldg(a.rv + i) : T(1);  // packed geometry carries fa * rv
     if (no_active_face(a, lo, hi)) {
     } else if (a.nface <= 2 * FB) {
         int nba[2 * FB];
@@ -600,6 +616,28 @@ __global__ void face_list_geo_kernel(long long E, long long ld, int ndims, const
         for (int d = 0; d < 3; ++d) geo[4 * e + d] = d < ndims ? nrm[(p * ndims + d) * ld + k] : T(0);
         geo[4 * e + 3] = rv ? fa[qq] * rv[k] : fa[qq];
     }
+}
+
+// Packed geometry of the FP32 run loop with both systems, per cell-face
+// (p, k): (outward normal, zero-padded to 3 components; fa * rv).
+__global__ void pack_geo4_kernel(long long N, int P, int ndims, const float *nrm, const float *fa, const float *rv,
+                                 float4 *geo4) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < (long long)P * N;
+         e += (long long)gridDim.x * blockDim.x) {
+        const long long p = e / N, k = e - p * N;
+        float4 g;
+        g.x = nrm[(p * ndims + 0) * N + k];
+        g.y = ndims > 1 ? nrm[(p * ndims + 1) * N + k] : 0.f;
+        g.z = ndims > 2 ? nrm[(p * ndims + 2) * N + k] : 0.f;
+        g.w = rv ? fa[e] * rv[k] : fa[e];
+        geo4[e] = g;
+    }
+}
+
+// (lam, tlam) per cell-face for the same loop.
+__global__ void pack_lam2_kernel(long long n, const float *lam, const float *tlam, float2 *lam2) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+        lam2[e] = make_float2(lam[e], tlam[e]);
 }
 
 // Two threads per cell (ELL width <= 6, level-major or coloured): the even

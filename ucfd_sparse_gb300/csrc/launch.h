@@ -25,6 +25,9 @@
     template <typename T>                                                                          \
     void face_list_geo(long long E, long long ld, int ndims, const int *q, const T *nrm,           \
                        const T *fa, const T *rv, T *geo, cudaStream_t s);                          \
+    void pack_geo4(long long N, int P, int ndims, const float *nrm, const float *fa,               \
+                   const float *rv, void *geo4, cudaStream_t s);                                   \
+    void pack_lam2(long long n, const float *lam, const float *tlam, void *lam2, cudaStream_t s);  \
     template <typename T>                                                                          \
     void legacy_pre(int neles, int nface, T factor, const T *fnorm_vol, const T *dt, T *diag,      \
                     const T *fspr, cudaStream_t s);                                                \

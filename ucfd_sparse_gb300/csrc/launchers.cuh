@@ -54,6 +54,22 @@ void face_list_geo(long long E, long long ld, int ndims, const int *q, const T *
                                                                                           rv, geo);
 }
 
+void pack_geo4(long long N, int P, int ndims, const float *nrm, const float *fa, const float *rv, void *geo4,
+               cudaStream_t s) {
+    const long long n = (long long)P * N;
+    if (n <= 0) return;
+    const long long g = (n + kBlock - 1) / kBlock;
+    pack_geo4_kernel<<<(unsigned)(g < 65535 * 16 ? g : 65535 * 16), kBlock, 0, s>>>(N, P, ndims, nrm, fa, rv,
+                                                                                   static_cast<float4 *>(geo4));
+}
+
+void pack_lam2(long long n, const float *lam, const float *tlam, void *lam2, cudaStream_t s) {
+    if (n <= 0) return;
+    const long long g = (n + kBlock - 1) / kBlock;
+    pack_lam2_kernel<<<(unsigned)(g < 65535 * 16 ? g : 65535 * 16), kBlock, 0, s>>>(n, lam, tlam,
+                                                                                   static_cast<float2 *>(lam2));
+}
+
 template <typename T, int NV, int NFV, int NDIMS, bool RANS>
 static void sweep_go(const ::ucfd::ScalarSweepArgs<T> &a, int block, cudaStream_t s) {
     const long long n = a.t1 - a.t0;
