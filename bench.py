@@ -794,6 +794,7 @@ def run_lusgs(args):
             # the loop's sweep with the turbulence system: both systems in one
             # pass (one thread per cell), or the RANS sweep after the NS sweep
             res["rans_sweep_ms"] = lower_ms(S.lusgs_rans_lower)
+            S.lusgs_nsrans_prepare(1.0)  # the packed face data the loop's sweep reads
             res["nsrans_sweep_ms"] = lower_ms(S.lusgs_nsrans_lower)
             cand = {}
             for var in (0, 1, 2, 3, 5):

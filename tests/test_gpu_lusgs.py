@@ -296,6 +296,45 @@ def test_nsrans_calls_bitexact(name, variant, golden, ucfd):
     np.testing.assert_array_equal(e["upts"].cpu().numpy(), arr[f"{name}_upts"])
 
 
+@pytest.mark.parametrize("prec", [1, 2])
+def test_nsrans_calls_equal_separate_calls(prec, ucfd):
+    """In the fast modes too, NSRANSPrepare / NSRANSLowerSweep /
+    NSRANSUpperSweep (in FP32 on the packed per cell-face geometry and
+    spectral radii) give the values of the six NS and RANS calls, bit for
+    bit, also when a separate NSPrepare comes in between."""
+    kw = cases.FLOWSYS["fs5"]
+    fs, inp = cases.flowsys_case(**kw)
+    outs = []
+    for calls in ("both", "separate", "both_after_ns"):
+        S, e = make_flowsys(fs, inp, prec=prec, on_device=True)
+        S.set_launch_config(threads_per_block=128, sweep_variant=0)
+        for _ in range(2):
+            S.lusgs_pack(0, kw["turb_factor"], kw["a0"])
+            if calls == "separate":
+                S.lusgs_ns_prepare(kw["kappa"])
+                S.lusgs_rans_prepare(kw["kappa"])
+                S.lusgs_ns_lower(kw["kappa"])
+                S.lusgs_ns_upper(kw["kappa"])
+                S.lusgs_rans_lower(kw["kappa"])
+                S.lusgs_rans_upper(kw["kappa"])
+            else:
+                S.lusgs_nsrans_prepare(kw["kappa"])
+                if calls == "both_after_ns":
+                    # a separate Prepare afterwards re-gathers one system's
+                    # radii: the packed copy must not be used for the next sweeps
+                    S.lusgs_pack(0, kw["turb_factor"], kw["a0"])
+                    S.lusgs_ns_prepare(kw["kappa"])
+                    S.lusgs_rans_prepare(kw["kappa"])
+                S.lusgs_nsrans_lower(kw["kappa"])
+                S.lusgs_nsrans_upper(kw["kappa"])
+            S.lusgs_update(0)
+        outs.append(e["upts"].cpu().numpy())
+        S.destroy()
+    assert np.abs(outs[0] - inp["upts"]).max() > 0
+    np.testing.assert_array_equal(outs[0], outs[1])
+    np.testing.assert_array_equal(outs[2], outs[1])
+
+
 @pytest.mark.parametrize("prec", [0, 1, 2])
 def test_run_loop_both_systems_equal_separate_sweeps(prec, ucfd):
     """The loop's one-pass sweeps of both systems (one thread per cell:

@@ -97,6 +97,7 @@ struct _FlowSys {
     SplitState split[2];           // NS / turbulence rows of the fast block sweeps
     unsigned jver[2] = {1, 1};     // Prepare count of the NS / turbulence blocks
     bool has_self = false;         // some CSR row lists itself
+    bool lam2_ok = false;          // Work::lam2 packs the current NS and RANS spectral radii (FP32)
     DevBuf<double> part, red, resid;
     PinnedBuf<double> h_red;
 
@@ -342,7 +343,7 @@ void lusgs_sweep(FlowSys s, int sys, bool upper, double kappa, bool persistent =
     a.nrm = w.nrm.p;
     a.lam = rans ? w.lamT.p : w.lamN.p;
     a.tlam = sys == 2 ? w.lamT.p : nullptr;
-    if (sys == 2 && packed && w.geo4.p && w.lam2.p) {
+    if (sys == 2 && packed && s->lam2_ok && w.geo4.p && w.lam2.p) {
         a.geo4 = w.geo4.p;
         a.lam2 = w.lam2.p;
     }
@@ -591,6 +592,23 @@ void run_graph_drop(FlowSys s) {
     s->run_exec = nullptr;
 }
 
+// The packed per cell-face geometry and both spectral radii of the FP32
+// sweeps of both systems, from lamN and lamT as just gathered.
+template <typename S>
+void pack_both(FlowSys s, cudaStream_t st) {
+    if constexpr (std::is_same<S, float>::value) {
+        Work<S> &w = work<S>(s);
+        const long long nl = (long long)s->P * s->N;
+        if (!w.geo4.p) {
+            w.geo4.ensure((size_t)nl);
+            kfast::pack_geo4(s->N, s->P, s->ndims, w.nrm.p, geo_fa<S>(s), geo_rv<S>(s), w.geo4.p, st);
+        }
+        w.lam2.ensure((size_t)nl);
+        kfast::pack_lam2(nl, w.lamN.p, w.lamT.p, w.lam2.p, st);
+        s->lam2_ok = true;
+    }
+}
+
 // Spectral radii of the loop, gathered from the face arrays (fspr / tfspr)
 // into the ELL layout, and the scratch of the loop's norms.
 template <typename S>
@@ -604,24 +622,18 @@ void run_gather_lambda(FlowSys s, bool rans, int niter) {
     w.lamN.ensure((size_t)s->P * s->N);
     kfast::gather_idx<S>((long long)s->P * s->N, s->d_slot.p, device_view<double>(s->fspr, s->nfaces, stage, st),
                          w.lamN.p, st);
+    s->lam2_ok = false;
     if (rans) {
         w.lamT.ensure((size_t)s->P * s->N);
         kfast::gather_idx<S>((long long)s->P * s->N, s->d_slot.p, device_view<double>(s->tfspr, s->nfaces, stage, st),
                              w.lamT.p, st);
-        if constexpr (std::is_same<S, float>::value) {
-            // FP32 loop sweeping both systems: the geometry (fixed with the
-            // mesh) and both spectral radii packed per cell-face, so a face
-            // costs two vector loads instead of six
-            const long long nl = (long long)s->P * s->N;
-            if (!w.geo4.p) {
-                w.geo4.ensure((size_t)nl);
-                kfast::pack_geo4(s->N, s->P, s->ndims, w.nrm.p, geo_fa<S>(s), geo_rv<S>(s), w.geo4.p, st);
-            }
-            w.lam2.ensure((size_t)nl);
-            kfast::pack_lam2(nl, w.lamN.p, w.lamT.p, w.lam2.p, st);
-        }
+        // FP32 loop sweeping both systems: the geometry (fixed with the mesh)
+        // and both spectral radii packed per cell-face, so a face costs two
+        // vector loads instead of six
+        pack_both<S>(s, st);
     }
 }
+
 
 // One iteration captured once per (rans, kappa, launch shape) and replayed.
 template <typename S, bool EX>
@@ -1101,11 +1113,14 @@ static ucfd_status_t lusgs_prepare_api(FlowSys s, int sys, UCFDReal kappa) {
             w.lamT.ensure((size_t)nl);
             kfast::gather_idx<S>(nl, s->d_slot.p, lfT, w.lamT.p, st);
         }
-        if (sys == 2)
+        s->lam2_ok = false;
+        if (sys == 2) {
             KCALL(EX, fs_lusgs_prepare_both<S>, s->N, s->P, s->nfvars, s->nvars, (S)kappa, s->d_nei.p, geo_fa<S>(s),
                   geo_rv<S>(s), w.lamN.p, w.lamT.p, (const S *)nullptr, w.diag.p, st);
-        else
+            pack_both<S>(s, st);
+        } else {
             lusgs_prepare<S, EX>(s, sys == 1, kappa, nullptr);
+        }
     });
     finish(s, (lfN && !is_device_ptr(s->fspr)) || (lfT && !is_device_ptr(s->tfspr)));
     UCFD_API_END
@@ -1127,7 +1142,7 @@ static ucfd_status_t lusgs_sweep_api(FlowSys s, int sys, bool upper, UCFDReal ka
             lusgs_sweep<S, EX>(s, 0, upper, kappa);
             lusgs_sweep<S, EX>(s, 1, upper, kappa);
         } else {
-            lusgs_sweep<S, EX>(s, sys, upper, kappa);
+            lusgs_sweep<S, EX>(s, sys, upper, kappa, false, sys == 2);
         }
     });
     finish(s);
