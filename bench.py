@@ -715,6 +715,18 @@ def lusgs_iter_bytes(rowptr, elt, nfv=5, nt=1, both=False):
     return nnz * per_face + N * per_cell
 
 
+def nsrans_sweep_bytes(rowptr, nfv=5, nt=1, elt=4):
+    """Algorithmic bytes of one sweep of both scalar systems (the loop's
+    one-pass kernel): per cell-face the neighbour index, area, both spectral
+    radii and the normal; per cell rcp_vol, the mean-flow state values the
+    fluxes read, du of every variable (own and neighbours' once), du written
+    and diag -- 264 B per hex cell in FP32."""
+    nnz = int(rowptr[-1])
+    N = rowptr.shape[0] - 1
+    nv = nfv + nt
+    return nnz * (4 + (3 + 3) * elt) + N * (elt + nfv * elt + 3 * nv * elt)
+
+
 def run_lusgs(args):
     """Steady pseudo-time loop: jittered, permuted hex, nvars = 5 + 1 RANS,
     FP32 state, greedy colouring; args.iters iterations as a captured CUDA
@@ -844,10 +856,7 @@ def run_lusgs(args):
     # per cell rcp_vol and 4 x nvars state values (u and du of neighbours as
     # other cells' own data, du read and written, diag) -- 228 B/cell on hex
     ns_bytes = nnz * (4 + (2 + 3) * 4) + N * (4 + 4 * 5 * 4)
-    # both systems: per cell-face also the turbulence spectral radius; per
-    # cell the 5 mean-flow state values the fluxes read and du (own + nbr),
-    # du written and diag of all 6 variables -- 264 B/cell on hex
-    both_bytes = nnz * (4 + (3 + 3) * 4) + N * (4 + 5 * 4 + 3 * 6 * 4)
+    both_bytes = nsrans_sweep_bytes(rp)
     sweep_bytes_, sweep_ms_ = (both_bytes, res["nsrans_sweep_ms"]) if both else (ns_bytes, res["sweep_ms"])
     out = {"workload": "lusgs", "metric": METRIC, "unit": UNIT,
            "config": {"workload": f"scalar LU-SGS pseudo-time loop, {m}^3 jittered permuted hex ({N} cells), "

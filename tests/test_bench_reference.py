@@ -34,3 +34,14 @@ def test_cpu_step_composition_and_sweep_bytes():
     rowptr = np.arange(0, 6 * 11, 6)              # 10 cells of 6 faces each
     assert bench.sweep_bytes(rowptr, 4, 5) == 10 * 424
     assert bench.sweep_bytes(rowptr, 8, 5) == 10 * 824
+
+
+def test_scalar_loop_byte_counts():
+    """One sweep of both scalar systems moves 264 B per interior hex cell
+    (6 faces x 28 B, 4 + 20 + 72 B per cell); the loop's iteration with the
+    one-pass kernels moves fewer bytes than with separate NS and RANS ones."""
+    import numpy as np
+    import bench
+    rowptr = np.arange(0, 6 * 11, 6)              # 10 cells of 6 faces each
+    assert bench.nsrans_sweep_bytes(rowptr) == 10 * 264
+    assert bench.lusgs_iter_bytes(rowptr, 4, both=True) < bench.lusgs_iter_bytes(rowptr, 4)
